@@ -10,9 +10,12 @@
 // interaction-list sets, ACA ranks and pivots, and the matvec to rounding.
 //
 // Arithmetic is kept free of fused multiply-adds (built with
-// -ffp-contract=off) and every reduction runs sequentially in index order, so
-// the ACA pivots are reproducible bit for bit across hosts.
+// -ffp-contract=off).  The ACA's norms and dot products use the canonical
+// reduction order of canonical_sum.h (the order of the CUDA kernels); the
+// other reductions run sequentially in index order.  Ranks and pivots are
+// therefore reproducible bit for bit on every host and on the GPU.
 #include "hodlr3d_oracle.h"
+#include "canonical_sum.h"
 
 #include <algorithm>
 #include <cmath>
@@ -308,15 +311,11 @@ inline int argmax_abs(const std::vector<double>& v, const std::vector<char>& use
 }
 
 inline double seq_norm(const std::vector<double>& v) {
-  double s = 0.0;
-  for (double e : v) s += e * e;
-  return std::sqrt(s);
+  return std::sqrt(hodlr3d_canonical_sum([&](long i) { return v[i] * v[i]; }, (long)v.size()));
 }
 
 inline double seq_dot(const double* a, const std::vector<double>& b) {
-  double s = 0.0;
-  for (size_t i = 0; i < b.size(); ++i) s += a[i] * b[i];
-  return s;
+  return hodlr3d_canonical_sum([&](long i) { return a[i] * b[i]; }, (long)b.size());
 }
 
 // Partially pivoted ACA of the block K(rows, cols)
