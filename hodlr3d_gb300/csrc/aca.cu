@@ -1,0 +1,316 @@
+// Batched partially pivoted ACA: one thread block per interaction-list pair,
+// persistent blocks pulling pairs (largest first) from a work counter.
+//
+// Reference: LowRank::ACA_only_nodesCUR (src/ACA.cpp:127-238) driven by
+// HODLR3DTree::getUVtTree / getUVtInstance (src/HODLR3DTree.cpp:1621-1645).
+// The kept factors are the ACA's residual vectors: U = [u_1..u_r] (n x r) and
+// V = [v_1..v_r] (m x r), column-major, so that K(box, source) ~ U V^T; the
+// reference's CUR form Ac R^-1 L^-1 Ar is the same product (Ac R^-1 = U and
+// L^-1 Ar = V^T with L(i,j) = U(row_i, j), R(j,i) = V(col_i, j)).
+//
+// Bit-exactness: kernel entries and residual rows/columns are evaluated with
+// the reference's operation order and no fused multiply-adds; norms and dot
+// products use the canonical reduction order; pivots are first maxima.  The
+// CPU checker reproduces the same ranks and pivots.
+#include "aca.h"
+#include "common.cuh"
+
+namespace h3d {
+
+struct AcaShared {
+  double red_v[32];
+  int red_i[32];
+  int flag_bad;
+  int ctl_break;
+  int row_index, col_index, next_row;
+  double nu, nv, normS;
+};
+
+template <int BS>
+__device__ __forceinline__ void block_argmax(double v, int i, AcaShared& S, double& out_v,
+                                             int& out_i) {
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  warp_argmax(v, i);
+  if (lane == 0) {
+    S.red_v[w] = v;
+    S.red_i[w] = i;
+  }
+  __syncthreads();
+  if (w == 0) {
+    double vv = lane < BS / 32 ? S.red_v[lane] : 0.0;
+    int ii = lane < BS / 32 ? S.red_i[lane] : -1;
+    warp_argmax(vv, ii);
+    if (lane == 0) {
+      S.red_v[0] = vv;
+      S.red_i[0] = ii;
+    }
+  }
+  __syncthreads();
+  out_v = S.red_v[0];
+  out_i = S.red_i[0];
+  __syncthreads();
+}
+
+// Residual row at `row` with r previous terms -> V[:, r]; returns the first
+// maximum of |row| over unused columns.
+template <int BS>
+__device__ void row_pass(const AcaTask& T, const PointsF64& P, const KernelDesc& kd, int row,
+                         int r, const double* __restrict__ ubuf, const double* __restrict__ U,
+                         double* __restrict__ V, const unsigned char* __restrict__ used_c,
+                         AcaShared& S, double& amax, int& aidx) {
+  const double xi = P.x[T.t0 + row], yi = P.y[T.t0 + row], zi = P.z[T.t0 + row];
+  double bv = 0.0;
+  int bi = -1;
+  bool bad = false;
+  for (int s = threadIdx.x; s < T.m; s += BS) {
+    const int q = T.s0 + s;
+    double e = entry64_offdiag(kd, __dsub_rn(xi, P.x[q]), __dsub_rn(yi, P.y[q]),
+                               __dsub_rn(zi, P.z[q]));
+    for (int l = 0; l < r; ++l) e = __dsub_rn(e, __dmul_rn(ubuf[l], V[(size_t)l * T.m + s]));
+    V[(size_t)r * T.m + s] = e;
+    if (!isfinite(e)) bad = true;
+    if (!used_c[s]) argmax_merge(bv, bi, fabs(e), s);
+  }
+  if (bad) S.flag_bad = 1;
+  block_argmax<BS>(bv, bi, S, amax, aidx);
+}
+
+// Residual column at `col` with r previous terms, divided by the pivot ->
+// U[:, r]; returns the first maximum of |column| over unused rows.
+template <int BS>
+__device__ void col_pass(const AcaTask& T, const PointsF64& P, const KernelDesc& kd, int col,
+                         int r, double pivot, const double* __restrict__ vbuf,
+                         double* __restrict__ U, const unsigned char* __restrict__ used_r,
+                         AcaShared& S, double& amax, int& aidx) {
+  const int qc = T.s0 + col;
+  const double xj = P.x[qc], yj = P.y[qc], zj = P.z[qc];
+  double bv = 0.0;
+  int bi = -1;
+  bool bad = false;
+  for (int t = threadIdx.x; t < T.n; t += BS) {
+    const int q = T.t0 + t;
+    double e = entry64_offdiag(kd, __dsub_rn(P.x[q], xj), __dsub_rn(P.y[q], yj),
+                               __dsub_rn(P.z[q], zj));
+    for (int l = 0; l < r; ++l) e = __dsub_rn(e, __dmul_rn(vbuf[l], U[(size_t)l * T.n + t]));
+    const double u = __ddiv_rn(e, pivot);
+    U[(size_t)r * T.n + t] = u;
+    if (!isfinite(u)) bad = true;
+    if (!used_r[t]) argmax_merge(bv, bi, fabs(e), t);
+  }
+  if (bad) S.flag_bad = 1;
+  block_argmax<BS>(bv, bi, S, amax, aidx);
+}
+
+template <int BS>
+__global__ void __launch_bounds__(BS) k_aca(const AcaTask* __restrict__ tasks, int ntasks,
+                                            int* __restrict__ counter, PointsF64 P, KernelDesc kd,
+                                            double tol, double* __restrict__ ws,
+                                            unsigned char* __restrict__ flags,
+                                            int32_t* __restrict__ piv, int32_t* __restrict__ out_rank,
+                                            int32_t* __restrict__ out_status) {
+  extern __shared__ double dyn[];
+  __shared__ AcaShared S;
+  __shared__ int s_task;
+  constexpr int NW = BS / 32;
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  for (;;) {
+    if (tid == 0) s_task = atomicAdd(counter, 1);
+    __syncthreads();
+    const int ti = s_task;
+    __syncthreads();
+    if (ti >= ntasks) break;
+    const AcaTask T = tasks[ti];
+    double* ubuf = dyn;
+    double* vbuf = dyn + T.cap;
+    double* du = dyn + 2 * T.cap;
+    double* dv = dyn + 3 * T.cap;
+    double* U = ws + T.ws_off;
+    double* V = U + (size_t)T.cap * T.n;
+    unsigned char* used_r = flags + T.fl_off;
+    unsigned char* used_c = used_r + T.n;
+    int32_t* rows = piv + T.piv_off;
+    int32_t* cols = rows + T.cap;
+    const int mn = min(T.n, T.m);
+    if (mn == 0 || T.cap == 0) {
+      if (tid == 0) {
+        out_rank[ti] = 0;
+        out_status[ti] = mn == 0 ? 0 : 1;
+      }
+      continue;
+    }
+    for (int i = tid; i < T.n + T.m; i += BS) used_r[i] = 0;
+    if (tid == 0) S.flag_bad = 0;
+    __syncthreads();
+    // first row with a maximum above 1e-16 (src/ACA.cpp:153-161)
+    double amax;
+    int aidx;
+    int row_index = -1, col_index = -1;
+    for (int l = 0; l < T.n; ++l) {
+      row_pass<BS>(T, P, kd, l, 0, ubuf, U, V, used_c, S, amax, aidx);
+      if (amax > 1e-16) {
+        row_index = l;
+        col_index = aidx;
+        break;
+      }
+    }
+    int status = 0;
+    int r = 0;
+    if (row_index >= 0) {
+      const double pivot0 = V[col_index];
+      if (tid == 0) used_r[row_index] = 1;
+      __syncthreads();
+      col_pass<BS>(T, P, kd, col_index, 0, pivot0, vbuf, U, used_r, S, amax, aidx);
+      if (tid == 0) {
+        rows[0] = row_index;
+        cols[0] = col_index;
+        used_c[col_index] = 1;
+      }
+      int next_row = aidx;
+      r = 1;
+      // norms of the first pair of vectors (loop test, src/ACA.cpp:178)
+      if (w == 0) {
+        const double s2 = warp_canonical_dot(U, U, T.n, lane);
+        if (lane == 0) S.nu = sqrt(s2);
+      }
+      if (w == (NW > 1 ? 1 : 0)) {
+        const double s2 = warp_canonical_dot(V, V, T.m, lane);
+        if (lane == 0) S.nv = sqrt(s2);
+      }
+      if (tid == 0) S.normS = 0.0;
+      __syncthreads();
+      row_index = next_row;
+      for (;;) {
+        if (S.flag_bad) {
+          status = 2;
+          break;
+        }
+        if (!(__dmul_rn(S.nu, S.nv) > __dmul_rn(tol, S.normS) && r < mn)) break;
+        if (r >= T.cap) {
+          status = 1;
+          break;
+        }
+        for (int l = tid; l < r; l += BS) ubuf[l] = U[(size_t)l * T.n + row_index];
+        __syncthreads();
+        row_pass<BS>(T, P, kd, row_index, r, ubuf, U, V, used_c, S, amax, aidx);
+        col_index = aidx;
+        const double pivot = V[(size_t)r * T.m + col_index];
+        for (int l = tid; l < r; l += BS) vbuf[l] = V[(size_t)l * T.m + col_index];
+        if (tid == 0) used_r[row_index] = 1;
+        __syncthreads();
+        col_pass<BS>(T, P, kd, col_index, r, pivot, vbuf, U, used_r, S, amax, aidx);
+        next_row = aidx;
+        const double* un = U + (size_t)r * T.n;
+        const double* vn = V + (size_t)r * T.m;
+        double nu2 = 0.0, nv2 = 0.0;
+        if (w == 0) {
+          nu2 = warp_canonical_dot(un, un, T.n, lane);
+          if (lane == 0) {
+            du[r] = nu2;
+            S.nu = sqrt(nu2);
+          }
+        }
+        if (w == (NW > 1 ? 1 : 0)) {
+          nv2 = warp_canonical_dot(vn, vn, T.m, lane);
+          if (lane == 0) {
+            dv[r] = nv2;
+            S.nv = sqrt(nv2);
+          }
+        }
+        __syncthreads();
+        if (S.flag_bad) {
+          status = 2;
+          break;
+        }
+        if (S.nu < 1e-16 || S.nv < 1e-16) break;  // src/ACA.cpp:199-203
+        if (tid == 0) {
+          rows[r] = row_index;
+          cols[r] = col_index;
+          used_c[col_index] = 1;
+        }
+        // dot products with every kept vector (src/ACA.cpp:212-214)
+        for (int job = w; job < 2 * r; job += NW) {
+          const int l = job >> 1;
+          if (job & 1) {
+            const double d = warp_canonical_dot(V + (size_t)l * T.m, vn, T.m, lane);
+            if (lane == 0) dv[l] = d;
+          } else {
+            const double d = warp_canonical_dot(U + (size_t)l * T.n, un, T.n, lane);
+            if (lane == 0) du[l] = d;
+          }
+        }
+        ++r;
+        __syncthreads();
+        if (tid == 0) {
+          const double p = __dmul_rn(S.nu, S.nv);
+          double ns = __dadd_rn(__dmul_rn(S.normS, S.normS), __dmul_rn(p, p));
+          for (int l = 0; l < r; ++l) ns = __dadd_rn(ns, __dmul_rn(2.0, fabs(__dmul_rn(du[l], dv[l]))));
+          S.normS = __dsqrt_rn(ns);
+        }
+        __syncthreads();
+        row_index = next_row;
+      }
+    } else if (S.flag_bad) {
+      status = 2;
+    }
+    if (tid == 0) {
+      out_rank[ti] = r;
+      out_status[ti] = status;
+    }
+    __syncthreads();
+  }
+}
+
+// Copies the first r columns of U and V of every task into the final pools
+// (FP64, and optionally FP32), U (n x r) then V (m x r) at dst_off.
+__global__ void k_aca_compact(const AcaTask* __restrict__ tasks, const int32_t* __restrict__ rank,
+                              const int64_t* __restrict__ dst_off, const double* __restrict__ ws,
+                              double* __restrict__ out64, float* __restrict__ out32) {
+  const AcaTask T = tasks[blockIdx.x];
+  const int r = rank[blockIdx.x];
+  const double* U = ws + T.ws_off;
+  const double* V = U + (size_t)T.cap * T.n;
+  const int64_t o = dst_off[blockIdx.x];
+  const int64_t nu = (int64_t)r * T.n, nv = (int64_t)r * T.m;
+  for (int64_t i = threadIdx.x; i < nu; i += blockDim.x) {
+    const double v = U[i];
+    out64[o + i] = v;
+    if (out32) out32[o + i] = (float)v;
+  }
+  for (int64_t i = threadIdx.x; i < nv; i += blockDim.x) {
+    const double v = V[i];
+    out64[o + nu + i] = v;
+    if (out32) out32[o + nu + i] = (float)v;
+  }
+}
+
+size_t aca_shared_bytes(int cap_max) { return (size_t)4 * cap_max * sizeof(double); }
+
+cudaError_t launch_aca(cudaStream_t s, int block, int grid, const AcaTask* tasks, int ntasks,
+                       int* counter, PointsF64 P, KernelDesc kd, double tol, double* ws,
+                       unsigned char* flags, int32_t* piv, int32_t* out_rank, int32_t* out_status,
+                       int cap_max) {
+  const size_t shm = aca_shared_bytes(cap_max);
+  cudaError_t e;
+  if (block == 64) {
+    e = cudaFuncSetAttribute(k_aca<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+    if (e != cudaSuccess) return e;
+    k_aca<64><<<grid, 64, shm, s>>>(tasks, ntasks, counter, P, kd, tol, ws, flags, piv, out_rank,
+                                     out_status);
+  } else {
+    e = cudaFuncSetAttribute(k_aca<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+    if (e != cudaSuccess) return e;
+    k_aca<256><<<grid, 256, shm, s>>>(tasks, ntasks, counter, P, kd, tol, ws, flags, piv,
+                                       out_rank, out_status);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_aca_compact(cudaStream_t s, int ntasks, const AcaTask* tasks,
+                               const int32_t* rank, const int64_t* dst_off, const double* ws,
+                               double* out64, float* out32) {
+  if (ntasks == 0) return cudaSuccess;
+  k_aca_compact<<<ntasks, 256, 0, s>>>(tasks, rank, dst_off, ws, out64, out32);
+  return cudaGetLastError();
+}
+
+}  // namespace h3d

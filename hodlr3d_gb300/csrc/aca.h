@@ -1,0 +1,38 @@
+// Batched ACA launchers (aca.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace h3d {
+
+// Points in tree order, FP64.
+struct PointsF64 {
+  const double* x;
+  const double* y;
+  const double* z;
+};
+
+// One ACA task: the block K(rows [t0, t0+n), cols [s0, s0+m)) in tree order.
+struct AcaTask {
+  int32_t t0, n, s0, m;
+  int32_t cap;      // rank capacity of the workspace
+  int32_t pair;     // pair index
+  int64_t ws_off;   // doubles: U (cap x n) then V (cap x m), column-major
+  int64_t fl_off;   // bytes: used-row flags (n) then used-column flags (m)
+  int64_t piv_off;  // ints: row pivots (cap) then column pivots (cap), local indices
+};
+
+enum AcaStatus { kAcaOk = 0, kAcaCapReached = 1, kAcaNonFinite = 2 };
+
+size_t aca_shared_bytes(int cap_max);
+cudaError_t launch_aca(cudaStream_t s, int block, int grid, const AcaTask* tasks, int ntasks,
+                       int* counter, PointsF64 P, KernelDesc kd, double tol, double* ws,
+                       unsigned char* flags, int32_t* piv, int32_t* out_rank, int32_t* out_status,
+                       int cap_max);
+cudaError_t launch_aca_compact(cudaStream_t s, int ntasks, const AcaTask* tasks,
+                               const int32_t* rank, const int64_t* dst_off, const double* ws,
+                               double* out64, float* out32);
+
+}  // namespace h3d

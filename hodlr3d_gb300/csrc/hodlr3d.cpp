@@ -1,0 +1,1131 @@
+// Host side of the hodlr3d_gb300 C ABI: handle life cycle, device memory,
+// tree build, batched ACA orchestration, matvec and GMRES drivers.
+//
+// Reference interfaces replaced: HODLR3D (include/HODLR3D.hpp:12-21,
+// src/HODLR3D.cpp), HODLR3DTree (include/HODLR3DTree.hpp, src/HODLR3DTree.cpp),
+// LowRank (src/ACA.cpp), classGMRES (include/gmres.hpp, src/gmres.cpp).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/hodlr3d.h"
+#include "aca.h"
+#include "common.cuh"
+#include "gmres.h"
+#include "matvec.h"
+#include "tree.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int set_error(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+#define H3D_CUDA(call)                                                                   \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess) {                                                             \
+      if (e_ == cudaErrorMemoryAllocation)                                               \
+        return set_error(HODLR3D_ERR_OUT_OF_MEMORY, "%s: %s (%s:%d)", #call,             \
+                         cudaGetErrorString(e_), __FILE__, __LINE__);                    \
+      return set_error(HODLR3D_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                       __FILE__, __LINE__);                                              \
+    }                                                                                    \
+  } while (0)
+
+#define H3D_TRY(call)           \
+  do {                          \
+    int s_ = (call);            \
+    if (s_ != HODLR3D_OK) return s_; \
+  } while (0)
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// Gauss-Legendre nodes and weights on [-1, 1] by Newton iteration on the
+// three-term Legendre recurrence (the classical "gauleg" method).
+void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w) {
+  x.assign(n, 0.0);
+  w.assign(n, 0.0);
+  for (int i = 0; i < (n + 1) / 2; ++i) {
+    long double z = std::cos(3.1415926535897932384626L * (i + 0.75L) / (n + 0.5L));
+    long double dp = 0.0L;
+    for (int it = 0; it < 100; ++it) {
+      long double p0 = 1.0L, p1 = 0.0L;
+      for (int j = 1; j <= n; ++j) {
+        const long double pm = p1;
+        p1 = p0;
+        p0 = ((2.0L * j - 1.0L) * z * p1 - (j - 1.0L) * pm) / j;
+      }
+      dp = n * (z * p0 - p1) / (z * z - 1.0L);
+      const long double dz = p0 / dp;
+      z -= dz;
+      if (std::fabs((double)dz) < 1e-19) break;
+    }
+    x[i] = (double)(-z);
+    x[n - 1 - i] = (double)z;
+    const long double wi = 2.0L / ((1.0L - z * z) * dp * dp);
+    w[i] = w[n - 1 - i] = (double)wi;
+  }
+}
+
+// Diagonal of the second-kind integral operator (Qchoice 16): the integral of
+// 1/(4 pi r) over the point's cell [-h/2, h/2]^3 (8 times the octant
+// [0, h/2]^3, 16^3 Gauss-Legendre points) plus 1, h = 1 / cbrt(N)
+// (include/kernel.hpp:43-61, src/Integral3D.cpp:9-43).
+double quadrature_kii(int64_t N) {
+  const double pi = 3.1415926535897932384;
+  const double h = 1.0 / std::cbrt(double(N));
+  std::vector<double> g, wg;
+  gauss_legendre(16, g, wg);
+  const double half = 0.5 * (h * 0.5), mid = 0.5 * (h * 0.5);
+  double acc = 0.0;
+  for (int i = 0; i < 16; ++i) {
+    const double tx = half * g[i] + mid;
+    for (int j = 0; j < 16; ++j) {
+      const double ty = half * g[j] + mid;
+      for (int k = 0; k < 16; ++k) {
+        const double tz = half * g[k] + mid;
+        const double f = 1.0 / ((4 * pi) * std::sqrt(tx * tx + ty * ty + tz * tz));
+        acc += wg[i] * wg[j] * wg[k] * f;
+      }
+    }
+  }
+  acc *= (half * half * half);
+  acc *= 8;
+  return acc + 1.0;
+}
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  cudaError_t ensure(size_t b) {
+    if (b <= bytes && p) return cudaSuccess;
+    release();
+    cudaError_t e = cudaMalloc(&p, b ? b : 16);
+    if (e == cudaSuccess) bytes = b;
+    return e;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+}  // namespace
+
+struct hodlr3d_handle {
+  // problem
+  int64_t N = 0;
+  int nP1D = 0;
+  double L = 1.0;
+  int tol_pow = 0;
+  double tol = 0.0;
+  int levels = 0;
+  int64_t nleaf = 0;
+  int64_t nbox_all = 0;
+  hodlr3d_options opt{};
+  h3d::KernelDesc kd{};
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  int64_t launches = 0;
+  // tree (device)
+  DevBuf xyz, perm, leaf_off, xs, ys, zs, xl, yl, zl, centre, nbr_all, nbr_leaf, il_ptr, pair_tgt,
+      pair_src, rev;
+  std::vector<int32_t> h_perm, h_leaf_off, h_pair_tgt, h_pair_src, h_pair_level;
+  std::vector<int64_t> h_il_ptr;
+  int max_leaf = 0;
+  int64_t npairs = 0;
+  double tree_seconds = 0.0;
+  // factors
+  bool assembled = false;
+  std::vector<int32_t> h_rank;
+  std::vector<std::vector<int32_t>> h_piv_rows, h_piv_cols;  // local pivots per pair
+  std::vector<DevBuf*> pools;
+  std::vector<int64_t> h_fac_off;       // per pair: element offset in its pool
+  std::vector<int32_t> h_fac_pool;      // per pair: pool index
+  std::vector<double*> h_u64, h_v64;
+  std::vector<float*> h_u32, h_v32;
+  DevBuf rank, u64, v64, u32, v32, tr_off, part_off, nonleaf, pair_level;
+  int64_t sum_rank = 0, part_total = 0, n_nonleaf = 0, factor_entries = 0;
+  int max_rank = 0;
+  double assemble_seconds = 0.0;
+  int aca_batches = 0;
+  // matvec work buffers
+  DevBuf xsorted, tbuf, pbuf, stage_x, stage_y;
+  int mv_nrhs_cap = 0;
+  void* pinned_x = nullptr;
+  void* pinned_y = nullptr;
+  size_t pinned_bytes = 0;
+  // GMRES work buffers
+  DevBuf g_Q, g_w, g_r, g_x, g_b, g_H, g_cs, g_sn, g_beta, g_hk, g_bnorm, g_err, g_part, g_y,
+      g_kcol, g_brk, g_scal, g_d, g_coef;
+
+  ~hodlr3d_handle() {
+    for (DevBuf* b : pools) delete b;
+    if (pinned_x) cudaFreeHost(pinned_x);
+    if (pinned_y) cudaFreeHost(pinned_y);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+int check_handle(hodlr3d_t h) {
+  if (!h) return set_error(HODLR3D_ERR_INVALID_ARG, "null handle");
+  cudaError_t e = cudaSetDevice(h->device);
+  if (e != cudaSuccess) return set_error(HODLR3D_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+  return HODLR3D_OK;
+}
+
+bool kernel_supported(int k) { return (k >= 0 && k <= 10) || k == 13 || k == 15 || k == 16; }
+
+// ---------------------------------------------------------------------------
+// tree
+// ---------------------------------------------------------------------------
+int build_tree(hodlr3d_t h, const double* xyz_host) {
+  const double t_start = now_s();
+  cudaStream_t s = h->stream;
+  const int64_t N = h->N;
+  const int d = h->levels;
+  std::vector<double> radii(d + 1);
+  radii[0] = h->L;
+  for (int k = 1; k <= d; ++k) radii[k] = 0.5 * radii[k - 1];
+  h->nleaf = int64_t(1) << (3 * d);
+  h->nbox_all = h3d::level_base(d + 1);
+  H3D_CUDA(h->xyz.ensure(sizeof(double) * 3 * N));
+  H3D_CUDA(cudaMemcpyAsync(h->xyz.p, xyz_host, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, s));
+  DevBuf keys, keys_tmp, vals_tmp, counts;
+  H3D_CUDA(keys.ensure(sizeof(uint32_t) * N));
+  H3D_CUDA(keys_tmp.ensure(sizeof(uint32_t) * N));
+  H3D_CUDA(vals_tmp.ensure(sizeof(int32_t) * N));
+  H3D_CUDA(h->perm.ensure(sizeof(int32_t) * N));
+  const int64_t ntiles = (N + 1023) / 1024;
+  H3D_CUDA(counts.ensure(sizeof(int32_t) * 256 * ntiles));
+  h3d::launch_leaf_keys(s, N, h->xyz.as<double>(), d, radii.data(), keys.as<uint32_t>(),
+                        h->perm.as<int32_t>());
+  int launches = 1;
+  h3d::radix_sort_pairs(s, N, 3 * d, keys.as<uint32_t>(), h->perm.as<int32_t>(),
+                        keys_tmp.as<uint32_t>(), vals_tmp.as<int32_t>(), counts.as<int32_t>(),
+                        &launches);
+  H3D_CUDA(h->leaf_off.ensure(sizeof(int32_t) * (h->nleaf + 1)));
+  h3d::launch_leaf_offsets(s, N, keys.as<uint32_t>(), h->nleaf, h->leaf_off.as<int32_t>());
+  H3D_CUDA(h->xs.ensure(8 * N));
+  H3D_CUDA(h->ys.ensure(8 * N));
+  H3D_CUDA(h->zs.ensure(8 * N));
+  H3D_CUDA(h->xl.ensure(4 * N));
+  H3D_CUDA(h->yl.ensure(4 * N));
+  H3D_CUDA(h->zl.ensure(4 * N));
+  H3D_CUDA(h->centre.ensure(sizeof(double) * 3 * h->nleaf));
+  h3d::launch_gather_points(s, N, h->xyz.as<double>(), h->perm.as<int32_t>(), keys.as<uint32_t>(), d,
+                            radii.data(), h->xs.as<double>(), h->ys.as<double>(),
+                            h->zs.as<double>(), h->xl.as<float>(), h->yl.as<float>(),
+                            h->zl.as<float>());
+  h3d::launch_leaf_centres(s, h->nleaf, d, radii.data(), h->centre.as<double>());
+  launches += 3;
+  // neighbour slots and interaction lists, level by level: count, scan on the host, write
+  H3D_CUDA(h->nbr_all.ensure(sizeof(int32_t) * 26 * h->nbox_all));
+  H3D_CUDA(cudaMemsetAsync(h->nbr_all.p, 0xff, sizeof(int32_t) * 26 * h->nbox_all, s));
+  DevBuf il_count;
+  H3D_CUDA(il_count.ensure(sizeof(int32_t) * h->nbox_all));
+  H3D_CUDA(cudaMemsetAsync(il_count.p, 0, sizeof(int32_t) * h->nbox_all, s));
+  for (int j = 1; j <= d; ++j) {
+    h3d::launch_box_lists(s, j, 0, nullptr, il_count.as<int32_t>(), nullptr, nullptr, nullptr);
+    ++launches;
+  }
+  std::vector<int32_t> cnt(h->nbox_all);
+  H3D_CUDA(cudaMemcpyAsync(cnt.data(), il_count.p, sizeof(int32_t) * h->nbox_all,
+                           cudaMemcpyDeviceToHost, s));
+  H3D_CUDA(cudaStreamSynchronize(s));
+  h->h_il_ptr.assign(h->nbox_all + 1, 0);
+  for (int64_t b = 0; b < h->nbox_all; ++b) h->h_il_ptr[b + 1] = h->h_il_ptr[b] + cnt[b];
+  h->npairs = h->h_il_ptr[h->nbox_all];
+  H3D_CUDA(h->il_ptr.ensure(sizeof(int64_t) * (h->nbox_all + 1)));
+  H3D_CUDA(cudaMemcpyAsync(h->il_ptr.p, h->h_il_ptr.data(), sizeof(int64_t) * (h->nbox_all + 1),
+                           cudaMemcpyHostToDevice, s));
+  H3D_CUDA(h->pair_tgt.ensure(sizeof(int32_t) * std::max<int64_t>(1, h->npairs)));
+  H3D_CUDA(h->pair_src.ensure(sizeof(int32_t) * std::max<int64_t>(1, h->npairs)));
+  H3D_CUDA(h->rev.ensure(sizeof(int32_t) * std::max<int64_t>(1, h->npairs)));
+  for (int j = 1; j <= d; ++j) {
+    h3d::launch_box_lists(s, j, 1, h->nbr_all.as<int32_t>(), il_count.as<int32_t>(),
+                          h->il_ptr.as<int64_t>(), h->pair_tgt.as<int32_t>(),
+                          h->pair_src.as<int32_t>());
+    ++launches;
+  }
+  DevBuf err;
+  H3D_CUDA(err.ensure(sizeof(int32_t)));
+  H3D_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int32_t), s));
+  h3d::launch_reverse_pairs(s, h->npairs, h->pair_tgt.as<int32_t>(), h->pair_src.as<int32_t>(),
+                            h->il_ptr.as<int64_t>(), h->rev.as<int32_t>(), err.as<int32_t>());
+  ++launches;
+  // leaf neighbour table (a view of the leaf level of nbr_all, re-based to leaf ids)
+  std::vector<int32_t> nb_leaf(26 * h->nleaf);
+  H3D_CUDA(cudaMemcpyAsync(nb_leaf.data(),
+                           h->nbr_all.as<int32_t>() + 26 * h3d::level_base(d),
+                           sizeof(int32_t) * 26 * h->nleaf, cudaMemcpyDeviceToHost, s));
+  h->h_perm.resize(N);
+  h->h_leaf_off.resize(h->nleaf + 1);
+  h->h_pair_tgt.resize(h->npairs);
+  h->h_pair_src.resize(h->npairs);
+  int32_t herr = 0;
+  H3D_CUDA(cudaMemcpyAsync(h->h_perm.data(), h->perm.p, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, s));
+  H3D_CUDA(cudaMemcpyAsync(h->h_leaf_off.data(), h->leaf_off.p, sizeof(int32_t) * (h->nleaf + 1),
+                           cudaMemcpyDeviceToHost, s));
+  if (h->npairs) {
+    H3D_CUDA(cudaMemcpyAsync(h->h_pair_tgt.data(), h->pair_tgt.p, sizeof(int32_t) * h->npairs,
+                             cudaMemcpyDeviceToHost, s));
+    H3D_CUDA(cudaMemcpyAsync(h->h_pair_src.data(), h->pair_src.p, sizeof(int32_t) * h->npairs,
+                             cudaMemcpyDeviceToHost, s));
+  }
+  H3D_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  H3D_CUDA(cudaStreamSynchronize(s));
+  H3D_CUDA(cudaGetLastError());
+  h->launches += launches;
+  if (herr) return set_error(HODLR3D_ERR_CUDA, "interaction lists are not symmetric");
+  H3D_CUDA(h->nbr_leaf.ensure(sizeof(int32_t) * 26 * h->nleaf));
+  H3D_CUDA(cudaMemcpyAsync(h->nbr_leaf.p, nb_leaf.data(), sizeof(int32_t) * 26 * h->nleaf,
+                           cudaMemcpyHostToDevice, s));
+  h->h_pair_level.resize(h->npairs);
+  for (int64_t p = 0; p < h->npairs; ++p) {
+    int j = 0;
+    while (h3d::level_base(j + 1) <= h->h_pair_tgt[p]) ++j;
+    h->h_pair_level[p] = j;
+  }
+  h->max_leaf = 0;
+  for (int64_t k = 0; k < h->nleaf; ++k)
+    h->max_leaf = std::max(h->max_leaf, h->h_leaf_off[k + 1] - h->h_leaf_off[k]);
+  H3D_CUDA(cudaStreamSynchronize(s));
+  h->tree_seconds = now_s() - t_start;
+  return HODLR3D_OK;
+}
+
+// range [start, end) in tree order of box k at level j
+inline void box_range(const hodlr3d_t h, int j, int64_t k, int64_t& a, int64_t& b) {
+  const int sh = 3 * (h->levels - j);
+  a = h->h_leaf_off[k << sh];
+  b = h->h_leaf_off[(k + 1) << sh];
+}
+
+// ---------------------------------------------------------------------------
+// assembly
+// ---------------------------------------------------------------------------
+struct HostTask {
+  int64_t pair;
+  int32_t t0, n, s0, m;
+  int32_t cap;
+  bool leaf;
+};
+
+int run_aca_batch(hodlr3d_t h, std::vector<HostTask>& batch, std::vector<HostTask>& retry,
+                  bool small_kernel) {
+  cudaStream_t s = h->stream;
+  const int nt = (int)batch.size();
+  std::vector<h3d::AcaTask> tasks(nt);
+  int64_t ws = 0, fl = 0, pv = 0;
+  int cap_max = 1;
+  for (int i = 0; i < nt; ++i) {
+    const HostTask& b = batch[i];
+    h3d::AcaTask& t = tasks[i];
+    t.t0 = b.t0;
+    t.n = b.n;
+    t.s0 = b.s0;
+    t.m = b.m;
+    t.cap = b.cap;
+    t.pair = (int32_t)b.pair;
+    t.ws_off = ws;
+    t.fl_off = fl;
+    t.piv_off = pv;
+    ws += (int64_t)b.cap * (b.n + b.m);
+    fl += b.n + b.m;
+    pv += 2 * (int64_t)b.cap;
+    cap_max = std::max(cap_max, b.cap);
+  }
+  DevBuf d_tasks, d_ws, d_fl, d_pv, d_rank, d_status, d_counter, d_off;
+  H3D_CUDA(d_tasks.ensure(sizeof(h3d::AcaTask) * nt));
+  H3D_CUDA(d_ws.ensure(sizeof(double) * std::max<int64_t>(ws, 1)));
+  H3D_CUDA(d_fl.ensure(std::max<int64_t>(fl, 1)));
+  H3D_CUDA(d_pv.ensure(sizeof(int32_t) * std::max<int64_t>(pv, 1)));
+  H3D_CUDA(d_rank.ensure(sizeof(int32_t) * nt));
+  H3D_CUDA(d_status.ensure(sizeof(int32_t) * nt));
+  H3D_CUDA(d_counter.ensure(sizeof(int32_t)));
+  H3D_CUDA(cudaMemcpyAsync(d_tasks.p, tasks.data(), sizeof(h3d::AcaTask) * nt, cudaMemcpyHostToDevice, s));
+  H3D_CUDA(cudaMemsetAsync(d_counter.p, 0, sizeof(int32_t), s));
+  const int block = small_kernel ? 64 : 256;
+  const size_t shm = h3d::aca_shared_bytes(cap_max);
+  int per_sm = small_kernel ? 16 : 4;
+  if (shm > 0) {
+    const int by_shm = (int)std::max<size_t>(1, (200 * 1024) / (shm + 2048));
+    per_sm = std::max(1, std::min(per_sm, by_shm));
+  }
+  const int grid = std::max(1, std::min(nt, h->num_sms * per_sm));
+  h3d::PointsF64 P{h->xs.as<double>(), h->ys.as<double>(), h->zs.as<double>()};
+  H3D_CUDA(h3d::launch_aca(s, block, grid, d_tasks.as<h3d::AcaTask>(), nt, d_counter.as<int>(), P,
+                           h->kd, h->tol, d_ws.as<double>(), d_fl.as<unsigned char>(),
+                           d_pv.as<int32_t>(), d_rank.as<int32_t>(), d_status.as<int32_t>(),
+                           cap_max));
+  ++h->launches;
+  std::vector<int32_t> rk(nt), st(nt), pvh(pv);
+  H3D_CUDA(cudaMemcpyAsync(rk.data(), d_rank.p, sizeof(int32_t) * nt, cudaMemcpyDeviceToHost, s));
+  H3D_CUDA(cudaMemcpyAsync(st.data(), d_status.p, sizeof(int32_t) * nt, cudaMemcpyDeviceToHost, s));
+  if (pv) H3D_CUDA(cudaMemcpyAsync(pvh.data(), d_pv.p, sizeof(int32_t) * pv, cudaMemcpyDeviceToHost, s));
+  H3D_CUDA(cudaStreamSynchronize(s));
+  H3D_CUDA(cudaGetLastError());
+  // finished tasks -> exact-size pools; capacity overflows -> retried with twice the capacity
+  std::vector<int64_t> dst(nt, 0);
+  int64_t total = 0;
+  for (int i = 0; i < nt; ++i) {
+    if (st[i] == h3d::kAcaNonFinite)
+      return set_error(HODLR3D_ERR_NONFINITE,
+                       "non-finite kernel entry in the ACA of pair %lld (coincident points?)",
+                       (long long)batch[i].pair);
+    if (st[i] == h3d::kAcaCapReached) {
+      HostTask t = batch[i];
+      t.cap = std::min(std::min(t.n, t.m), 2 * t.cap);
+      retry.push_back(t);
+      rk[i] = 0;
+      continue;
+    }
+    dst[i] = total;
+    total += (int64_t)rk[i] * (batch[i].n + batch[i].m);
+  }
+  DevBuf* pool64 = new DevBuf();
+  h->pools.push_back(pool64);
+  H3D_CUDA(pool64->ensure(sizeof(double) * std::max<int64_t>(total, 1)));
+  DevBuf* pool32 = nullptr;
+  if (h->opt.keep_fp32) {
+    pool32 = new DevBuf();
+    h->pools.push_back(pool32);
+    H3D_CUDA(pool32->ensure(sizeof(float) * std::max<int64_t>(total, 1)));
+  }
+  H3D_CUDA(d_off.ensure(sizeof(int64_t) * nt));
+  H3D_CUDA(cudaMemcpyAsync(d_off.p, dst.data(), sizeof(int64_t) * nt, cudaMemcpyHostToDevice, s));
+  H3D_CUDA(cudaMemcpyAsync(d_rank.p, rk.data(), sizeof(int32_t) * nt, cudaMemcpyHostToDevice, s));
+  H3D_CUDA(h3d::launch_aca_compact(s, nt, d_tasks.as<h3d::AcaTask>(), d_rank.as<int32_t>(),
+                                   d_off.as<int64_t>(), d_ws.as<double>(), pool64->as<double>(),
+                                   pool32 ? pool32->as<float>() : nullptr));
+  ++h->launches;
+  for (int i = 0; i < nt; ++i) {
+    if (st[i] == h3d::kAcaCapReached) continue;
+    const int64_t p = batch[i].pair;
+    const int r = rk[i];
+    h->h_rank[p] = r;
+    double* base64 = pool64->as<double>() + dst[i];
+    h->h_u64[p] = base64;
+    h->h_v64[p] = base64 + (int64_t)r * batch[i].n;
+    if (pool32) {
+      float* base32 = pool32->as<float>() + dst[i];
+      h->h_u32[p] = base32;
+      h->h_v32[p] = base32 + (int64_t)r * batch[i].n;
+    }
+    const int32_t* pr = pvh.data() + tasks[i].piv_off;
+    h->h_piv_rows[p].assign(pr, pr + r);
+    h->h_piv_cols[p].assign(pr + tasks[i].cap, pr + tasks[i].cap + r);
+  }
+  H3D_CUDA(cudaStreamSynchronize(s));
+  ++h->aca_batches;
+  return HODLR3D_OK;
+}
+
+int assemble(hodlr3d_t h) {
+  const double t_start = now_s();
+  const int64_t np = h->npairs;
+  h->h_rank.assign(np, 0);
+  h->h_piv_rows.assign(np, {});
+  h->h_piv_cols.assign(np, {});
+  h->h_u64.assign(np, nullptr);
+  h->h_v64.assign(np, nullptr);
+  h->h_u32.assign(np, nullptr);
+  h->h_v32.assign(np, nullptr);
+  for (DevBuf* b : h->pools) delete b;
+  h->pools.clear();
+  h->aca_batches = 0;
+  const int cap0 = h->opt.rank_cap > 0 ? h->opt.rank_cap : 256;
+  std::vector<HostTask> todo;
+  todo.reserve(np);
+  for (int64_t p = 0; p < np; ++p) {
+    const int j = h->h_pair_level[p];
+    const int64_t kt = h->h_pair_tgt[p] - h3d::level_base(j);
+    const int64_t ks = h->h_pair_src[p] - h3d::level_base(j);
+    int64_t a0, a1, b0, b1;
+    box_range(h, j, kt, a0, a1);
+    box_range(h, j, ks, b0, b1);
+    HostTask t;
+    t.pair = p;
+    t.t0 = (int32_t)a0;
+    t.n = (int32_t)(a1 - a0);
+    t.s0 = (int32_t)b0;
+    t.m = (int32_t)(b1 - b0);
+    t.leaf = j == h->levels;
+    const int mn = std::min(t.n, t.m);
+    t.cap = (t.leaf || mn <= cap0) ? mn : cap0;
+    todo.push_back(t);
+  }
+  const size_t budget = h->opt.aca_workspace_bytes ? h->opt.aca_workspace_bytes : (size_t(8) << 30);
+  while (!todo.empty()) {
+    // largest blocks first
+    std::stable_sort(todo.begin(), todo.end(), [](const HostTask& a, const HostTask& b) {
+      return (int64_t)a.n * a.m > (int64_t)b.n * b.m;
+    });
+    std::vector<HostTask> retry;
+    size_t i = 0;
+    while (i < todo.size()) {
+      const bool small = std::max(todo[i].n, todo[i].m) <= 128;
+      std::vector<HostTask> batch;
+      size_t bytes = 0;
+      while (i < todo.size()) {
+        const HostTask& t = todo[i];
+        if ((std::max(t.n, t.m) <= 128) != small) break;
+        const size_t tb = sizeof(double) * (size_t)t.cap * (t.n + t.m) + (t.n + t.m) + 8 * t.cap + 64;
+        if (!batch.empty() && bytes + tb > budget) break;
+        batch.push_back(t);
+        bytes += tb;
+        ++i;
+      }
+      H3D_TRY(run_aca_batch(h, batch, retry, small));
+    }
+    todo.swap(retry);
+  }
+  // per-pair tables for the matvec
+  std::vector<int64_t> tr(np), po(np, -1);
+  std::vector<int32_t> nonleaf;
+  int64_t acc = 0, pacc = 0, fe = 0;
+  h->max_rank = 0;
+  for (int64_t p = 0; p < np; ++p) {
+    tr[p] = acc;
+    acc += h->h_rank[p];
+    h->max_rank = std::max(h->max_rank, h->h_rank[p]);
+    const int j = h->h_pair_level[p];
+    const int64_t kt = h->h_pair_tgt[p] - h3d::level_base(j), ks = h->h_pair_src[p] - h3d::level_base(j);
+    int64_t a0, a1, b0, b1;
+    box_range(h, j, kt, a0, a1);
+    box_range(h, j, ks, b0, b1);
+    fe += (int64_t)h->h_rank[p] * ((a1 - a0) + (b1 - b0));
+    if (j < h->levels) {
+      po[p] = pacc;
+      pacc += (int64_t)h->h_rank[p] << (3 * (h->levels - j));
+      nonleaf.push_back((int32_t)p);
+    }
+  }
+  h->sum_rank = acc;
+  h->part_total = pacc;
+  h->n_nonleaf = (int64_t)nonleaf.size();
+  h->factor_entries = fe;
+  cudaStream_t s = h->stream;
+  const size_t npb = std::max<int64_t>(np, 1);
+  H3D_CUDA(h->rank.ensure(sizeof(int32_t) * npb));
+  H3D_CUDA(h->u64.ensure(sizeof(void*) * npb));
+  H3D_CUDA(h->v64.ensure(sizeof(void*) * npb));
+  H3D_CUDA(h->u32.ensure(sizeof(void*) * npb));
+  H3D_CUDA(h->v32.ensure(sizeof(void*) * npb));
+  H3D_CUDA(h->tr_off.ensure(sizeof(int64_t) * npb));
+  H3D_CUDA(h->part_off.ensure(sizeof(int64_t) * npb));
+  H3D_CUDA(h->nonleaf.ensure(sizeof(int32_t) * std::max<size_t>(nonleaf.size(), 1)));
+  H3D_CUDA(h->pair_level.ensure(sizeof(int32_t) * npb));
+  if (np) {
+    H3D_CUDA(cudaMemcpyAsync(h->rank.p, h->h_rank.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice, s));
+    H3D_CUDA(cudaMemcpyAsync(h->u64.p, h->h_u64.data(), sizeof(void*) * np, cudaMemcpyHostToDevice, s));
+    H3D_CUDA(cudaMemcpyAsync(h->v64.p, h->h_v64.data(), sizeof(void*) * np, cudaMemcpyHostToDevice, s));
+    H3D_CUDA(cudaMemcpyAsync(h->u32.p, h->h_u32.data(), sizeof(void*) * np, cudaMemcpyHostToDevice, s));
+    H3D_CUDA(cudaMemcpyAsync(h->v32.p, h->h_v32.data(), sizeof(void*) * np, cudaMemcpyHostToDevice, s));
+    H3D_CUDA(cudaMemcpyAsync(h->tr_off.p, tr.data(), sizeof(int64_t) * np, cudaMemcpyHostToDevice, s));
+    H3D_CUDA(cudaMemcpyAsync(h->part_off.p, po.data(), sizeof(int64_t) * np, cudaMemcpyHostToDevice, s));
+    H3D_CUDA(cudaMemcpyAsync(h->pair_level.p, h->h_pair_level.data(), sizeof(int32_t) * np,
+                             cudaMemcpyHostToDevice, s));
+  }
+  if (!nonleaf.empty())
+    H3D_CUDA(cudaMemcpyAsync(h->nonleaf.p, nonleaf.data(), sizeof(int32_t) * nonleaf.size(),
+                             cudaMemcpyHostToDevice, s));
+  H3D_CUDA(cudaStreamSynchronize(s));
+  h->mv_nrhs_cap = 0;
+  h->assembled = true;
+  h->assemble_seconds = now_s() - t_start;
+  return HODLR3D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// matvec
+// ---------------------------------------------------------------------------
+int ensure_matvec_buffers(hodlr3d_t h, int nrhs) {
+  if (nrhs <= h->mv_nrhs_cap) return HODLR3D_OK;
+  H3D_CUDA(h->xsorted.ensure(sizeof(double) * h->N * nrhs));
+  H3D_CUDA(h->tbuf.ensure(sizeof(double) * std::max<int64_t>(h->sum_rank, 1) * nrhs));
+  H3D_CUDA(h->pbuf.ensure(sizeof(double) * std::max<int64_t>(h->part_total, 1) * nrhs));
+  h->mv_nrhs_cap = nrhs;
+  return HODLR3D_OK;
+}
+
+int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld, int precision,
+                  cudaStream_t s, bool trans) {
+  if (!h->assembled) return set_error(HODLR3D_ERR_NOT_ASSEMBLED, "hodlr3d_assemble has not run");
+  if (!x || !y) return set_error(HODLR3D_ERR_INVALID_ARG, "null vector");
+  if (nrhs < 1 || nrhs > 64) return set_error(HODLR3D_ERR_INVALID_ARG, "nrhs must be in 1..64");
+  if (ld < h->N) return set_error(HODLR3D_ERR_INVALID_ARG, "ld < n");
+  if (precision != HODLR3D_FP64 && precision != HODLR3D_MIXED)
+    return set_error(HODLR3D_ERR_INVALID_ARG, "unknown precision %d", precision);
+  if (precision == HODLR3D_MIXED && !h->opt.keep_fp32)
+    return set_error(HODLR3D_ERR_INVALID_ARG, "mixed precision needs keep_fp32");
+  H3D_TRY(ensure_matvec_buffers(h, nrhs));
+  const bool f32 = precision == HODLR3D_MIXED;
+  h3d::FarOp far{};
+  far.levels = h->levels;
+  far.nleaf = h->nleaf;
+  far.leaf_off = h->leaf_off.as<int32_t>();
+  far.il_ptr = h->il_ptr.as<int64_t>();
+  far.rev = h->rev.as<int32_t>();
+  far.rank = h->rank.as<int32_t>();
+  far.tr_off = h->tr_off.as<int64_t>();
+  far.part_off = h->part_off.as<int64_t>();
+  far.ufac = f32 ? h->u32.as<const void*>() : h->u64.as<const void*>();
+  far.vfac = f32 ? h->v32.as<const void*>() : h->v64.as<const void*>();
+  h3d::NearOp nr{};
+  nr.nbr_leaf = h->nbr_leaf.as<int32_t>();
+  nr.xs = h->xs.as<double>();
+  nr.ys = h->ys.as<double>();
+  nr.zs = h->zs.as<double>();
+  nr.xl = h->xl.as<float>();
+  nr.yl = h->yl.as<float>();
+  nr.zl = h->zl.as<float>();
+  nr.centre = h->centre.as<double>();
+  nr.kd = h->kd;
+  h3d::MatvecBuffers B{};
+  B.xsorted = h->xsorted.p;
+  B.tbuf = h->tbuf.as<double>();
+  B.pbuf = h->pbuf.as<double>();
+  B.nonleaf_pairs = h->nonleaf.as<int32_t>();
+  B.n_nonleaf = h->n_nonleaf;
+  B.pair_level = h->pair_level.as<int32_t>();
+  B.max_leaf = h->max_leaf;
+  h->launches += h3d::launch_matvec(s, h->N, h->perm.as<int32_t>(), far, nr, B, x, ld, y, ld, nrhs,
+                                    precision, trans ? 1 : 0);
+  H3D_CUDA(cudaGetLastError());
+  return HODLR3D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// GMRES
+// ---------------------------------------------------------------------------
+// One GMRES(m) cycle from the current x (device, packed N x nrhs, ld = N) for
+// right-hand side b (packed).  Returns the iterations done; err_out holds the
+// final estimates per column.  Matvec precision `prec`.
+int gmres_cycle(hodlr3d_t h, const double* b, double* x, int nrhs, int m, double tol, int prec,
+                bool trans, bool x_is_zero, const std::vector<double>& bnorm_h, int* iters,
+                std::vector<double>& err_out, std::vector<double>* hist, bool* breakdown_any) {
+  cudaStream_t s = h->stream;
+  const int64_t N = h->N;
+  const int64_t vec = N * nrhs;
+  H3D_CUDA(h->g_Q.ensure(sizeof(double) * vec * (m + 1)));
+  H3D_CUDA(h->g_w.ensure(sizeof(double) * vec));
+  H3D_CUDA(h->g_r.ensure(sizeof(double) * vec));
+  H3D_CUDA(h->g_H.ensure(sizeof(double) * nrhs * m * (m + 1)));
+  H3D_CUDA(h->g_cs.ensure(sizeof(double) * nrhs * m));
+  H3D_CUDA(h->g_sn.ensure(sizeof(double) * nrhs * m));
+  H3D_CUDA(h->g_beta.ensure(sizeof(double) * nrhs * (m + 1)));
+  H3D_CUDA(h->g_hk.ensure(sizeof(double) * nrhs * (m + 1)));
+  H3D_CUDA(h->g_bnorm.ensure(sizeof(double) * nrhs));
+  H3D_CUDA(h->g_err.ensure(sizeof(double) * nrhs));
+  H3D_CUDA(h->g_part.ensure(sizeof(double) * nrhs * 1024));
+  H3D_CUDA(h->g_y.ensure(sizeof(double) * nrhs * m));
+  H3D_CUDA(h->g_kcol.ensure(sizeof(int) * nrhs));
+  H3D_CUDA(h->g_brk.ensure(sizeof(int) * nrhs));
+  H3D_CUDA(h->g_scal.ensure(sizeof(double) * nrhs));
+  H3D_CUDA(h->g_coef.ensure(sizeof(double) * nrhs));
+  double* Q = h->g_Q.as<double>();
+  double* w = h->g_w.as<double>();
+  double* r = h->g_r.as<double>();
+  double* hk = h->g_hk.as<double>();
+  // r = b - A x
+  if (x_is_zero) {
+    H3D_CUDA(cudaMemcpyAsync(r, b, sizeof(double) * vec, cudaMemcpyDeviceToDevice, s));
+  } else {
+    H3D_TRY(matvec_device(h, x, w, nrhs, N, prec, s, trans));
+    h->launches += h3d::gmres_sub(s, vec, b, w, r);
+  }
+  H3D_CUDA(cudaMemcpyAsync(h->g_bnorm.p, bnorm_h.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, s));
+  // beta(0) = |r|, Q0 = r / |r|
+  h->launches += h3d::gmres_dot(s, N, nrhs, r, nullptr, nullptr, nullptr, 0, 1, h->g_part.as<double>(),
+                                h->g_scal.as<double>(), 1);
+  H3D_CUDA(cudaMemsetAsync(h->g_beta.p, 0, sizeof(double) * nrhs * (m + 1), s));
+  H3D_CUDA(cudaMemsetAsync(h->g_H.p, 0, sizeof(double) * nrhs * m * (m + 1), s));
+  H3D_CUDA(cudaMemsetAsync(h->g_brk.p, 0, sizeof(int) * nrhs, s));
+  H3D_CUDA(cudaMemcpy2DAsync(h->g_beta.p, sizeof(double) * (m + 1), h->g_scal.p, sizeof(double),
+                             sizeof(double), nrhs, cudaMemcpyDeviceToDevice, s));
+  h->launches += h3d::gmres_scale_copy(s, N, nrhs, r, h->g_scal.as<double>(), Q);
+  std::vector<double> rn(nrhs), err(nrhs);
+  H3D_CUDA(cudaMemcpyAsync(rn.data(), h->g_scal.p, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s));
+  H3D_CUDA(cudaStreamSynchronize(s));
+  std::vector<int> kcol(nrhs, -1);
+  std::vector<char> done(nrhs, 0);
+  bool all_done = true;
+  for (int c = 0; c < nrhs; ++c) {
+    err[c] = rn[c] / bnorm_h[c];
+    if (err[c] <= tol || rn[c] == 0.0) done[c] = 1;
+    all_done = all_done && done[c];
+  }
+  int k = 0;
+  for (; k < m && !all_done; ++k) {
+    double* Qk = Q + (int64_t)k * vec;
+    double* Qn = Q + (int64_t)(k + 1) * vec;
+    H3D_TRY(matvec_device(h, Qk, Qn, nrhs, N, prec, s, trans));
+    // modified Gram-Schmidt (arnoldi, src/gmres.cpp:29-38) as fused passes:
+    // pass i applies q -= h_{i-1} Q_{i-1} and forms h_i = q . Q_i; the last
+    // pass forms h_{k+1} = |q|.
+    for (int i = 0; i <= k + 1; ++i) {
+      const bool upd = i > 0;
+      const bool last = i == k + 1;
+      h->launches += h3d::gmres_dot(s, N, nrhs, Qn, upd ? Q + (int64_t)(i - 1) * vec : nullptr,
+                                    upd ? h->g_coef.as<double>() : nullptr,
+                                    last ? nullptr : Q + (int64_t)i * vec, upd ? 1 : 0, last ? 1 : 0,
+                                    h->g_part.as<double>(), h->g_scal.as<double>(), last ? 1 : 0);
+      H3D_CUDA(cudaMemcpy2DAsync(hk + i, sizeof(double) * (m + 1), h->g_scal.p, sizeof(double),
+                                 sizeof(double), nrhs, cudaMemcpyDeviceToDevice, s));
+      if (!last)
+        H3D_CUDA(cudaMemcpyAsync(h->g_coef.p, h->g_scal.p, sizeof(double) * nrhs,
+                                 cudaMemcpyDeviceToDevice, s));
+    }
+    // Q_{k+1} = q / h_{k+1}
+    h->launches += h3d::gmres_scale_copy(s, N, nrhs, Qn, h->g_scal.as<double>(), Qn);
+    h->launches += h3d::gmres_givens(s, k, m, nrhs, hk, h->g_H.as<double>(), h->g_cs.as<double>(),
+                                     h->g_sn.as<double>(), h->g_beta.as<double>(),
+                                     h->g_bnorm.as<double>(), h->g_err.as<double>(),
+                                     h->g_brk.as<int>());
+    H3D_CUDA(cudaMemcpyAsync(err.data(), h->g_err.p, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s));
+    H3D_CUDA(cudaStreamSynchronize(s));
+    if (hist) hist->push_back(err[0]);
+    all_done = true;
+    for (int c = 0; c < nrhs; ++c) {
+      if (!done[c] && err[c] <= tol) {
+        done[c] = 1;
+        kcol[c] = k;
+      }
+      all_done = all_done && done[c];
+    }
+  }
+  const int kdone = k;  // iterations performed
+  for (int c = 0; c < nrhs; ++c)
+    if (kcol[c] < 0) kcol[c] = kdone - 1;
+  if (kdone > 0) {
+    H3D_CUDA(cudaMemcpyAsync(h->g_kcol.p, kcol.data(), sizeof(int) * nrhs, cudaMemcpyHostToDevice, s));
+    h->launches += h3d::gmres_solve_update(s, N, nrhs, m, h->g_H.as<double>(), h->g_beta.as<double>(),
+                                           h->g_kcol.as<int>(), h->g_y.as<double>(), Q, kdone, x, N);
+  }
+  std::vector<int> brk(nrhs);
+  H3D_CUDA(cudaMemcpyAsync(brk.data(), h->g_brk.p, sizeof(int) * nrhs, cudaMemcpyDeviceToHost, s));
+  H3D_CUDA(cudaStreamSynchronize(s));
+  *breakdown_any = false;
+  for (int c = 0; c < nrhs; ++c) *breakdown_any = *breakdown_any || brk[c];
+  err_out = err;
+  *iters = kdone;
+  return HODLR3D_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int hodlr3d_abi_version(void) { return HODLR3D_ABI_VERSION; }
+
+const char* hodlr3d_last_error(void) { return g_last_error.c_str(); }
+
+void hodlr3d_default_options(hodlr3d_options* opt) {
+  if (!opt) return;
+  opt->device = 0;
+  opt->diag_override = NAN;
+  opt->keep_fp32 = 1;
+  opt->aca_workspace_bytes = 0;
+  opt->rank_cap = 0;
+}
+
+int hodlr3d_create(const double* xyz, int64_t n, int nP1D, double L, int tol_pow, int kernel_id,
+                   const hodlr3d_options* opt, hodlr3d_t* out) {
+  if (!out) return set_error(HODLR3D_ERR_INVALID_ARG, "null output handle");
+  *out = nullptr;
+  if (!xyz || n < 2) return set_error(HODLR3D_ERR_INVALID_ARG, "need at least 2 points");
+  if (n > INT32_MAX / 2) return set_error(HODLR3D_ERR_INVALID_ARG, "too many points");
+  if (nP1D < 1) return set_error(HODLR3D_ERR_INVALID_ARG, "nParticlesInLeafAlong1D must be >= 1");
+  if (!(L > 0.0)) return set_error(HODLR3D_ERR_INVALID_ARG, "L must be positive");
+  if (tol_pow < 0 || tol_pow > 30) return set_error(HODLR3D_ERR_INVALID_ARG, "TOL_POW out of range");
+  if (kernel_id < 0 || kernel_id > 16) return set_error(HODLR3D_ERR_INVALID_ARG, "unknown Qchoice %d", kernel_id);
+  if (!kernel_supported(kernel_id))
+    return set_error(HODLR3D_ERR_UNSUPPORTED, "Qchoice %d (Bessel function kernel) is not available on the device", kernel_id);
+  for (int64_t i = 0; i < 3 * n; ++i)
+    if (!std::isfinite(xyz[i])) return set_error(HODLR3D_ERR_NONFINITE, "non-finite coordinate");
+  // depth as the reference computes it (src/HODLR3D.cpp:6-7)
+  const double cubeRootN = std::pow(double(n), 1.0 / 3.0);
+  const int levels = (int)std::ceil(3 * std::log(double(cubeRootN) / nP1D) / std::log(8));
+  if (levels < 1) return set_error(HODLR3D_ERR_INVALID_ARG, "the tree would have %d levels (< 1)", levels);
+  if (levels > h3d::kMaxLevels) return set_error(HODLR3D_ERR_INVALID_ARG, "the tree would have %d levels (> %d)", levels, h3d::kMaxLevels);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return set_error(HODLR3D_ERR_NO_DEVICE, "no CUDA device");
+  hodlr3d_handle* h = new hodlr3d_handle();
+  if (opt) h->opt = *opt;
+  else hodlr3d_default_options(&h->opt);
+  h->device = h->opt.device;
+  if (h->device < 0 || h->device >= ndev) {
+    delete h;
+    return set_error(HODLR3D_ERR_INVALID_ARG, "device %d out of range", h->opt.device);
+  }
+  cudaError_t e = cudaSetDevice(h->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
+  if (e != cudaSuccess) {
+    delete h;
+    return set_error(HODLR3D_ERR_CUDA, "device setup: %s", cudaGetErrorString(e));
+  }
+  h->N = n;
+  h->nP1D = nP1D;
+  h->L = L;
+  h->tol_pow = tol_pow;
+  h->tol = std::pow(10, -1.0 * tol_pow);  // src/ACA.cpp:5
+  h->levels = levels;
+  h->kd.kind = kernel_id;
+  if (kernel_id == 16) {
+    h->kd.kii = quadrature_kii(n);
+    h->kd.h3 = 1.0 / double(n);
+  }
+  h->kd.diag = std::isnan(h->opt.diag_override) ? (kernel_id == 16 ? h->kd.kii : 0.0)
+                                                : h->opt.diag_override;
+  const int st = build_tree(h, xyz);
+  if (st != HODLR3D_OK) {
+    delete h;
+    return st;
+  }
+  *out = h;
+  return HODLR3D_OK;
+}
+
+void hodlr3d_destroy(hodlr3d_t h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  delete h;
+}
+
+int hodlr3d_assemble(hodlr3d_t h) {
+  H3D_TRY(check_handle(h));
+  return assemble(h);
+}
+
+int hodlr3d_matvec(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld, int precision,
+                   void* stream) {
+  H3D_TRY(check_handle(h));
+  return matvec_device(h, x, y, nrhs, ld, precision, (cudaStream_t)stream, false);
+}
+
+int hodlr3d_matvec_transpose(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
+                             int precision, void* stream) {
+  H3D_TRY(check_handle(h));
+  return matvec_device(h, x, y, nrhs, ld, precision, (cudaStream_t)stream, true);
+}
+
+int hodlr3d_matvec_host(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
+                        int precision) {
+  H3D_TRY(check_handle(h));
+  if (!x || !y) return set_error(HODLR3D_ERR_INVALID_ARG, "null vector");
+  if (nrhs < 1 || nrhs > 64 || ld < h->N) return set_error(HODLR3D_ERR_INVALID_ARG, "bad nrhs or ld");
+  const size_t bytes = sizeof(double) * h->N * nrhs;
+  if (bytes > h->pinned_bytes) {
+    if (h->pinned_x) cudaFreeHost(h->pinned_x);
+    if (h->pinned_y) cudaFreeHost(h->pinned_y);
+    h->pinned_x = h->pinned_y = nullptr;
+    h->pinned_bytes = 0;
+    H3D_CUDA(cudaMallocHost(&h->pinned_x, bytes));
+    H3D_CUDA(cudaMallocHost(&h->pinned_y, bytes));
+    h->pinned_bytes = bytes;
+  }
+  H3D_CUDA(h->stage_x.ensure(bytes));
+  H3D_CUDA(h->stage_y.ensure(bytes));
+  cudaStream_t s = h->stream;
+  // pack the caller's columns into pinned memory, copy in, multiply, copy out
+  double* px = static_cast<double*>(h->pinned_x);
+  double* py = static_cast<double*>(h->pinned_y);
+  for (int c = 0; c < nrhs; ++c) std::memcpy(px + c * h->N, x + c * ld, sizeof(double) * h->N);
+  H3D_CUDA(cudaMemcpyAsync(h->stage_x.p, px, bytes, cudaMemcpyHostToDevice, s));
+  H3D_TRY(matvec_device(h, h->stage_x.as<double>(), h->stage_y.as<double>(), nrhs, h->N, precision, s, false));
+  H3D_CUDA(cudaMemcpyAsync(py, h->stage_y.p, bytes, cudaMemcpyDeviceToHost, s));
+  H3D_CUDA(cudaStreamSynchronize(s));
+  for (int c = 0; c < nrhs; ++c) std::memcpy(y + c * ld, py + c * h->N, sizeof(double) * h->N);
+  return HODLR3D_OK;
+}
+
+int hodlr3d_dense_rows(hodlr3d_t h, const int64_t* rows, int64_t nrows, const double* x, double* y,
+                       int nrhs, int64_t ldx, void* stream) {
+  H3D_TRY(check_handle(h));
+  if (!rows || !x || !y || nrows < 0 || nrhs < 1 || ldx < h->N)
+    return set_error(HODLR3D_ERR_INVALID_ARG, "bad arguments");
+  h3d::launch_dense_rows((cudaStream_t)stream, h->N, h->xyz.as<double>(), h->kd,
+                         rows, nrows, x, ldx, y, nrhs);
+  ++h->launches;
+  H3D_CUDA(cudaGetLastError());
+  return HODLR3D_OK;
+}
+
+int hodlr3d_gmres(hodlr3d_t h, const double* b, double* x, int nrhs, int64_t ld,
+                  const hodlr3d_gmres_params* prm, hodlr3d_gmres_result* res, double* hist,
+                  int hist_cap, int* n_hist, void* stream) {
+  H3D_TRY(check_handle(h));
+  if (!h->assembled) return set_error(HODLR3D_ERR_NOT_ASSEMBLED, "hodlr3d_assemble has not run");
+  if (!b || !x || !prm || nrhs < 1 || nrhs > 64 || ld < h->N || prm->maxit < 1 || !(prm->tol > 0))
+    return set_error(HODLR3D_ERR_INVALID_ARG, "bad GMRES arguments");
+  // inputs may still be in flight on the caller's stream
+  H3D_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  cudaStream_t s = h->stream;
+  const int64_t N = h->N;
+  const int64_t vec = N * nrhs;
+  H3D_CUDA(h->g_b.ensure(sizeof(double) * vec));
+  H3D_CUDA(h->g_x.ensure(sizeof(double) * vec));
+  H3D_CUDA(h->g_d.ensure(sizeof(double) * vec));
+  h->launches += h3d::gmres_pack(s, N, nrhs, b, ld, h->g_b.as<double>(), N);
+  H3D_CUDA(cudaMemsetAsync(h->g_x.p, 0, sizeof(double) * vec, s));
+  H3D_CUDA(h->g_part.ensure(sizeof(double) * nrhs * 1024));
+  H3D_CUDA(h->g_scal.ensure(sizeof(double) * nrhs));
+  h->launches += h3d::gmres_dot(s, N, nrhs, h->g_b.as<double>(), nullptr, nullptr, nullptr, 0, 1,
+                                h->g_part.as<double>(), h->g_scal.as<double>(), 1);
+  std::vector<double> bnorm(nrhs);
+  H3D_CUDA(cudaMemcpyAsync(bnorm.data(), h->g_scal.p, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s));
+  H3D_CUDA(cudaStreamSynchronize(s));
+  for (int c = 0; c < nrhs; ++c)
+    if (bnorm[c] == 0.0) bnorm[c] = 1.0;  // b = 0: x = 0 is exact
+  const bool trans = prm->transpose != 0;
+  std::vector<double> history, err;
+  std::vector<double>* hp = hist ? &history : nullptr;
+  if (hp) hp->push_back(1.0);
+  int total_it = 0, outer = 0;
+  bool brk = false, converged = false;
+  double final_err = 0.0;
+  if (prm->precision == HODLR3D_FP64) {
+    const int m = prm->restart > 0 ? prm->restart : prm->maxit;
+    bool first = true;
+    while (total_it < prm->maxit) {
+      int it = 0;
+      const int mm = std::min(m, prm->maxit - total_it);
+      H3D_TRY(gmres_cycle(h, h->g_b.as<double>(), h->g_x.as<double>(), nrhs, mm, prm->tol, HODLR3D_FP64,
+                          trans, first, bnorm, &it, err, hp, &brk));
+      first = false;
+      total_it += it;
+      ++outer;
+      final_err = *std::max_element(err.begin(), err.end());
+      converged = final_err <= prm->tol;
+      if (converged || prm->restart <= 0 || it == 0) break;
+    }
+  } else {
+    // iterative refinement: FP64 residual, FP32-matvec inner GMRES(m) on the correction
+    const int m = prm->restart > 0 ? prm->restart : 30;
+    const int max_outer = prm->max_outer > 0 ? prm->max_outer : 20;
+    const double itol = prm->inner_tol > 0 ? prm->inner_tol : 1e-5;
+    double* r = h->g_d.as<double>();
+    H3D_CUDA(cudaMemcpyAsync(r, h->g_b.p, sizeof(double) * vec, cudaMemcpyDeviceToDevice, s));
+    DevBuf dx, wtmp;
+    H3D_CUDA(dx.ensure(sizeof(double) * vec));
+    H3D_CUDA(wtmp.ensure(sizeof(double) * vec));
+    for (outer = 0; outer < max_outer && total_it < prm->maxit; ++outer) {
+      // relative residual of the current x in FP64
+      h->launches += h3d::gmres_dot(s, N, nrhs, r, nullptr, nullptr, nullptr, 0, 1,
+                                    h->g_part.as<double>(), h->g_scal.as<double>(), 1);
+      std::vector<double> rn(nrhs);
+      H3D_CUDA(cudaMemcpyAsync(rn.data(), h->g_scal.p, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s));
+      H3D_CUDA(cudaStreamSynchronize(s));
+      final_err = 0.0;
+      for (int c = 0; c < nrhs; ++c) final_err = std::max(final_err, rn[c] / bnorm[c]);
+      if (hp && outer > 0) hp->push_back(final_err);
+      if (final_err <= prm->tol) {
+        converged = true;
+        break;
+      }
+      // inner solve A d = r to relative accuracy itol (restarted until reached)
+      H3D_CUDA(cudaMemsetAsync(dx.p, 0, sizeof(double) * vec, s));
+      int inner_total = 0;
+      bool first = true;
+      while (inner_total < prm->maxit - total_it) {
+        int it = 0;
+        const int mm = std::min(m, prm->maxit - total_it - inner_total);
+        H3D_TRY(gmres_cycle(h, r, dx.as<double>(), nrhs, mm, itol, HODLR3D_MIXED, trans, first, rn,
+                            &it, err, nullptr, &brk));
+        first = false;
+        inner_total += it;
+        if (*std::max_element(err.begin(), err.end()) <= itol || it == 0) break;
+      }
+      total_it += inner_total;
+      h->launches += h3d::gmres_add(s, vec, dx.as<double>(), h->g_x.as<double>());
+      // r = b - A x in FP64
+      H3D_TRY(matvec_device(h, h->g_x.as<double>(), wtmp.as<double>(), nrhs, N, HODLR3D_FP64, s, trans));
+      h->launches += h3d::gmres_sub(s, vec, h->g_b.as<double>(), wtmp.as<double>(), r);
+    }
+    if (!converged) {
+      h->launches += h3d::gmres_dot(s, N, nrhs, r, nullptr, nullptr, nullptr, 0, 1,
+                                    h->g_part.as<double>(), h->g_scal.as<double>(), 1);
+      std::vector<double> rn(nrhs);
+      H3D_CUDA(cudaMemcpyAsync(rn.data(), h->g_scal.p, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s));
+      H3D_CUDA(cudaStreamSynchronize(s));
+      final_err = 0.0;
+      for (int c = 0; c < nrhs; ++c) final_err = std::max(final_err, rn[c] / bnorm[c]);
+      converged = final_err <= prm->tol;
+    }
+  }
+  h->launches += h3d::gmres_pack(s, N, nrhs, h->g_x.as<double>(), N, x, ld);
+  H3D_CUDA(cudaStreamSynchronize(s));
+  if (res) {
+    res->iterations = total_it;
+    res->outer = outer;
+    res->rel_residual = final_err;
+    res->converged = converged ? 1 : 0;
+  }
+  if (hist && n_hist) {
+    const int nh = std::min<int>(hist_cap, (int)history.size());
+    for (int i = 0; i < nh; ++i) hist[i] = history[i];
+    *n_hist = nh;
+  }
+  if (!converged) {
+    if (brk) return set_error(HODLR3D_ERR_BREAKDOWN, "GMRES breakdown before the tolerance");
+    return set_error(HODLR3D_ERR_NO_CONVERGENCE, "GMRES reached %d iterations at %.3e", total_it, final_err);
+  }
+  return HODLR3D_OK;
+}
+
+int hodlr3d_get_stats(hodlr3d_t h, hodlr3d_stats* s) {
+  if (!h || !s) return set_error(HODLR3D_ERR_INVALID_ARG, "null argument");
+  std::memset(s, 0, sizeof(*s));
+  s->n_points = h->N;
+  s->levels = h->levels;
+  s->n_pairs = h->npairs;
+  s->max_rank = h->max_rank;
+  s->sum_rank = h->sum_rank;
+  s->factor_entries = h->factor_entries;
+  s->factor_bytes_fp64 = h->factor_entries * 8;
+  s->factor_bytes_fp32 = h->opt.keep_fp32 ? h->factor_entries * 4 : 0;
+  s->tree_seconds = h->tree_seconds;
+  s->assemble_seconds = h->assemble_seconds;
+  s->aca_batches = h->aca_batches;
+  // near blocks and the reference's memory count (findMemory, src/HODLR3DTree.cpp:1757-1778)
+  const int d = h->levels;
+  double mem = 0.0;
+  int64_t nb = 0, ne = 0;
+  std::vector<int32_t> nbl(26 * h->nleaf);
+  if (cudaMemcpy(nbl.data(), h->nbr_leaf.p, sizeof(int32_t) * 26 * h->nleaf, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return set_error(HODLR3D_ERR_CUDA, "copy of the neighbour table failed");
+  for (int64_t k = 0; k < h->nleaf; ++k) {
+    const int64_t n = h->h_leaf_off[k + 1] - h->h_leaf_off[k];
+    ++nb;
+    ne += n * n;
+    for (int sl = 0; sl < 26; ++sl) {
+      const int32_t q = nbl[26 * k + sl];
+      if (q < 0) continue;
+      ++nb;
+      ne += n * (int64_t)(h->h_leaf_off[q + 1] - h->h_leaf_off[q]);
+    }
+  }
+  if (h->assembled) {
+    for (int64_t p = 0; p < h->npairs; ++p) {
+      const int j = h->h_pair_level[p];
+      int64_t a0, a1, b0, b1;
+      box_range(h, j, h->h_pair_tgt[p] - h3d::level_base(j), a0, a1);
+      box_range(h, j, h->h_pair_src[p] - h3d::level_base(j), b0, b1);
+      const double r = h->h_rank[p];
+      mem += r * double(a1 - a0) + r * r + double(b1 - b0) * r;
+    }
+  }
+  mem += (double)ne;
+  (void)d;
+  s->n_near_blocks = nb;
+  s->near_entries = ne;
+  s->memory_entries = mem;
+  return HODLR3D_OK;
+}
+
+int hodlr3d_get_tree(hodlr3d_t h, int32_t* perm, int64_t* leaf_off) {
+  if (!h) return set_error(HODLR3D_ERR_INVALID_ARG, "null handle");
+  if (perm) std::copy(h->h_perm.begin(), h->h_perm.end(), perm);
+  if (leaf_off)
+    for (int64_t k = 0; k <= h->nleaf; ++k) leaf_off[k] = h->h_leaf_off[k];
+  return HODLR3D_OK;
+}
+
+int hodlr3d_get_neighbors(hodlr3d_t h, int level, int32_t* nbr) {
+  H3D_TRY(check_handle(h));
+  if (!nbr || level < 0 || level > h->levels) return set_error(HODLR3D_ERR_INVALID_ARG, "bad level");
+  const int64_t nb = int64_t(1) << (3 * level);
+  H3D_CUDA(cudaMemcpy(nbr, h->nbr_all.as<int32_t>() + 26 * h3d::level_base(level),
+                      sizeof(int32_t) * 26 * nb, cudaMemcpyDeviceToHost));
+  return HODLR3D_OK;
+}
+
+int hodlr3d_get_pairs(hodlr3d_t h, int32_t* lts) {
+  if (!h || !lts) return set_error(HODLR3D_ERR_INVALID_ARG, "null argument");
+  for (int64_t p = 0; p < h->npairs; ++p) {
+    const int j = h->h_pair_level[p];
+    lts[3 * p] = j;
+    lts[3 * p + 1] = (int32_t)(h->h_pair_tgt[p] - h3d::level_base(j));
+    lts[3 * p + 2] = (int32_t)(h->h_pair_src[p] - h3d::level_base(j));
+  }
+  return HODLR3D_OK;
+}
+
+int hodlr3d_get_ranks(hodlr3d_t h, int32_t* rank) {
+  if (!h || !rank) return set_error(HODLR3D_ERR_INVALID_ARG, "null argument");
+  if (!h->assembled) return set_error(HODLR3D_ERR_NOT_ASSEMBLED, "not assembled");
+  std::copy(h->h_rank.begin(), h->h_rank.end(), rank);
+  return HODLR3D_OK;
+}
+
+int hodlr3d_get_pivots(hodlr3d_t h, int32_t* rows, int32_t* cols) {
+  if (!h || !rows || !cols) return set_error(HODLR3D_ERR_INVALID_ARG, "null argument");
+  if (!h->assembled) return set_error(HODLR3D_ERR_NOT_ASSEMBLED, "not assembled");
+  int64_t w = 0;
+  for (int64_t p = 0; p < h->npairs; ++p) {
+    const int j = h->h_pair_level[p];
+    int64_t a0, a1, b0, b1;
+    box_range(h, j, h->h_pair_tgt[p] - h3d::level_base(j), a0, a1);
+    box_range(h, j, h->h_pair_src[p] - h3d::level_base(j), b0, b1);
+    for (int r = 0; r < h->h_rank[p]; ++r) {
+      rows[w] = h->h_perm[a0 + h->h_piv_rows[p][r]];
+      cols[w] = h->h_perm[b0 + h->h_piv_cols[p][r]];
+      ++w;
+    }
+  }
+  return HODLR3D_OK;
+}
+
+int hodlr3d_get_pair_factors(hodlr3d_t h, int64_t pair, double* U, double* V) {
+  H3D_TRY(check_handle(h));
+  if (!h->assembled) return set_error(HODLR3D_ERR_NOT_ASSEMBLED, "not assembled");
+  if (pair < 0 || pair >= h->npairs) return set_error(HODLR3D_ERR_INVALID_ARG, "pair out of range");
+  const int j = h->h_pair_level[pair];
+  int64_t a0, a1, b0, b1;
+  box_range(h, j, h->h_pair_tgt[pair] - h3d::level_base(j), a0, a1);
+  box_range(h, j, h->h_pair_src[pair] - h3d::level_base(j), b0, b1);
+  const int64_t r = h->h_rank[pair];
+  if (U && r) H3D_CUDA(cudaMemcpy(U, h->h_u64[pair], sizeof(double) * r * (a1 - a0), cudaMemcpyDeviceToHost));
+  if (V && r) H3D_CUDA(cudaMemcpy(V, h->h_v64[pair], sizeof(double) * r * (b1 - b0), cudaMemcpyDeviceToHost));
+  return HODLR3D_OK;
+}
+
+int64_t hodlr3d_launch_count(hodlr3d_t h) { return h ? h->launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,167 @@
+/* hodlr3d_gb300 -- C ABI of the GB300-native HODLR3D path (tree build, ACA
+ * assembly, fast matvec, GMRES) on one GPU.
+ *
+ * Plain pointers and sizes only.  Every call returns an int status
+ * (HODLR3D_OK = 0); nothing aborts.  hodlr3d_last_error() describes the last
+ * failure of the calling thread.
+ *
+ * Each entry point names the reference interface it replaces (paths inside the
+ * SAFRAN-LAB/HODLR3D source tree).
+ */
+#ifndef HODLR3D_GB300_H
+#define HODLR3D_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HODLR3D_ABI_VERSION 1
+
+typedef struct hodlr3d_handle* hodlr3d_t;
+
+enum hodlr3d_status {
+  HODLR3D_OK = 0,
+  HODLR3D_ERR_INVALID_ARG = 1,   /* bad size, pointer, kernel id or option */
+  HODLR3D_ERR_CUDA = 2,          /* a CUDA call failed (message in last_error) */
+  HODLR3D_ERR_OUT_OF_MEMORY = 3, /* device or host allocation failed */
+  HODLR3D_ERR_NOT_ASSEMBLED = 4, /* matvec / solve before hodlr3d_assemble */
+  HODLR3D_ERR_NONFINITE = 5,     /* NaN or Inf met in kernel entries or vectors */
+  HODLR3D_ERR_BREAKDOWN = 6,     /* GMRES Arnoldi breakdown (h(k+1,k) == 0) */
+  HODLR3D_ERR_NO_CONVERGENCE = 7,/* GMRES stopped at maxit above the tolerance */
+  HODLR3D_ERR_UNSUPPORTED = 8,   /* kernel or feature not available on the device */
+  HODLR3D_ERR_NO_DEVICE = 9      /* no usable CUDA device */
+};
+
+enum hodlr3d_precision {
+  HODLR3D_FP64 = 0, /* FP64 end to end (matches the reference's FP64 matvec) */
+  HODLR3D_MIXED = 1 /* FP32 factors and near field, FP64 accumulation across tiles */
+};
+
+/* Options of hodlr3d_create; fill with hodlr3d_default_options first. */
+typedef struct hodlr3d_options {
+  int device;                 /* CUDA device ordinal (0) */
+  double diag_override;       /* NaN: the reference diagonal (Kii for kernel 16, else 0) */
+  int keep_fp32;              /* also keep FP32 copies of the factors for HODLR3D_MIXED (1) */
+  size_t aca_workspace_bytes; /* device workspace for one assembly batch (0: 8 GiB) */
+  int rank_cap;               /* first per-pair rank capacity above leaf size (0: 256) */
+} hodlr3d_options;
+
+typedef struct hodlr3d_stats {
+  int64_t n_points;
+  int levels;               /* octree depth (reference nLevels, src/HODLR3D.cpp:7) */
+  int64_t n_pairs;          /* compressed interaction-list pairs, levels 1..levels */
+  int64_t n_near_blocks;    /* dense leaf blocks (self + face/edge neighbours) */
+  int max_rank;             /* reference HODLR3DTree::getMaxRank */
+  int64_t sum_rank;         /* sum of pair ranks */
+  double memory_entries;    /* reference HODLR3DTree::findMemory count */
+  int64_t factor_entries;   /* sum over pairs of rank * (n + m) */
+  int64_t factor_bytes_fp64;
+  int64_t factor_bytes_fp32;
+  int64_t near_entries;     /* sum over near blocks of n * m */
+  double tree_seconds;      /* last hodlr3d_create, device tree + lists */
+  double assemble_seconds;  /* last hodlr3d_assemble */
+  int aca_batches;          /* assembly batches of the last hodlr3d_assemble */
+} hodlr3d_stats;
+
+typedef struct hodlr3d_gmres_params {
+  int maxit;        /* Krylov iterations (unrestarted) or per cycle when restart > 0 */
+  int restart;      /* 0: unrestarted as the reference; m > 0: GMRES(m) */
+  double tol;       /* relative residual |r| / |b| to reach */
+  int precision;    /* HODLR3D_FP64: plain GMRES; HODLR3D_MIXED: FP32 inner GMRES(restart)
+                       with FP64 outer residual (iterative refinement) */
+  int max_outer;    /* HODLR3D_MIXED: refinement steps (0: 20) */
+  double inner_tol; /* HODLR3D_MIXED: inner relative tolerance (0: 1e-5) */
+  int transpose;    /* solve A^T x = b (adjoint) instead of A x = b */
+} hodlr3d_gmres_params;
+
+typedef struct hodlr3d_gmres_result {
+  int iterations;        /* total Krylov iterations (max over right-hand sides) */
+  int outer;             /* refinement steps (mixed) */
+  double rel_residual;   /* max over RHS of the final estimate |r| / |b| */
+  int converged;         /* all right-hand sides reached tol */
+} hodlr3d_gmres_result;
+
+/* ---- life cycle ------------------------------------------------------ */
+int hodlr3d_abi_version(void);
+void hodlr3d_default_options(hodlr3d_options* opt);
+const char* hodlr3d_last_error(void);
+
+/* Builds the kernel and the uniform octree with its neighbour slots and
+ * interaction lists on the device.  Replaces HODLR3D::HODLR3D(nParticlesInLeafAlong1D,
+ * L, TOL_POW, Qchoice, particles) (include/HODLR3D.hpp:18, src/HODLR3D.cpp:3-15).
+ * xyz: host array of n points, x y z interleaved (the reference's pts3D).
+ * kernel_id: the reference's Qchoice (src/kernel.cpp:65-227); 0-10, 13, 15, 16
+ * run on the device, 11, 12, 14 (Bessel) return HODLR3D_ERR_UNSUPPORTED. */
+int hodlr3d_create(const double* xyz, int64_t n, int nP1D, double L, int tol_pow, int kernel_id,
+                   const hodlr3d_options* opt, hodlr3d_t* out);
+
+/* Frees everything (HODLR3D::~HODLR3D, src/HODLR3D.cpp:29-32). */
+void hodlr3d_destroy(hodlr3d_t h);
+
+/* Partially pivoted ACA of every interaction-list pair.  Replaces
+ * HODLR3D::assemble -> HODLR3DTree::getUVtTree (src/HODLR3D.cpp:17-19,
+ * src/HODLR3DTree.cpp:1621-1645, src/ACA.cpp:127-238). */
+int hodlr3d_assemble(hodlr3d_t h);
+
+/* ---- products -------------------------------------------------------- */
+/* y = A x for nrhs columns (column-major, leading dimension ld >= n), device
+ * pointers, enqueued on `stream` (a cudaStream_t; NULL is the CUDA default
+ * stream); the call returns once the work is enqueued.  Calls on one handle
+ * share its work buffers and must not overlap in time (as the reference's
+ * facade, which is not re-entrant).  Replaces HODLR3D::MatVecProduct(b, Ab)
+ * (src/HODLR3D.cpp:21-27).  1 <= nrhs <= 64. */
+int hodlr3d_matvec(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld, int precision,
+                   void* stream);
+/* Same with host pointers: copies in, multiplies, copies out, synchronises. */
+int hodlr3d_matvec_host(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
+                        int precision);
+/* y = A^T x with the transposed operator (V (U^T x) on compressed pairs,
+ * transposed near field).  No reference counterpart (the reference has no
+ * transpose product); device pointers. */
+int hodlr3d_matvec_transpose(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
+                             int precision, void* stream);
+/* y[r] = sum_j K(rows[r], j) x[j], the dense FP64 product of sampled rows
+ * (the reference drivers' check by columns, kernel::getCol,
+ * src/kernel.cpp:27-35; K symmetric).  Device pointers, nrhs columns. */
+int hodlr3d_dense_rows(hodlr3d_t h, const int64_t* rows, int64_t nrows, const double* x,
+                       double* y, int nrhs, int64_t ldx, void* stream);
+
+/* ---- solve ----------------------------------------------------------- */
+/* GMRES from x0 = 0 for nrhs right-hand sides (device pointers, column-major).
+ * Replaces classGMRES::gmres(M, b, maxIterations, threshold, x, error,
+ * noOfIterations, e) (include/gmres.hpp:23, src/gmres.cpp:40-94).
+ * hist (optional, host, hist_cap values): relative residual estimates of
+ * the first right-hand side, as the reference's e vector; *n_hist receives
+ * the count.  Waits for `stream` before it starts and returns with x ready. */
+int hodlr3d_gmres(hodlr3d_t h, const double* b, double* x, int nrhs, int64_t ld,
+                  const hodlr3d_gmres_params* prm, hodlr3d_gmres_result* res, double* hist,
+                  int hist_cap, int* n_hist, void* stream);
+
+/* ---- introspection (parity tests, statistics) --------------------------- */
+int hodlr3d_get_stats(hodlr3d_t h, hodlr3d_stats* s);
+/* perm[t]: original index of the t-th point in tree order (host, n values);
+ * leaf_off: 8^levels + 1 offsets of the leaves in tree order (host). */
+int hodlr3d_get_tree(hodlr3d_t h, int32_t* perm, int64_t* leaf_off);
+/* neighbour slots of every box of one level, 8^level x 26 (host; -1 = none);
+ * the reference's HODLR3DBox::neighborNumbers (include/HODLR3DTree.hpp:16). */
+int hodlr3d_get_neighbors(hodlr3d_t h, int level, int32_t* nbr);
+/* (level, target box, source box) of every pair, sorted (host, 3 x n_pairs);
+ * the reference's HODLR3DBox::interactionList (include/HODLR3DTree.hpp:17). */
+int hodlr3d_get_pairs(hodlr3d_t h, int32_t* level_tgt_src);
+/* per-pair rank (host, n_pairs) and the global ids of the row and column
+ * pivots concatenated in pair order (host, sum_rank each); the reference's
+ * L[i].cols(), row_basis[i], col_basis[i] (include/HODLR3DTree.hpp:20-21). */
+int hodlr3d_get_ranks(hodlr3d_t h, int32_t* rank);
+int hodlr3d_get_pivots(hodlr3d_t h, int32_t* rows, int32_t* cols);
+/* U (n x r) and V (m x r) FP64 factors of one pair, column-major (host). */
+int hodlr3d_get_pair_factors(hodlr3d_t h, int64_t pair, double* U, double* V);
+/* number of kernel launches issued by the library since creation */
+int64_t hodlr3d_launch_count(hodlr3d_t h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,71 @@
+"""The C-ABI library builds, loads and exports every entry point that
+include/*.h declares; host-only calls behave (no GPU needed)."""
+import ctypes
+import glob
+import math
+import os
+import re
+
+import pytest
+
+from hodlr3d_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"\b(hodlr3d_[a-z0-9_]+)\s*\(", src):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_headers_declare_the_abi():
+    names = declared_functions()
+    for must in ("hodlr3d_create", "hodlr3d_assemble", "hodlr3d_matvec", "hodlr3d_gmres",
+                 "hodlr3d_destroy", "hodlr3d_last_error", "hodlr3d_matvec_transpose"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.lib()
+    missing = [n for n in declared_functions() if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_abi_version_and_default_options():
+    L = _lib.lib()
+    assert L.hodlr3d_abi_version() == 1
+    o = _lib.Options()
+    L.hodlr3d_default_options(ctypes.byref(o))
+    assert o.device == 0 and o.keep_fp32 == 1 and math.isnan(o.diag_override)
+
+
+def test_invalid_arguments_fail_cleanly():
+    L = _lib.lib()
+    h = ctypes.c_void_p()
+    import numpy as np
+    pts = np.zeros((10, 3))
+    # bad kernel id
+    code = L.hodlr3d_create(pts.ctypes.data, 10, 4, 1.0, 10, 42, None, ctypes.byref(h))
+    assert code == _lib.ERR_INVALID_ARG and not h.value
+    # Bessel kernels are not offered on the device
+    code = L.hodlr3d_create(pts.ctypes.data, 10, 4, 1.0, 10, 11, None, ctypes.byref(h))
+    assert code == _lib.ERR_UNSUPPORTED
+    assert b"Bessel" in L.hodlr3d_last_error()
+    # null handle
+    assert L.hodlr3d_assemble(None) == _lib.ERR_INVALID_ARG
+
+
+def test_no_device_or_tree_error_is_reported():
+    """Without a GPU creation reports ERR_NO_DEVICE; with one, a too-shallow tree is refused."""
+    import numpy as np
+    L = _lib.lib()
+    h = ctypes.c_void_p()
+    pts = np.random.default_rng(0).uniform(-1, 1, (64, 3))
+    code = L.hodlr3d_create(pts.ctypes.data, 64, 4, 1.0, 10, 16, None, ctypes.byref(h))
+    assert code in (_lib.ERR_NO_DEVICE, _lib.ERR_INVALID_ARG)
+    assert not h.value
