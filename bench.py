@@ -1,0 +1,387 @@
+"""Benchmark: right-hand sides per second of the HODLR3D matvec and GMRES solve
+at N = 64^3 (1/r with the quadrature diagonal, ACA tol 1e-10, leaf 64).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = one matvec of 32 right-hand sides in the mixed form (FP32 factors
+and near field, FP64 accumulation across tiles) with the inputs resident in
+HBM.  `e2e` is the same product through the C-ABI host entry point
+(hodlr3d_matvec_host: host buffers, copies inside the timed region).  The
+FP64 form at one right-hand side and the GMRES solves are reported beside it.
+`--impl reference` times the reference algorithm on the host cores (the CPU
+oracle port of it, since the reference itself cannot be built on the GPU
+host) on a bounded sample of the same workload.  For N > 1 (torchrun) every
+rank runs an independent replica; value = all ranks' right-hand sides / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RHS/sec (matvec, GMRES) at N=64^3, 1/r, 1e-6 err: mixed+batched vs FP64 GPU"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)),
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ----------------------------------------------------------------------------
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("H3D_BACKEND") != "gloo" else "gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, v: float) -> float:
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------------------
+def cpu_sample(pts, tol_pow, steps, warmup, threads, n_leaves=16):
+    """Times the reference algorithm (the CPU oracle, CUR form with the kernel
+    entries re-evaluated as src/HODLR3DTree.cpp:1660-1755 does) on a bounded
+    sample: the far field of the ancestors of n_leaves spread-out leaves at
+    every level plus their near field, each level scaled by its box count.
+    Returns seconds per full matvec (one right-hand side) per step."""
+    from oracle import oracle as orc
+    orc.set_threads(threads)
+    o = orc.Oracle(pts, 4, 1.0, tol_pow, 16)
+    d = o.levels
+    nleaf = 8 ** d
+    leaves = np.linspace(0, nleaf - 1, n_leaves).astype(np.int64)
+    sel = {j: sorted({int(l >> (3 * (d - j))) for l in leaves}) for j in range(1, d + 1)}
+    lv = np.concatenate([[j] * len(b) for j, b in sel.items()]).astype(np.int32)
+    bx = np.concatenate([b for b in sel.values()]).astype(np.int32)
+    t = time.perf_counter()
+    o.assemble(lv, bx)
+    t_aca = time.perf_counter() - t
+    x = np.random.default_rng(5).standard_normal(o.N)
+    out = []
+    for it in range(warmup + steps):
+        total = 0.0
+        for j in range(1, d + 1):
+            b = np.array(sel[j], np.int32)
+            t = time.perf_counter()
+            o.matvec(x, np.full(len(b), j, np.int32), b)
+            total += (time.perf_counter() - t) * (8 ** j) / len(b)
+        if it >= warmup:
+            out.append(total)
+    desc = (f"far field of the ancestors of {n_leaves} spread leaves at every level "
+            f"({', '.join(f'L{j}:{len(b)}/{8**j}' for j, b in sel.items())} target boxes) plus their "
+            f"near field, CUR form with re-evaluated entries as the reference, scaled by box count; "
+            f"sample ACA {t_aca:.1f}s")
+    return out, desc
+
+
+def run_reference(args):
+    ws, rank, _ = dist_init()
+    if rank != 0:
+        return
+    from hodlr3d_gb300.workloads import grid_cell_centres
+    pts = grid_cell_centres(args.n)
+    threads = os.cpu_count() or 1
+    secs, desc = cpu_sample(pts, args.tol_pow, args.steps, args.warmup, threads)
+    s = float(np.mean(secs))
+    v = 1.0 / s
+    line = {
+        "metric": METRIC, "value": v, "unit": "RHS/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": s * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "impl": "reference",
+        "config": config(args),
+        "cpu_baseline": {"value": v, "unit": "RHS/s", "cores": threads, "kind": "port",
+                         "sample": desc},
+        "e2e": {"value": v, "unit": "RHS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config(args):
+    return {"workload": f"HODLR3D matvec, {args.n}^3 grid cell centres on [-1,1]^3, leaf 64 "
+                        f"(nP1D 4), kernel 1/r with quadrature diagonal (Qchoice 16), ACA tol "
+                        f"1e-{args.tol_pow}, {args.nrhs} right-hand sides N(0,1)",
+            "N": args.n ** 3, "nrhs": args.nrhs, "precision": "mixed (FP32 factors and near field, "
+            "FP64 accumulation across tiles)", "tol_pow": args.tol_pow,
+            "l2": "inputs larger than L2 (the FP32 factors alone exceed 129 MB by two orders)"}
+
+
+# ----------------------------------------------------------------------------
+def level_bytes(H, nr_pad, s):
+    """Algorithmic bytes per launch of the matvec kernels."""
+    P = H.pairs()
+    R = H.ranks().astype(np.int64)
+    off = H.leaf_offsets()
+    d = int(P[:, 0].max()) if len(P) else 0
+    N = H.N
+
+    def sizes(level, boxes):
+        sh = 3 * (d - level)
+        return off[(boxes + 1) << sh] - off[boxes << sh]
+
+    n = np.zeros(len(P), np.int64)
+    m = np.zeros(len(P), np.int64)
+    for j in range(1, d + 1):
+        sel = P[:, 0] == j
+        n[sel] = sizes(j, P[sel, 1].astype(np.int64))
+        m[sel] = sizes(j, P[sel, 2].astype(np.int64))
+    leaf = P[:, 0] == d
+    up = ~leaf
+    xb = N * nr_pad * s
+    b = {
+        "gather": N * 8 * min(nr_pad, 64) + xb,
+        "vtx": int((R[up] * m[up]).sum()) * s + xb + int(R[up].sum()) * nr_pad * 8,
+        "ut": int((R[up] * n[up]).sum()) * s + int(R[up].sum()) * nr_pad * s + N * nr_pad * 8,
+        "leaf": int((R[leaf] * (n[leaf] + m[leaf])).sum()) * s + xb + N * nr_pad * 8 + N * nr_pad * 8,
+    }
+    return b
+
+
+def run_ours(args):
+    import torch
+
+    from hodlr3d_gb300 import HODLR3D
+    from hodlr3d_gb300.workloads import charges_normal, charges_uniform, grid_cell_centres
+
+    ws, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pts = grid_cell_centres(args.n)
+    N = len(pts)
+    t = time.perf_counter()
+    H = HODLR3D(4, 1.0, args.tol_pow, 16, pts, device=local)
+    H.assemble()
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter() - t
+    st = H.stats()
+    nrhs = args.nrhs
+    X = torch.tensor(charges_normal(N, nrhs, seed=11), device=dev)
+    x1 = X[:, 0].contiguous()
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        barrier(ws)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(ws)
+        return e0.elapsed_time(e1) / steps
+
+    # accuracy against the dense FP64 product on sampled rows
+    rows = np.sort(np.random.default_rng(3).choice(N, 512, replace=False))
+    Yd = H.dense_rows(rows, X)
+    ridx = torch.as_tensor(rows, device=dev)
+
+    def col_err(Y):
+        D = Yd.reshape(len(rows), -1)
+        return float((torch.linalg.norm(Y.reshape(N, -1)[ridx] - D, dim=0) /
+                      torch.linalg.norm(D, dim=0)).max().item())
+
+    err_mixed = col_err(H.matvec(X, "mixed"))
+    err_fp64 = col_err(H.matvec(X, "fp64"))
+
+    # ---- headline: mixed, nrhs columns, device resident ------------------
+    launches0 = H.launch_count()
+    clk = ClockSampler(local)
+    clk.start()
+    ms = timed(lambda: H.matvec(X, "mixed"), args.steps, args.warmup)
+    clocks = clk.stop()
+    launches = (H.launch_count() - launches0) // (args.steps + args.warmup)
+    ms_max = max_over_ranks(ws, ms)
+    value = ws * nrhs / (ms_max * 1e-3)
+
+    # ---- FP64 form, one right-hand side ----------------------------------
+    ms64 = timed(lambda: H.matvec(x1, "fp64"), max(3, args.steps // 2), 2)
+
+    # ---- per-kernel times (events between launches) -> roofline ----------
+    H.set_profiling(True)
+    nprof = max(3, args.steps // 2)
+    for _ in range(nprof):
+        H.matvec(X, "mixed")
+    torch.cuda.synchronize()
+    rep = H.profile_report()
+    H.set_profiling(False)
+    kern_ms = {k: v[1] / v[0] for k, v in rep.items()}
+    nr_pad = 1 << (nrhs - 1).bit_length()
+    alg = level_bytes(H, nr_pad, 4)
+    top = max(kern_ms, key=kern_ms.get)
+    hbm, peak_kind = peaks()
+    achieved = alg[top] / (kern_ms[top] * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": f"k_{top}", "achieved": achieved, "peak": hbm,
+            "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+            "kernel_ms": kern_ms, "algorithmic_bytes": alg,
+            "whole_matvec_GBps": sum(alg.values()) / (ms * 1e-3) / 1e9}
+
+    # ---- GMRES: b = A x_true, x_true U[0,1) ------------------------------
+    xt = torch.tensor(charges_uniform(N, nrhs, seed=21), device=dev)
+    B = H.matvec(xt, "fp64")
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    Xs, info = H.gmres(B, maxit=300, tol=1e-10, restart=30, precision="mixed")
+    torch.cuda.synchronize()
+    t_mixed = time.perf_counter() - t
+    fwd_mixed = float((torch.linalg.norm(Xs - xt, dim=0) / torch.linalg.norm(xt, dim=0)).max())
+    b1 = B[:, 0].contiguous()
+    t = time.perf_counter()
+    x64, info64 = H.gmres(b1, maxit=400, tol=1e-10, restart=0, precision="fp64")
+    torch.cuda.synchronize()
+    t_fp64 = time.perf_counter() - t
+    gmres = {"mixed_rhs_per_s": nrhs / t_mixed, "mixed_seconds": t_mixed,
+             "mixed_iterations": info["iterations"], "mixed_outer": info["outer"],
+             "mixed_rel_residual": info["rel_residual"], "mixed_forward_err": fwd_mixed,
+             "fp64_rhs_per_s": 1.0 / t_fp64, "fp64_seconds": t_fp64,
+             "fp64_iterations": info64["iterations"], "fp64_rel_residual": info64["rel_residual"],
+             "speedup_mixed_batched_vs_fp64": (nrhs / t_mixed) / (1.0 / t_fp64)}
+
+    # ---- e2e through the C ABI with host buffers -------------------------
+    Xh = np.ascontiguousarray(X.cpu().numpy())
+    for _ in range(2):
+        H.MatVecProduct(Xh, "mixed")
+    t = time.perf_counter()
+    ke = max(3, args.steps // 2)
+    for _ in range(ke):
+        H.MatVecProduct(Xh, "mixed")
+    t_e2e = (time.perf_counter() - t) / ke
+    t_e2e = max_over_ranks(ws, t_e2e)
+    e2e = {"value": ws * nrhs / t_e2e, "unit": "RHS/s", "h2d_bytes_per_step": int(Xh.nbytes),
+           "d2h_bytes_per_step": int(Xh.nbytes), "ms_per_step": t_e2e * 1e3,
+           "entry": "hodlr3d_matvec_host"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        secs, desc = cpu_sample(pts, args.tol_pow, 1, 0, threads)
+        cpu = {"value": 1.0 / float(np.mean(secs)), "unit": "RHS/s", "cores": threads,
+               "kind": "port", "sample": desc}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "RHS/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config(args), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": int(launches), "clocks": clocks,
+            "fp64_1rhs": {"rhs_per_s": 1e3 / ms64, "ms": ms64},
+            "speedup_mixed_batched_vs_fp64": value / ws / (1e3 / ms64),
+            "error_vs_dense_fp64": {"mixed_max_col_rel": err_mixed, "fp64_max_col_rel": err_fp64,
+                                    "rows_sampled": len(rows)},
+            "gmres": gmres, "setup_seconds": t_setup,
+            "assembly": {"seconds": st["assemble_seconds"], "tree_seconds": st["tree_seconds"],
+                         "pairs": st["n_pairs"], "max_rank": st["max_rank"],
+                         "factor_bytes_fp32": st["factor_bytes_fp32"],
+                         "factor_bytes_fp64": st["factor_bytes_fp64"]},
+        }
+        print(json.dumps(line), flush=True)
+    H.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--nrhs", type=int, default=32)
+    ap.add_argument("--tol-pow", type=int, default=10)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

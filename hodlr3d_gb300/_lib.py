@@ -37,7 +37,8 @@ class Stats(ctypes.Structure):
     _fields_ = [("n_points", ctypes.c_int64), ("levels", ctypes.c_int), ("n_pairs", ctypes.c_int64),
                 ("n_near_blocks", ctypes.c_int64), ("max_rank", ctypes.c_int),
                 ("sum_rank", ctypes.c_int64), ("memory_entries", ctypes.c_double),
-                ("factor_entries", ctypes.c_int64), ("factor_bytes_fp64", ctypes.c_int64),
+                ("factor_entries", ctypes.c_int64), ("u_entries", ctypes.c_int64),
+                ("v_entries", ctypes.c_int64), ("factor_bytes_fp64", ctypes.c_int64),
                 ("factor_bytes_fp32", ctypes.c_int64), ("near_entries", ctypes.c_int64),
                 ("tree_seconds", ctypes.c_double), ("assemble_seconds", ctypes.c_double),
                 ("aca_batches", ctypes.c_int)]
@@ -102,6 +103,8 @@ def lib() -> ctypes.CDLL:
         "hodlr3d_get_pivots": ([vp, vp, vp], i32),
         "hodlr3d_get_pair_factors": ([vp, i64, vp, vp], i32),
         "hodlr3d_launch_count": ([vp], i64),
+        "hodlr3d_set_profiling": ([vp, i32], i32),
+        "hodlr3d_profile_report": ([vp, ctypes.c_char_p, i32], i32),
     }
     for name, (args, res) in sigs.items():
         f = getattr(L, name)

@@ -170,14 +170,46 @@ struct hodlr3d_handle {
   std::vector<int32_t> h_fac_pool;      // per pair: pool index
   std::vector<double*> h_u64, h_v64;
   std::vector<float*> h_u32, h_v32;
-  DevBuf rank, u64, v64, u32, v32, tr_off, part_off, nonleaf, pair_level;
-  int64_t sum_rank = 0, part_total = 0, n_nonleaf = 0, factor_entries = 0;
+  DevBuf rank, u64, v64, u32, v32, tr_off, part_off, items, upper, pair_level;
+  int64_t sum_rank = 0, part_total = 0, n_items = 0, n_upper = 0, factor_entries = 0;
+  int64_t u_entries = 0, v_entries = 0;
+  int max_slice = 0;
   int max_rank = 0;
   double assemble_seconds = 0.0;
   int aca_batches = 0;
   // matvec work buffers
-  DevBuf xsorted, tbuf, pbuf, stage_x, stage_y;
+  DevBuf xsorted, tbuf, pbuf, ynl, stage_x, stage_y;
   int mv_nrhs_cap = 0;
+  // optional per-kernel timing of matvec launches
+  struct Prof : h3d::MatvecProfiler {
+    std::vector<cudaEvent_t> pool;
+    size_t used = 0;
+    std::vector<std::pair<const char*, std::pair<cudaEvent_t, cudaEvent_t>>> spans;
+    cudaEvent_t last = nullptr;
+    cudaEvent_t next_event() {
+      if (used == pool.size()) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        pool.push_back(e);
+      }
+      return pool[used++];
+    }
+    void begin(cudaStream_t s) override {
+      last = next_event();
+      cudaEventRecord(last, s);
+    }
+    void mark(cudaStream_t s, const char* name) override {
+      cudaEvent_t e = next_event();
+      cudaEventRecord(e, s);
+      spans.push_back({name, {last, e}});
+      last = e;
+    }
+    ~Prof() {
+      for (cudaEvent_t e : pool) cudaEventDestroy(e);
+    }
+  };
+  bool profiling = false;
+  Prof prof;
   void* pinned_x = nullptr;
   void* pinned_y = nullptr;
   size_t pinned_bytes = 0;
@@ -509,10 +541,12 @@ int assemble(hodlr3d_t h) {
     }
     todo.swap(retry);
   }
-  // per-pair tables for the matvec
+  // per-pair tables for the matvec: T offsets, slice work items of the
+  // non-leaf pairs, partial offsets of the pairs above level d - 1
+  const int d = h->levels;
   std::vector<int64_t> tr(np), po(np, -1);
-  std::vector<int32_t> nonleaf;
-  int64_t acc = 0, pacc = 0, fe = 0;
+  std::vector<int32_t> items, upper;
+  int64_t acc = 0, pacc = 0, fe = 0, ue = 0, ve = 0;
   h->max_rank = 0;
   for (int64_t p = 0; p < np; ++p) {
     tr[p] = acc;
@@ -523,17 +557,34 @@ int assemble(hodlr3d_t h) {
     int64_t a0, a1, b0, b1;
     box_range(h, j, kt, a0, a1);
     box_range(h, j, ks, b0, b1);
+    ue += (int64_t)h->h_rank[p] * (a1 - a0);
+    ve += (int64_t)h->h_rank[p] * (b1 - b0);
     fe += (int64_t)h->h_rank[p] * ((a1 - a0) + (b1 - b0));
-    if (j < h->levels) {
-      po[p] = pacc;
-      pacc += (int64_t)h->h_rank[p] << (3 * (h->levels - j));
-      nonleaf.push_back((int32_t)p);
+    if (j < d) {
+      const int nsl = 1 << (3 * (d - 1 - j));
+      for (int sl = 0; sl < nsl; ++sl) {
+        items.push_back((int32_t)p);
+        items.push_back(sl);
+      }
     }
+    if (j < d - 1) {
+      po[p] = pacc;
+      pacc += (int64_t)h->h_rank[p] << (3 * (d - 1 - j));
+      upper.push_back((int32_t)p);
+    }
+  }
+  h->max_slice = 0;
+  if (d >= 1) {
+    for (int64_t b = 0; b < (int64_t(1) << (3 * (d - 1))); ++b)
+      h->max_slice = std::max(h->max_slice, h->h_leaf_off[(b + 1) << 3] - h->h_leaf_off[b << 3]);
   }
   h->sum_rank = acc;
   h->part_total = pacc;
-  h->n_nonleaf = (int64_t)nonleaf.size();
+  h->n_items = (int64_t)items.size() / 2;
+  h->n_upper = (int64_t)upper.size();
   h->factor_entries = fe;
+  h->u_entries = ue;
+  h->v_entries = ve;
   cudaStream_t s = h->stream;
   const size_t npb = std::max<int64_t>(np, 1);
   H3D_CUDA(h->rank.ensure(sizeof(int32_t) * npb));
@@ -543,7 +594,8 @@ int assemble(hodlr3d_t h) {
   H3D_CUDA(h->v32.ensure(sizeof(void*) * npb));
   H3D_CUDA(h->tr_off.ensure(sizeof(int64_t) * npb));
   H3D_CUDA(h->part_off.ensure(sizeof(int64_t) * npb));
-  H3D_CUDA(h->nonleaf.ensure(sizeof(int32_t) * std::max<size_t>(nonleaf.size(), 1)));
+  H3D_CUDA(h->items.ensure(sizeof(int32_t) * std::max<size_t>(items.size(), 2)));
+  H3D_CUDA(h->upper.ensure(sizeof(int32_t) * std::max<size_t>(upper.size(), 1)));
   H3D_CUDA(h->pair_level.ensure(sizeof(int32_t) * npb));
   if (np) {
     H3D_CUDA(cudaMemcpyAsync(h->rank.p, h->h_rank.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice, s));
@@ -556,8 +608,11 @@ int assemble(hodlr3d_t h) {
     H3D_CUDA(cudaMemcpyAsync(h->pair_level.p, h->h_pair_level.data(), sizeof(int32_t) * np,
                              cudaMemcpyHostToDevice, s));
   }
-  if (!nonleaf.empty())
-    H3D_CUDA(cudaMemcpyAsync(h->nonleaf.p, nonleaf.data(), sizeof(int32_t) * nonleaf.size(),
+  if (!items.empty())
+    H3D_CUDA(cudaMemcpyAsync(h->items.p, items.data(), sizeof(int32_t) * items.size(),
+                             cudaMemcpyHostToDevice, s));
+  if (!upper.empty())
+    H3D_CUDA(cudaMemcpyAsync(h->upper.p, upper.data(), sizeof(int32_t) * upper.size(),
                              cudaMemcpyHostToDevice, s));
   H3D_CUDA(cudaStreamSynchronize(s));
   h->mv_nrhs_cap = 0;
@@ -570,11 +625,13 @@ int assemble(hodlr3d_t h) {
 // matvec
 // ---------------------------------------------------------------------------
 int ensure_matvec_buffers(hodlr3d_t h, int nrhs) {
-  if (nrhs <= h->mv_nrhs_cap) return HODLR3D_OK;
-  H3D_CUDA(h->xsorted.ensure(sizeof(double) * h->N * nrhs));
-  H3D_CUDA(h->tbuf.ensure(sizeof(double) * std::max<int64_t>(h->sum_rank, 1) * nrhs));
-  H3D_CUDA(h->pbuf.ensure(sizeof(double) * std::max<int64_t>(h->part_total, 1) * nrhs));
-  h->mv_nrhs_cap = nrhs;
+  const int nr = h3d::padded_nrhs(nrhs);
+  if (nr <= h->mv_nrhs_cap) return HODLR3D_OK;
+  H3D_CUDA(h->xsorted.ensure(sizeof(double) * h->N * nr));
+  H3D_CUDA(h->tbuf.ensure(sizeof(double) * std::max<int64_t>(h->sum_rank, 1) * nr));
+  H3D_CUDA(h->pbuf.ensure(sizeof(double) * std::max<int64_t>(h->part_total, 1) * nr));
+  H3D_CUDA(h->ynl.ensure(sizeof(double) * h->N * nr));
+  h->mv_nrhs_cap = nr;
   return HODLR3D_OK;
 }
 
@@ -597,6 +654,9 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
   far.il_ptr = h->il_ptr.as<int64_t>();
   far.rev = h->rev.as<int32_t>();
   far.rank = h->rank.as<int32_t>();
+  far.pair_level = h->pair_level.as<int32_t>();
+  far.pair_tgt = h->pair_tgt.as<int32_t>();
+  far.pair_src = h->pair_src.as<int32_t>();
   far.tr_off = h->tr_off.as<int64_t>();
   far.part_off = h->part_off.as<int64_t>();
   far.ufac = f32 ? h->u32.as<const void*>() : h->u64.as<const void*>();
@@ -613,14 +673,16 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
   nr.kd = h->kd;
   h3d::MatvecBuffers B{};
   B.xsorted = h->xsorted.p;
-  B.tbuf = h->tbuf.as<double>();
+  B.tbuf = h->tbuf.p;
   B.pbuf = h->pbuf.as<double>();
-  B.nonleaf_pairs = h->nonleaf.as<int32_t>();
-  B.n_nonleaf = h->n_nonleaf;
-  B.pair_level = h->pair_level.as<int32_t>();
-  B.max_leaf = h->max_leaf;
+  B.ynl = h->ynl.as<double>();
+  B.items = h->items.as<int32_t>();
+  B.n_items = h->n_items;
+  B.upper_pairs = h->upper.as<int32_t>();
+  B.n_upper = h->n_upper;
+  B.max_slice = h->max_slice;
   h->launches += h3d::launch_matvec(s, h->N, h->perm.as<int32_t>(), far, nr, B, x, ld, y, ld, nrhs,
-                                    precision, trans ? 1 : 0);
+                                    precision, trans ? 1 : 0, h->profiling ? &h->prof : nullptr);
   H3D_CUDA(cudaGetLastError());
   return HODLR3D_OK;
 }
@@ -1018,6 +1080,8 @@ int hodlr3d_get_stats(hodlr3d_t h, hodlr3d_stats* s) {
   s->max_rank = h->max_rank;
   s->sum_rank = h->sum_rank;
   s->factor_entries = h->factor_entries;
+  s->u_entries = h->u_entries;
+  s->v_entries = h->v_entries;
   s->factor_bytes_fp64 = h->factor_entries * 8;
   s->factor_bytes_fp32 = h->opt.keep_fp32 ? h->factor_entries * 4 : 0;
   s->tree_seconds = h->tree_seconds;
@@ -1127,5 +1191,45 @@ int hodlr3d_get_pair_factors(hodlr3d_t h, int64_t pair, double* U, double* V) {
 }
 
 int64_t hodlr3d_launch_count(hodlr3d_t h) { return h ? h->launches : 0; }
+
+int hodlr3d_set_profiling(hodlr3d_t h, int enable) {
+  if (!h) return set_error(HODLR3D_ERR_INVALID_ARG, "null handle");
+  h->profiling = enable != 0;
+  h->prof.spans.clear();
+  h->prof.used = 0;
+  return HODLR3D_OK;
+}
+
+int hodlr3d_profile_report(hodlr3d_t h, char* buf, int cap) {
+  H3D_TRY(check_handle(h));
+  if (!buf || cap <= 0) return set_error(HODLR3D_ERR_INVALID_ARG, "bad buffer");
+  std::vector<std::string> names;
+  std::vector<double> ms;
+  std::vector<int> cnt;
+  for (auto& sp : h->prof.spans) {
+    H3D_CUDA(cudaEventSynchronize(sp.second.second));
+    float t = 0.f;
+    H3D_CUDA(cudaEventElapsedTime(&t, sp.second.first, sp.second.second));
+    size_t i = 0;
+    while (i < names.size() && names[i] != sp.first) ++i;
+    if (i == names.size()) {
+      names.push_back(sp.first);
+      ms.push_back(0.0);
+      cnt.push_back(0);
+    }
+    ms[i] += t;
+    cnt[i] += 1;
+  }
+  std::string out;
+  for (size_t i = 0; i < names.size(); ++i) {
+    char line[128];
+    snprintf(line, sizeof(line), "%s %d %.6f\n", names[i].c_str(), cnt[i], ms[i]);
+    out += line;
+  }
+  h->prof.spans.clear();
+  h->prof.used = 0;
+  snprintf(buf, (size_t)cap, "%s", out.c_str());
+  return HODLR3D_OK;
+}
 
 }  // extern "C"

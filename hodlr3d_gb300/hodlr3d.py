@@ -189,6 +189,20 @@ class HODLR3D:
     def launch_count(self) -> int:
         return int(self._L.hodlr3d_launch_count(self.handle))
 
+    def set_profiling(self, enable: bool) -> None:
+        """Records CUDA events between the matvec's kernel launches."""
+        check(self._L.hodlr3d_set_profiling(self.handle, 1 if enable else 0))
+
+    def profile_report(self) -> dict:
+        """{kernel: (launches, total_ms)} accumulated since the last report."""
+        buf = ctypes.create_string_buffer(4096)
+        check(self._L.hodlr3d_profile_report(self.handle, buf, len(buf)))
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, n, ms = line.split()
+            out[name] = (int(n), float(ms))
+        return out
+
     # ---- helpers --------------------------------------------------------------
     def _host_cols(self, b):
         a = np.asarray(b, dtype=np.float64)

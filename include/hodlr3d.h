@@ -58,6 +58,8 @@ typedef struct hodlr3d_stats {
   int64_t sum_rank;         /* sum of pair ranks */
   double memory_entries;    /* reference HODLR3DTree::findMemory count */
   int64_t factor_entries;   /* sum over pairs of rank * (n + m) */
+  int64_t u_entries;        /* sum over pairs of rank * n (target-side factors) */
+  int64_t v_entries;        /* sum over pairs of rank * m (source-side factors) */
   int64_t factor_bytes_fp64;
   int64_t factor_bytes_fp32;
   int64_t near_entries;     /* sum over near blocks of n * m */
@@ -160,6 +162,11 @@ int hodlr3d_get_pivots(hodlr3d_t h, int32_t* rows, int32_t* cols);
 int hodlr3d_get_pair_factors(hodlr3d_t h, int64_t pair, double* U, double* V);
 /* number of kernel launches issued by the library since creation */
 int64_t hodlr3d_launch_count(hodlr3d_t h);
+/* Per-kernel timing of the matvec launches with CUDA events recorded between
+ * them on the launch stream (off by default).  The report lists one line per
+ * kernel, "name launches total_ms", accumulated since the last report. */
+int hodlr3d_set_profiling(hodlr3d_t h, int enable);
+int hodlr3d_profile_report(hodlr3d_t h, char* buf, int cap);
 
 #ifdef __cplusplus
 }
