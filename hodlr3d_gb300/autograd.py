@@ -1,0 +1,50 @@
+"""torch.autograd wrappers of the matvec and the solve.
+
+* ``matvec(H, x)``: y = A x; its backward is the hand-written transpose
+  product A^T g (V (U^T g) on the compressed pairs, transposed near field).
+* ``solve(H, b)``: x = A^{-1} b by GMRES; its backward is the adjoint solve
+  A^T lambda = g, and grad_b = lambda.
+
+Both take CUDA float64 tensors of shape (N,) or (N, nrhs).
+"""
+from __future__ import annotations
+
+import torch
+
+
+class _Matvec(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, H, precision):
+        ctx.H = H
+        ctx.precision = precision
+        return H.matvec(x.detach(), precision)
+
+    @staticmethod
+    def backward(ctx, g):
+        return ctx.H.matvec(g.contiguous(), ctx.precision, transpose=True), None, None
+
+
+class _Solve(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, b, H, opts):
+        ctx.H = H
+        ctx.opts = opts
+        x, info = H.gmres(b.detach(), **opts)
+        ctx.info = info
+        return x
+
+    @staticmethod
+    def backward(ctx, g):
+        lam, _ = ctx.H.gmres(g.contiguous(), transpose=True, **ctx.opts)
+        return lam, None, None
+
+
+def matvec(H, x, precision="fp64"):
+    """Differentiable y = A x (gradient w.r.t. the charges x)."""
+    return _Matvec.apply(x, H, precision)
+
+
+def solve(H, b, maxit=400, tol=1e-10, restart=30, precision="fp64", **kw):
+    """Differentiable x = A^{-1} b (gradient w.r.t. the right-hand side b)."""
+    opts = dict(maxit=maxit, tol=tol, restart=restart, precision=precision, **kw)
+    return _Solve.apply(b, H, opts)

@@ -1,0 +1,95 @@
+// C++ drop-in facade of the reference's HODLR3D class (include/HODLR3D.hpp:12-21
+// of SAFRAN-LAB/HODLR3D) over the hodlr3d_gb300 C ABI.  Header only.
+//
+// The reference's constructor, assemble() and MatVecProduct(b, Ab) keep their
+// signatures; the vector type is a template parameter so Eigen::VectorXd (or
+// std::vector<double>) works unchanged: it needs data(), size() and resize().
+// The kernel is chosen by Qchoice (src/kernel.cpp:65-227) instead of a
+// user-compiled getMatrixEntry; kernels 0-10, 13, 15 and 16 run on the GPU.
+// Errors are thrown as hodlr3d_gb300::Error (the reference has no error path).
+#ifndef HODLR3D_GB300_FACADE_HPP
+#define HODLR3D_GB300_FACADE_HPP
+
+#include <cmath>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "hodlr3d.h"
+
+#ifndef HODLR3D_GB300_PTS3D
+#define HODLR3D_GB300_PTS3D
+struct pts3D {  // include/definitions.hpp:7-9
+  double x, y, z;
+};
+#endif
+
+namespace hodlr3d_gb300 {
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+inline void check(int code) {
+  if (code != HODLR3D_OK) throw Error(code, hodlr3d_last_error());
+}
+
+// Statistics the reference drivers read from the tree (findMemory, getMaxRank).
+struct TreeView {
+  hodlr3d_t h;
+  int nLevels() const {
+    hodlr3d_stats s;
+    check(hodlr3d_get_stats(h, &s));
+    return s.levels;
+  }
+  void findMemory(double& sum) const {
+    hodlr3d_stats s;
+    check(hodlr3d_get_stats(h, &s));
+    sum = s.memory_entries;
+  }
+  int getMaxRank() const {
+    hodlr3d_stats s;
+    check(hodlr3d_get_stats(h, &s));
+    return s.max_rank;
+  }
+};
+
+}  // namespace hodlr3d_gb300
+
+class HODLR3D {
+ public:
+  hodlr3d_gb300::TreeView tree;  // stands in for the reference's A (HODLR3DTree*)
+  hodlr3d_gb300::TreeView* A;
+  int N;
+  int precision = HODLR3D_FP64;  // HODLR3D_MIXED selects the FP32 factors
+
+  HODLR3D(int nParticlesInLeafAlong1D, double L, int TOL_POW, int Qchoice,
+          std::vector<pts3D>& particles, double diag_override = NAN) {
+    hodlr3d_options opt;
+    hodlr3d_default_options(&opt);
+    opt.diag_override = diag_override;
+    N = (int)particles.size();
+    hodlr3d_t h = nullptr;
+    hodlr3d_gb300::check(hodlr3d_create(reinterpret_cast<const double*>(particles.data()), N,
+                                        nParticlesInLeafAlong1D, L, TOL_POW, Qchoice, &opt, &h));
+    tree.h = h;
+    A = &tree;
+  }
+  HODLR3D(const HODLR3D&) = delete;
+  HODLR3D& operator=(const HODLR3D&) = delete;
+  ~HODLR3D() { hodlr3d_destroy(tree.h); }
+
+  void assemble() { hodlr3d_gb300::check(hodlr3d_assemble(tree.h)); }
+
+  // Ab = A b (host vectors); Ab is resized like the reference's (src/HODLR3DTree.cpp:1782).
+  template <class Vec>
+  void MatVecProduct(Vec& b, Vec& AFMM_Ab) {
+    AFMM_Ab.resize(N);
+    hodlr3d_gb300::check(hodlr3d_matvec_host(tree.h, b.data(), AFMM_Ab.data(), 1, N, precision));
+  }
+
+  hodlr3d_t handle() const { return tree.h; }
+};
+
+#endif
