@@ -21,6 +21,7 @@
 #include "common.cuh"
 #include "gmres.h"
 #include "matvec.h"
+#include "noalloc.h"
 #include "tree.h"
 
 namespace {
@@ -905,6 +906,75 @@ int hodlr3d_matvec_transpose(hodlr3d_t h, const double* x, double* y, int nrhs, 
                              int precision, void* stream) {
   H3D_TRY(check_handle(h));
   return matvec_device(h, x, y, nrhs, ld, precision, (cudaStream_t)stream, true);
+}
+
+int hodlr3d_matvec_noalloc(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
+                           int precision, void* stream) {
+  H3D_TRY(check_handle(h));
+  if (!h->assembled) return set_error(HODLR3D_ERR_NOT_ASSEMBLED, "hodlr3d_assemble has not run");
+  if (!x || !y) return set_error(HODLR3D_ERR_INVALID_ARG, "null vector");
+  if (nrhs < 1 || nrhs > 64) return set_error(HODLR3D_ERR_INVALID_ARG, "nrhs must be in 1..64");
+  if (ld < h->N) return set_error(HODLR3D_ERR_INVALID_ARG, "ld < n");
+  if (precision != HODLR3D_FP64 && precision != HODLR3D_MIXED)
+    return set_error(HODLR3D_ERR_INVALID_ARG, "unknown precision %d", precision);
+  if (precision == HODLR3D_MIXED && !h->opt.keep_fp32)
+    return set_error(HODLR3D_ERR_INVALID_ARG, "mixed precision needs keep_fp32");
+  // the work buffers of the product, carved from the fixed scratch array
+  const int nr = h3d::padded_nrhs(nrhs);
+  const size_t s_real = precision == HODLR3D_MIXED ? sizeof(float) : sizeof(double);
+  auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
+  const size_t b_x = up(s_real * h->N * nr);
+  const size_t b_t = up(s_real * std::max<int64_t>(h->sum_rank, 1) * nr);
+  const size_t b_p = up(sizeof(double) * std::max<int64_t>(h->part_total, 1) * nr);
+  const size_t b_y = up(sizeof(double) * h->N * nr);
+  const size_t need = b_x + b_t + b_p + b_y;
+  if (need > h3d::kNoAllocScratchBytes)
+    return set_error(HODLR3D_ERR_INVALID_ARG,
+                     "hodlr3d_matvec_noalloc needs %zu bytes of scratch for n = %lld and nrhs = %d; "
+                     "its fixed scratch holds %zu bytes (use hodlr3d_matvec)",
+                     need, (long long)h->N, nrhs, (size_t)h3d::kNoAllocScratchBytes);
+  void* base = nullptr;
+  H3D_CUDA(h3d::noalloc_scratch(h->device, &base));
+  unsigned char* b8 = static_cast<unsigned char*>(base);
+  const bool f32 = precision == HODLR3D_MIXED;
+  h3d::FarOp far{};
+  far.levels = h->levels;
+  far.nleaf = h->nleaf;
+  far.leaf_off = h->leaf_off.as<int32_t>();
+  far.il_ptr = h->il_ptr.as<int64_t>();
+  far.rev = h->rev.as<int32_t>();
+  far.rank = h->rank.as<int32_t>();
+  far.pair_level = h->pair_level.as<int32_t>();
+  far.pair_tgt = h->pair_tgt.as<int32_t>();
+  far.pair_src = h->pair_src.as<int32_t>();
+  far.tr_off = h->tr_off.as<int64_t>();
+  far.part_off = h->part_off.as<int64_t>();
+  far.ufac = f32 ? h->u32.as<const void*>() : h->u64.as<const void*>();
+  far.vfac = f32 ? h->v32.as<const void*>() : h->v64.as<const void*>();
+  h3d::NearOp nrop{};
+  nrop.nbr_leaf = h->nbr_leaf.as<int32_t>();
+  nrop.xs = h->xs.as<double>();
+  nrop.ys = h->ys.as<double>();
+  nrop.zs = h->zs.as<double>();
+  nrop.xl = h->xl.as<float>();
+  nrop.yl = h->yl.as<float>();
+  nrop.zl = h->zl.as<float>();
+  nrop.centre = h->centre.as<double>();
+  nrop.kd = h->kd;
+  h3d::MatvecBuffers B{};
+  B.xsorted = b8;
+  B.tbuf = b8 + b_x;
+  B.pbuf = reinterpret_cast<double*>(b8 + b_x + b_t);
+  B.ynl = reinterpret_cast<double*>(b8 + b_x + b_t + b_p);
+  B.items = h->items.as<int32_t>();
+  B.n_items = h->n_items;
+  B.upper_pairs = h->upper.as<int32_t>();
+  B.n_upper = h->n_upper;
+  B.max_slice = h->max_slice;
+  h->launches += h3d::launch_matvec((cudaStream_t)stream, h->N, h->perm.as<int32_t>(), far, nrop, B,
+                                    x, ld, y, ld, nrhs, precision, 0, nullptr);
+  H3D_CUDA(cudaGetLastError());
+  return HODLR3D_OK;
 }
 
 int hodlr3d_matvec_host(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,

@@ -117,6 +117,17 @@ int hodlr3d_assemble(hodlr3d_t h);
  * (src/HODLR3D.cpp:21-27).  1 <= nrhs <= 64. */
 int hodlr3d_matvec(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld, int precision,
                    void* stream);
+/* The same product for callers that cannot allocate device memory while they
+ * run (a caller held to a memory budget fixed up front, or one whose
+ * allocator must not be re-entered from the computing thread).  No
+ * counterpart in the reference.  It never allocates: its work buffers come
+ * from one fixed 64 MiB device array that every GPU loading the library holds
+ * until exit, and sizes needing more are refused with HODLR3D_ERR_INVALID_ARG.
+ * The first call on a device looks the array's address up (make it before
+ * any stream capture).  All calls share the array, so calls that overlap on
+ * the GPU race.  Device pointers, enqueued on `stream`. */
+int hodlr3d_matvec_noalloc(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
+                           int precision, void* stream);
 /* Same with host pointers: copies in, multiplies, copies out, synchronises. */
 int hodlr3d_matvec_host(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
                         int precision);
