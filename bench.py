@@ -190,7 +190,9 @@ def config(args):
 
 # ----------------------------------------------------------------------------
 def level_bytes(H, nr_pad, s):
-    """Algorithmic bytes per launch of the matvec kernels."""
+    """Algorithmic bytes per launch of each matvec kernel, both engines: the
+    factor entries it streams (s bytes each), plus its right-hand-side,
+    intermediate (T, slice partials) and output traffic counted once."""
     P = H.pairs()
     R = H.ranks().astype(np.int64)
     off = H.leaf_offsets()
@@ -209,12 +211,28 @@ def level_bytes(H, nr_pad, s):
         m[sel] = sizes(j, P[sel, 2].astype(np.int64))
     leaf = P[:, 0] == d
     up = ~leaf
-    xb = N * nr_pad * s
+    above = P[:, 0] < d - 1
+    nslices = 8 ** np.maximum(d - 1 - P[:, 0], 0)
+    xb = N * nr_pad * s                       # right-hand sides in tree order
+    t_up = int(R[up].sum()) * nr_pad * s      # T of the non-leaf pairs
+    t_leaf = int(R[leaf].sum()) * nr_pad * s  # T of the leaf pairs
+    parts = int((R[above] * nslices[above]).sum()) * nr_pad * s
+    u_up, v_up = int((R[up] * n[up]).sum()) * s, int((R[up] * m[up]).sum()) * s
+    u_leaf, v_leaf = int((R[leaf] * n[leaf]).sum()) * s, int((R[leaf] * m[leaf]).sum()) * s
+    ynl = N * nr_pad * 8
+    y = N * min(nr_pad, 64) * 8
     b = {
-        "gather": N * 8 * min(nr_pad, 64) + xb,
-        "vtx": int((R[up] * m[up]).sum()) * s + xb + int(R[up].sum()) * nr_pad * 8,
-        "ut": int((R[up] * n[up]).sum()) * s + int(R[up].sum()) * nr_pad * s + N * nr_pad * 8,
-        "leaf": int((R[leaf] * (n[leaf] + m[leaf])).sum()) * s + xb + N * nr_pad * 8 + N * nr_pad * 8,
+        "gather": y + xb,
+        # CUDA-core engine
+        "vtx": v_up + xb + t_up + parts,
+        "tred": parts + t_up,
+        "ut": u_up + t_up + ynl,
+        "leaf": u_leaf + v_leaf + xb + ynl + y,
+        # tensor-core engine
+        "ta_slice": v_up + xb + t_up + parts,
+        "ta_leaf": v_leaf + xb + t_leaf,
+        "ut_tc": u_up + t_up + ynl,
+        "leaf_tc": u_leaf + t_leaf + xb + ynl + y,
     }
     return b
 

@@ -260,10 +260,14 @@ __global__ void __launch_bounds__(BS) k_aca(const AcaTask* __restrict__ tasks, i
   }
 }
 
-// Copies the first r columns of U and V of every task into the final pools
-// (FP64, and optionally FP32), U (n x r) then V (m x r) at dst_off.
+// Copies the first r columns of U and V of every task into the final pools.
+// FP64 (at dst_off): U (n x r) then V (m x r), column-major.  FP32 (at
+// dst_off32, optional): U row-major with the rank padded to rp = round4(r),
+// then V column-major with the leading dimension padded to mp = round4(m),
+// padding zero -- every row of U and column of V starts on 16 bytes.
 __global__ void k_aca_compact(const AcaTask* __restrict__ tasks, const int32_t* __restrict__ rank,
-                              const int64_t* __restrict__ dst_off, const double* __restrict__ ws,
+                              const int64_t* __restrict__ dst_off,
+                              const int64_t* __restrict__ dst_off32, const double* __restrict__ ws,
                               double* __restrict__ out64, float* __restrict__ out32) {
   const AcaTask T = tasks[blockIdx.x];
   const int r = rank[blockIdx.x];
@@ -271,15 +275,22 @@ __global__ void k_aca_compact(const AcaTask* __restrict__ tasks, const int32_t* 
   const double* V = U + (size_t)T.cap * T.n;
   const int64_t o = dst_off[blockIdx.x];
   const int64_t nu = (int64_t)r * T.n, nv = (int64_t)r * T.m;
-  for (int64_t i = threadIdx.x; i < nu; i += blockDim.x) {
-    const double v = U[i];
-    out64[o + i] = v;
-    if (out32) out32[o + i] = (float)v;
+  for (int64_t i = threadIdx.x; i < nu; i += blockDim.x) out64[o + i] = U[i];
+  for (int64_t i = threadIdx.x; i < nv; i += blockDim.x) out64[o + nu + i] = V[i];
+  if (!out32) return;
+  const int rp = (r + 3) & ~3;
+  const int64_t mp = (T.m + 3) & ~3;
+  float* u32 = out32 + dst_off32[blockIdx.x];
+  float* v32 = u32 + (int64_t)T.n * rp;
+  for (int64_t e = threadIdx.x; e < (int64_t)T.n * rp; e += blockDim.x) {
+    const int64_t i = e / rp;
+    const int l = (int)(e - i * rp);
+    u32[e] = l < r ? (float)U[(int64_t)l * T.n + i] : 0.f;
   }
-  for (int64_t i = threadIdx.x; i < nv; i += blockDim.x) {
-    const double v = V[i];
-    out64[o + nu + i] = v;
-    if (out32) out32[o + nu + i] = (float)v;
+  for (int64_t e = threadIdx.x; e < mp * r; e += blockDim.x) {
+    const int l = (int)(e / mp);
+    const int64_t i = e - (int64_t)l * mp;
+    v32[e] = i < T.m ? (float)V[(int64_t)l * T.m + i] : 0.f;
   }
 }
 
@@ -306,10 +317,11 @@ cudaError_t launch_aca(cudaStream_t s, int block, int grid, const AcaTask* tasks
 }
 
 cudaError_t launch_aca_compact(cudaStream_t s, int ntasks, const AcaTask* tasks,
-                               const int32_t* rank, const int64_t* dst_off, const double* ws,
-                               double* out64, float* out32) {
+                               const int32_t* rank, const int64_t* dst_off,
+                               const int64_t* dst_off32, const double* ws, double* out64,
+                               float* out32) {
   if (ntasks == 0) return cudaSuccess;
-  k_aca_compact<<<ntasks, 256, 0, s>>>(tasks, rank, dst_off, ws, out64, out32);
+  k_aca_compact<<<ntasks, 256, 0, s>>>(tasks, rank, dst_off, dst_off32, ws, out64, out32);
   return cudaGetLastError();
 }
 

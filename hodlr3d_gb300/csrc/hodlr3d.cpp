@@ -211,6 +211,12 @@ struct hodlr3d_handle {
   };
   bool profiling = false;
   Prof prof;
+  int engine = 0;   // 0 auto, 1 SIMT kernels, 2 tensor-core kernels
+  DevBuf dev_err;   // set by kernels whose bounded waits gave up
+  bool leaves_aligned = false;  // every leaf population a multiple of 4
+  DevBuf knear, near_off;       // FP32 near-field blocks of the tensor-core engine
+  bool near_built = false;
+  int64_t near_floats = 0;
   void* pinned_x = nullptr;
   void* pinned_y = nullptr;
   size_t pinned_bytes = 0;
@@ -349,8 +355,12 @@ int build_tree(hodlr3d_t h, const double* xyz_host) {
     h->h_pair_level[p] = j;
   }
   h->max_leaf = 0;
-  for (int64_t k = 0; k < h->nleaf; ++k)
-    h->max_leaf = std::max(h->max_leaf, h->h_leaf_off[k + 1] - h->h_leaf_off[k]);
+  h->leaves_aligned = true;
+  for (int64_t k = 0; k < h->nleaf; ++k) {
+    const int nk = h->h_leaf_off[k + 1] - h->h_leaf_off[k];
+    h->max_leaf = std::max(h->max_leaf, nk);
+    if (nk % 4) h->leaves_aligned = false;
+  }
   H3D_CUDA(cudaStreamSynchronize(s));
   h->tree_seconds = now_s() - t_start;
   return HODLR3D_OK;
@@ -428,8 +438,8 @@ int run_aca_batch(hodlr3d_t h, std::vector<HostTask>& batch, std::vector<HostTas
   H3D_CUDA(cudaStreamSynchronize(s));
   H3D_CUDA(cudaGetLastError());
   // finished tasks -> exact-size pools; capacity overflows -> retried with twice the capacity
-  std::vector<int64_t> dst(nt, 0);
-  int64_t total = 0;
+  std::vector<int64_t> dst(nt, 0), dst32(nt, 0);
+  int64_t total = 0, total32 = 0;
   for (int i = 0; i < nt; ++i) {
     if (st[i] == h3d::kAcaNonFinite)
       return set_error(HODLR3D_ERR_NONFINITE,
@@ -444,6 +454,8 @@ int run_aca_batch(hodlr3d_t h, std::vector<HostTask>& batch, std::vector<HostTas
     }
     dst[i] = total;
     total += (int64_t)rk[i] * (batch[i].n + batch[i].m);
+    dst32[i] = total32;
+    total32 += (int64_t)batch[i].n * ((rk[i] + 3) & ~3) + (int64_t)((batch[i].m + 3) & ~3) * rk[i];
   }
   DevBuf* pool64 = new DevBuf();
   h->pools.push_back(pool64);
@@ -452,14 +464,17 @@ int run_aca_batch(hodlr3d_t h, std::vector<HostTask>& batch, std::vector<HostTas
   if (h->opt.keep_fp32) {
     pool32 = new DevBuf();
     h->pools.push_back(pool32);
-    H3D_CUDA(pool32->ensure(sizeof(float) * std::max<int64_t>(total, 1)));
+    H3D_CUDA(pool32->ensure(sizeof(float) * std::max<int64_t>(total32, 4)));
   }
+  DevBuf d_off32;
   H3D_CUDA(d_off.ensure(sizeof(int64_t) * nt));
+  H3D_CUDA(d_off32.ensure(sizeof(int64_t) * nt));
   H3D_CUDA(cudaMemcpyAsync(d_off.p, dst.data(), sizeof(int64_t) * nt, cudaMemcpyHostToDevice, s));
+  H3D_CUDA(cudaMemcpyAsync(d_off32.p, dst32.data(), sizeof(int64_t) * nt, cudaMemcpyHostToDevice, s));
   H3D_CUDA(cudaMemcpyAsync(d_rank.p, rk.data(), sizeof(int32_t) * nt, cudaMemcpyHostToDevice, s));
   H3D_CUDA(h3d::launch_aca_compact(s, nt, d_tasks.as<h3d::AcaTask>(), d_rank.as<int32_t>(),
-                                   d_off.as<int64_t>(), d_ws.as<double>(), pool64->as<double>(),
-                                   pool32 ? pool32->as<float>() : nullptr));
+                                   d_off.as<int64_t>(), d_off32.as<int64_t>(), d_ws.as<double>(),
+                                   pool64->as<double>(), pool32 ? pool32->as<float>() : nullptr));
   ++h->launches;
   for (int i = 0; i < nt; ++i) {
     if (st[i] == h3d::kAcaCapReached) continue;
@@ -470,9 +485,9 @@ int run_aca_batch(hodlr3d_t h, std::vector<HostTask>& batch, std::vector<HostTas
     h->h_u64[p] = base64;
     h->h_v64[p] = base64 + (int64_t)r * batch[i].n;
     if (pool32) {
-      float* base32 = pool32->as<float>() + dst[i];
+      float* base32 = pool32->as<float>() + dst32[i];
       h->h_u32[p] = base32;
-      h->h_v32[p] = base32 + (int64_t)r * batch[i].n;
+      h->h_v32[p] = base32 + (int64_t)batch[i].n * ((r + 3) & ~3);
     }
     const int32_t* pr = pvh.data() + tasks[i].piv_off;
     h->h_piv_rows[p].assign(pr, pr + r);
@@ -682,8 +697,62 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
   B.upper_pairs = h->upper.as<int32_t>();
   B.n_upper = h->n_upper;
   B.max_slice = h->max_slice;
-  h->launches += h3d::launch_matvec(s, h->N, h->perm.as<int32_t>(), far, nr, B, x, ld, y, ld, nrhs,
-                                    precision, trans ? 1 : 0, h->profiling ? &h->prof : nullptr);
+  const int nrp = h3d::padded_nrhs(nrhs);
+  const bool tc_ok = precision == HODLR3D_MIXED && nrp == 32 && !trans && h->max_leaf <= 128 &&
+                     h->leaves_aligned;
+  if (h->engine == 2 && !tc_ok)
+    return set_error(HODLR3D_ERR_UNSUPPORTED,
+                     "the tensor-core engine needs A x (not the transpose) in the mixed form, 17..32 "
+                     "right-hand sides, and leaves of at most 128 points, each a multiple of 4");
+  if (tc_ok && h->engine != 1) {
+    if (!h->dev_err.p) {
+      H3D_CUDA(h->dev_err.ensure(sizeof(int)));
+      H3D_CUDA(cudaMemsetAsync(h->dev_err.p, 0, sizeof(int), s));
+    }
+    if (!h->near_built) {
+      // FP32 near-field blocks, evaluated once
+      std::vector<int32_t> nbl(26 * h->nleaf);
+      H3D_CUDA(cudaMemcpy(nbl.data(), h->nbr_leaf.p, sizeof(int32_t) * 26 * h->nleaf,
+                          cudaMemcpyDeviceToHost));
+      std::vector<int64_t> off(27 * h->nleaf, -1);
+      int64_t tot = 0;
+      for (int64_t k = 0; k < h->nleaf; ++k) {
+        const int64_t nk = h->h_leaf_off[k + 1] - h->h_leaf_off[k];
+        for (int sl = 0; sl < 27; ++sl) {
+          const int64_t nn = sl < 26 ? nbl[26 * k + sl] : k;
+          if (nn < 0) continue;
+          const int64_t ne = h->h_leaf_off[nn + 1] - h->h_leaf_off[nn];
+          off[27 * k + sl] = tot;
+          tot += nk * ((ne + 3) & ~int64_t(3));
+        }
+      }
+      H3D_CUDA(h->knear.ensure(sizeof(float) * std::max<int64_t>(tot, 4)));
+      H3D_CUDA(h->near_off.ensure(sizeof(int64_t) * off.size()));
+      H3D_CUDA(cudaMemcpy(h->near_off.p, off.data(), sizeof(int64_t) * off.size(),
+                          cudaMemcpyHostToDevice));
+      h->launches += h3d::launch_near_blocks(s, h->nleaf, h->leaf_off.as<int32_t>(), nr,
+                                             h->near_off.as<int64_t>(), h->knear.as<float>());
+      H3D_CUDA(cudaGetLastError());
+      h->near_floats = tot;
+      h->near_built = true;
+    }
+    h3d::TcBuffers T{};
+    T.xt = static_cast<float*>(h->xsorted.p);
+    T.t = static_cast<float*>(h->tbuf.p);
+    T.p = reinterpret_cast<float*>(h->pbuf.p);
+    T.ynl = h->ynl.as<double>();
+    T.err = h->dev_err.as<int>();
+    T.upper_pairs = h->upper.as<int32_t>();
+    T.n_upper = h->n_upper;
+    T.max_slice = h->max_slice;
+    T.knear = h->knear.as<float>();
+    T.near_off = h->near_off.as<int64_t>();
+    h->launches += h3d::launch_matvec_tc(s, h->N, h->perm.as<int32_t>(), far, nr, T, x, ld, y, ld,
+                                         nrhs, h->profiling ? &h->prof : nullptr);
+  } else {
+    h->launches += h3d::launch_matvec(s, h->N, h->perm.as<int32_t>(), far, nr, B, x, ld, y, ld, nrhs,
+                                      precision, trans ? 1 : 0, h->profiling ? &h->prof : nullptr);
+  }
   H3D_CUDA(cudaGetLastError());
   return HODLR3D_OK;
 }
@@ -1261,6 +1330,21 @@ int hodlr3d_get_pair_factors(hodlr3d_t h, int64_t pair, double* U, double* V) {
 }
 
 int64_t hodlr3d_launch_count(hodlr3d_t h) { return h ? h->launches : 0; }
+
+int hodlr3d_set_engine(hodlr3d_t h, int engine) {
+  if (!h || engine < 0 || engine > 2) return set_error(HODLR3D_ERR_INVALID_ARG, "engine must be 0, 1 or 2");
+  h->engine = engine;
+  return HODLR3D_OK;
+}
+
+int hodlr3d_device_status(hodlr3d_t h) {
+  H3D_TRY(check_handle(h));
+  H3D_CUDA(cudaDeviceSynchronize());
+  int v = 0;
+  if (h->dev_err.p) H3D_CUDA(cudaMemcpy(&v, h->dev_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (v) return set_error(HODLR3D_ERR_CUDA, "a tensor-core wait gave up (results of that call are invalid)");
+  return HODLR3D_OK;
+}
 
 int hodlr3d_set_profiling(hodlr3d_t h, int enable) {
   if (!h) return set_error(HODLR3D_ERR_INVALID_ARG, "null handle");

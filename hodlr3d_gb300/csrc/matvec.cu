@@ -84,7 +84,9 @@ __global__ void __launch_bounds__(256) k_vtx(FarOp op, const int32_t* __restrict
       __syncthreads();
       for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
         const int ll = e >> 6, ii = e & 63;
-        fs[ll][ii] = (l0 + ll < r && ii < ni) ? F[(int64_t)(l0 + ll) * ld + (i0 - box0) + ii] : (FT)0;
+        fs[ll][ii] = (l0 + ll < r && ii < ni)
+                         ? F[fac_idx<FT, TRANS>((i0 - box0) + ii, l0 + ll, r, ld)]
+                         : (FT)0;
       }
       for (int e = threadIdx.x; e < 64 * NR; e += blockDim.x) {
         const int ii = e / NR, c = e - ii * NR;
@@ -170,10 +172,9 @@ __global__ void __launch_bounds__(256) k_ut(FarOp op, const FT* __restrict__ T,
           for (int e = threadIdx.x; e < nl * NR; e += blockDim.x) ts[e / NR][e % NR] = Tp[l0 * NR + e];
           __syncthreads();
           if (live) {
-            const FT* Fr = F + (row - box0) + (int64_t)l0 * ld;
 #pragma unroll 4
             for (int l = 0; l < nl; ++l) {
-              const FT u = Fr[(int64_t)l * ld];
+              const FT u = F[fac_idx<FT, !TRANS>(row - box0, l0 + l, r, ld)];
 #pragma unroll
               for (int c = 0; c < C::CG; ++c) part[c] += u * ts[l][g * C::CG + c];
             }
@@ -269,7 +270,7 @@ __global__ void __launch_bounds__(256) k_leaf(FarOp op, NearOp nr, const FT* __r
           __syncthreads();
           for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
             const int ll = e >> 6, ii = e & 63;
-            fs[ll][ii] = (ll < nl && ii < na) ? Fin[(int64_t)(l0 + ll) * ni + a0 + ii] : (FT)0;
+            fs[ll][ii] = (ll < nl && ii < na) ? Fin[fac_idx<FT, TRANS>(a0 + ii, l0 + ll, r, ni)] : (FT)0;
           }
           for (int e = threadIdx.x; e < 64 * NR; e += blockDim.x) {
             const int ii = e / NR, c = e - ii * NR;
@@ -292,10 +293,9 @@ __global__ void __launch_bounds__(256) k_leaf(FarOp op, NearOp nr, const FT* __r
         }
         __syncthreads();
         if (live) {
-          const FT* Fr = Fout + (row - t0) + (int64_t)l0 * (t1 - t0);
 #pragma unroll 4
           for (int l = 0; l < nl; ++l) {
-            const FT u = Fr[(int64_t)l * (t1 - t0)];
+            const FT u = Fout[fac_idx<FT, !TRANS>(row - t0, l0 + l, r, t1 - t0)];
 #pragma unroll
             for (int c = 0; c < C::CG; ++c) part[c] += u * ts[l][g * C::CG + c];
           }

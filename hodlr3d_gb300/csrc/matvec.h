@@ -64,6 +64,45 @@ struct MatvecProfiler {
 
 int padded_nrhs(int nrhs);
 
+// Index of element (i, l) of a pair's factor with rank r over a box of n
+// points.  FP64 factors are column-major with leading dimension n.  In the
+// FP32 copies U is row-major with the rank padded to a multiple of 4 and V is
+// column-major with n padded to a multiple of 4 (zero padding), so that every
+// row of U and column of V starts on 16 bytes for the tensor-core kernels.
+template <typename FT, bool IS_U>
+__host__ __device__ __forceinline__ int64_t fac_idx(int64_t i, int l, int r, int64_t n) {
+  if (sizeof(FT) == 8) return (int64_t)l * n + i;
+  if (IS_U) return i * (int64_t)((r + 3) & ~3) + l;
+  return (int64_t)l * ((n + 3) & ~3) + i;
+}
+
+// Work buffers of the tensor-core form (32 right-hand sides, FP32):
+// xt: 32 * N, t: 32 * sum_rank, p: 32 * part_total floats; ynl: 32 * N doubles;
+// err: device flag set when an mbarrier wait gives up.
+struct TcBuffers {
+  float* xt;
+  float* t;
+  float* p;
+  double* ynl;
+  int* err;
+  const int32_t* upper_pairs;
+  int64_t n_upper;
+  int max_slice;
+  const float* knear;        // FP32 near-field blocks (launch_near_blocks)
+  const int64_t* near_off;   // 27 per leaf: block offsets, -1 for no neighbour
+};
+
+// Tensor-core mixed-precision product A X for 17..32 right-hand sides (padded
+// to 32); leaves of at most 128 points whose populations are multiples of 4
+// (16-byte aligned operand rows).  Returns the number of launches.
+int launch_matvec_tc(cudaStream_t s, int64_t N, const int32_t* perm, const FarOp& far,
+                     const NearOp& near, const TcBuffers& B, const double* X, int64_t ldx,
+                     double* Y, int64_t ldy, int nrhs, MatvecProfiler* prof);
+// Evaluates the FP32 near-field blocks of every leaf (row-major nk x round4(ne)
+// at near_off[27 k + slot], slots 0..25 the neighbours, 26 the leaf itself).
+int launch_near_blocks(cudaStream_t s, int64_t nleaf, const int32_t* leaf_off, const NearOp& near,
+                       const int64_t* near_off, float* Knear);
+
 // precision: 0 = FP64, 1 = mixed.  X, Y column-major in the original order.
 // Returns the number of kernel launches.
 int launch_matvec(cudaStream_t s, int64_t N, const int32_t* perm, const FarOp& far,

@@ -189,6 +189,14 @@ class HODLR3D:
     def launch_count(self) -> int:
         return int(self._L.hodlr3d_launch_count(self.handle))
 
+    def set_engine(self, engine: str) -> None:
+        """'auto', 'simt' (CUDA cores) or 'tc' (tcgen05 tensor cores, mixed form, 17..32 RHS)."""
+        check(self._L.hodlr3d_set_engine(self.handle, {"auto": 0, "simt": 1, "tc": 2}[engine]))
+
+    def device_status(self) -> None:
+        """Raises if a bounded device wait gave up in an earlier call."""
+        check(self._L.hodlr3d_device_status(self.handle))
+
     def set_profiling(self, enable: bool) -> None:
         """Records CUDA events between the matvec's kernel launches."""
         check(self._L.hodlr3d_set_profiling(self.handle, 1 if enable else 0))

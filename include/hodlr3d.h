@@ -173,6 +173,13 @@ int hodlr3d_get_pivots(hodlr3d_t h, int32_t* rows, int32_t* cols);
 int hodlr3d_get_pair_factors(hodlr3d_t h, int64_t pair, double* U, double* V);
 /* number of kernel launches issued by the library since creation */
 int64_t hodlr3d_launch_count(hodlr3d_t h);
+/* Matvec engine: 0 = automatic (tensor cores, tcgen05 3xTF32, for the mixed
+ * form with 17..32 right-hand sides, else CUDA-core kernels), 1 = CUDA-core
+ * kernels only, 2 = tensor cores only (HODLR3D_ERR_UNSUPPORTED elsewhere). */
+int hodlr3d_set_engine(hodlr3d_t h, int engine);
+/* Synchronises the device and reports HODLR3D_ERR_CUDA if a bounded
+ * tensor-core wait gave up in an earlier call on this handle. */
+int hodlr3d_device_status(hodlr3d_t h);
 /* Per-kernel timing of the matvec launches with CUDA events recorded between
  * them on the launch stream (off by default).  The report lists one line per
  * kernel, "name launches total_ms", accumulated since the last report. */

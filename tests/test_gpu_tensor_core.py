@@ -1,0 +1,77 @@
+"""The tensor-core engine (tcgen05 kind::tf32, 3xTF32) of the mixed-precision
+matvec against the CUDA-core engine and the reference's FP64 matvec.
+
+The engine takes A x with 17..32 right-hand sides on trees whose leaf
+populations are multiples of 4 (16-byte aligned FP32 operand rows); other
+cases are refused with HODLR3D_ERR_UNSUPPORTED when it is forced, and the
+automatic choice routes them to the CUDA-core engine."""
+import numpy as np
+import pytest
+import torch
+
+from golden_util import golden_names, load, points_of
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", params=golden_names())
+def case(request):
+    from hodlr3d_gb300 import HODLR3D
+    g = load(request.param)
+    H = HODLR3D(int(g["nP1D"]), float(g["L"]), int(g["tol_pow"]), int(g["kernel"]), points_of(g),
+                diag_override=float(g["diag"]))
+    H.assemble()
+    yield g, H
+    H.close()
+
+
+def tc_eligible(H):
+    return bool((np.diff(H.leaf_offsets()) % 4 == 0).all()) and int(np.diff(H.leaf_offsets()).max()) <= 128
+
+
+@pytest.mark.parametrize("nrhs", [32, 20])
+def test_tc_matches_simt_engine(case, nrhs):
+    g, H = case
+    X = torch.tensor(np.random.default_rng(nrhs).standard_normal((H.N, nrhs)), device="cuda")
+    H.set_engine("simt")
+    ys = H.matvec(X, "mixed")
+    H.set_engine("tc")
+    if not tc_eligible(H):
+        with pytest.raises(RuntimeError, match="tensor-core engine"):
+            H.matvec(X, "mixed")
+        H.set_engine("auto")
+        return
+    yt = H.matvec(X, "mixed")
+    H.set_engine("auto")
+    ya = H.matvec(X, "mixed")
+    H.device_status()
+    err = (torch.linalg.norm(yt - ys, dim=0) / torch.linalg.norm(ys, dim=0)).max().item()
+    assert err <= 2e-6, err
+    assert torch.equal(ya, yt)  # the automatic choice is the tensor-core engine here
+
+
+def test_tc_refuses_transpose(case):
+    g, H = case
+    X = torch.ones(H.N, 32, dtype=torch.float64, device="cuda")
+    H.set_engine("tc")
+    with pytest.raises(RuntimeError, match="tensor-core engine"):
+        H.matvec(X, "mixed", transpose=True)
+    H.set_engine("auto")
+    y = H.matvec(X, "mixed", transpose=True)  # served by the CUDA-core engine
+    assert torch.isfinite(y).all()
+
+
+def test_tc_matches_reference_fp64(case):
+    from hodlr3d_gb300.workloads import charges_uniform
+    g, H = case
+    if not tc_eligible(H):
+        pytest.skip("leaf populations not multiples of 4")
+    q = charges_uniform(H.N, seed=1)
+    X = torch.tensor(np.repeat(q[:, None], 32, axis=1), device="cuda")
+    H.set_engine("tc")
+    Y = H.matvec(X, "mixed").cpu().numpy()
+    H.set_engine("auto")
+    H.device_status()
+    ref = g["matvec"]
+    err = max(np.linalg.norm(Y[:, c] - ref) / np.linalg.norm(ref) for c in range(32))
+    assert err <= 2e-6, err
