@@ -285,12 +285,12 @@ __global__ void k_aca_compact(const AcaTask* __restrict__ tasks, const int32_t* 
   for (int64_t e = threadIdx.x; e < (int64_t)T.n * rp; e += blockDim.x) {
     const int64_t i = e / rp;
     const int l = (int)(e - i * rp);
-    u32[e] = l < r ? (float)U[(int64_t)l * T.n + i] : 0.f;
+    u32[e] = l < r ? tf32_split_value(U[(int64_t)l * T.n + i]) : 0.f;
   }
   for (int64_t e = threadIdx.x; e < mp * r; e += blockDim.x) {
     const int l = (int)(e / mp);
     const int64_t i = e - (int64_t)l * mp;
-    v32[e] = i < T.m ? (float)V[(int64_t)l * T.m + i] : 0.f;
+    v32[e] = i < T.m ? tf32_split_value(V[(int64_t)l * T.m + i]) : 0.f;
   }
 }
 

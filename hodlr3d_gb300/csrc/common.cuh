@@ -89,6 +89,30 @@ __device__ __forceinline__ float entry32_offdiag(const KernelDesc& kd, float dx,
 }
 
 // ---------------------------------------------------------------------------
+// TF32 forms of FP32 data for the tensor-core engine (a TF32 value is an FP32
+// value whose 13 low mantissa bits are zero; the tensor core reads an FP32
+// word as TF32 by ignoring those bits).
+// ---------------------------------------------------------------------------
+// x rounded to the nearest TF32 value (ties away from zero): half a TF32 ulp
+// added to the magnitude bits, the low bits cleared.
+__device__ __forceinline__ float tf32_rn(float x) {
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
+// x with the low bits cleared (rounded toward zero)
+__device__ __forceinline__ float tf32_rz(float x) {
+  return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+}
+// The "split-exact" FP32 form of x: v = hi + lo with hi = tf32_rz(v), the
+// truncation of x, and lo = v - hi the remainder x - hi rounded to 11
+// significant bits, so that both parts of v are TF32 and the tensor core
+// reads hi straight from v.  |v - x| <= 2^-22 |x|.
+__device__ __forceinline__ float tf32_split_value(double x) {
+  const float hi = tf32_rz(__double2float_rz(x));
+  const float lo = tf32_rn((float)(x - (double)hi));
+  return hi + lo;
+}
+
+// ---------------------------------------------------------------------------
 // Warp reductions
 // ---------------------------------------------------------------------------
 // The canonical reduction: each lane holds the sequential sum of its strided

@@ -171,8 +171,9 @@ struct hodlr3d_handle {
   std::vector<int32_t> h_fac_pool;      // per pair: pool index
   std::vector<double*> h_u64, h_v64;
   std::vector<float*> h_u32, h_v32;
-  DevBuf rank, u64, v64, u32, v32, tr_off, part_off, items, upper, pair_level;
-  int64_t sum_rank = 0, part_total = 0, n_items = 0, n_upper = 0, factor_entries = 0;
+  DevBuf rank, u64, v64, u32, v32, tr_off, tr_off4, part_off, items, upper, pair_level;
+  int64_t sum_rank = 0, sum_rank4 = 0, part_total = 0, n_items = 0, n_upper = 0, factor_entries = 0;
+  int tc_entries = 0;  // largest table of a tensor-core block
   int64_t u_entries = 0, v_entries = 0;
   int max_slice = 0;
   int max_rank = 0;
@@ -215,6 +216,7 @@ struct hodlr3d_handle {
   DevBuf dev_err;   // set by kernels whose bounded waits gave up
   bool leaves_aligned = false;  // every leaf population a multiple of 4
   DevBuf knear, near_off;       // FP32 near-field blocks of the tensor-core engine
+  DevBuf tct;                   // X and T of the tensor-core engine, split into TF32 parts
   bool near_built = false;
   int64_t near_floats = 0;
   void* pinned_x = nullptr;
@@ -560,13 +562,15 @@ int assemble(hodlr3d_t h) {
   // per-pair tables for the matvec: T offsets, slice work items of the
   // non-leaf pairs, partial offsets of the pairs above level d - 1
   const int d = h->levels;
-  std::vector<int64_t> tr(np), po(np, -1);
+  std::vector<int64_t> tr(np), tr4(np), po(np, -1);
   std::vector<int32_t> items, upper;
-  int64_t acc = 0, pacc = 0, fe = 0, ue = 0, ve = 0;
+  int64_t acc = 0, acc4 = 0, pacc = 0, fe = 0, ue = 0, ve = 0;
   h->max_rank = 0;
   for (int64_t p = 0; p < np; ++p) {
     tr[p] = acc;
     acc += h->h_rank[p];
+    tr4[p] = acc4;
+    acc4 += (h->h_rank[p] + 3) & ~3;
     h->max_rank = std::max(h->max_rank, h->h_rank[p]);
     const int j = h->h_pair_level[p];
     const int64_t kt = h->h_pair_tgt[p] - h3d::level_base(j), ks = h->h_pair_src[p] - h3d::level_base(j);
@@ -594,7 +598,25 @@ int assemble(hodlr3d_t h) {
     for (int64_t b = 0; b < (int64_t(1) << (3 * (d - 1))); ++b)
       h->max_slice = std::max(h->max_slice, h->h_leaf_off[(b + 1) << 3] - h->h_leaf_off[b << 3]);
   }
+  // table sizes of the tensor-core blocks: per level d - 1 box the pairs of
+  // its ancestors (interaction lists are symmetric, so as many by source as
+  // by target), per leaf its pairs plus 27 near-field blocks
+  h->tc_entries = 0;
+  {
+    auto cnt = [&](int j, int64_t b) {
+      const int64_t gb = h3d::level_base(j) + b;
+      return (int)(h->h_il_ptr[gb + 1] - h->h_il_ptr[gb]);
+    };
+    if (d >= 2)
+      for (int64_t b = 0; b < (int64_t(1) << (3 * (d - 1))); ++b) {
+        int n = 0;
+        for (int j = 1; j <= d - 1; ++j) n += cnt(j, b >> (3 * (d - 1 - j)));
+        h->tc_entries = std::max(h->tc_entries, n);
+      }
+    for (int64_t k = 0; k < h->nleaf; ++k) h->tc_entries = std::max(h->tc_entries, cnt(d, k) + 27);
+  }
   h->sum_rank = acc;
+  h->sum_rank4 = acc4;
   h->part_total = pacc;
   h->n_items = (int64_t)items.size() / 2;
   h->n_upper = (int64_t)upper.size();
@@ -609,6 +631,7 @@ int assemble(hodlr3d_t h) {
   H3D_CUDA(h->u32.ensure(sizeof(void*) * npb));
   H3D_CUDA(h->v32.ensure(sizeof(void*) * npb));
   H3D_CUDA(h->tr_off.ensure(sizeof(int64_t) * npb));
+  H3D_CUDA(h->tr_off4.ensure(sizeof(int64_t) * npb));
   H3D_CUDA(h->part_off.ensure(sizeof(int64_t) * npb));
   H3D_CUDA(h->items.ensure(sizeof(int32_t) * std::max<size_t>(items.size(), 2)));
   H3D_CUDA(h->upper.ensure(sizeof(int32_t) * std::max<size_t>(upper.size(), 1)));
@@ -620,6 +643,7 @@ int assemble(hodlr3d_t h) {
     H3D_CUDA(cudaMemcpyAsync(h->u32.p, h->h_u32.data(), sizeof(void*) * np, cudaMemcpyHostToDevice, s));
     H3D_CUDA(cudaMemcpyAsync(h->v32.p, h->h_v32.data(), sizeof(void*) * np, cudaMemcpyHostToDevice, s));
     H3D_CUDA(cudaMemcpyAsync(h->tr_off.p, tr.data(), sizeof(int64_t) * np, cudaMemcpyHostToDevice, s));
+    H3D_CUDA(cudaMemcpyAsync(h->tr_off4.p, tr4.data(), sizeof(int64_t) * np, cudaMemcpyHostToDevice, s));
     H3D_CUDA(cudaMemcpyAsync(h->part_off.p, po.data(), sizeof(int64_t) * np, cudaMemcpyHostToDevice, s));
     H3D_CUDA(cudaMemcpyAsync(h->pair_level.p, h->h_pair_level.data(), sizeof(int32_t) * np,
                              cudaMemcpyHostToDevice, s));
@@ -674,6 +698,7 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
   far.pair_tgt = h->pair_tgt.as<int32_t>();
   far.pair_src = h->pair_src.as<int32_t>();
   far.tr_off = h->tr_off.as<int64_t>();
+  far.tr_off4 = h->tr_off4.as<int64_t>();
   far.part_off = h->part_off.as<int64_t>();
   far.ufac = f32 ? h->u32.as<const void*>() : h->u64.as<const void*>();
   far.vfac = f32 ? h->v32.as<const void*>() : h->v64.as<const void*>();
@@ -699,11 +724,12 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
   B.max_slice = h->max_slice;
   const int nrp = h3d::padded_nrhs(nrhs);
   const bool tc_ok = precision == HODLR3D_MIXED && nrp == 32 && !trans && h->max_leaf <= 128 &&
-                     h->leaves_aligned;
+                     h->leaves_aligned && h->tc_entries <= h3d::tc_max_entries();
   if (h->engine == 2 && !tc_ok)
     return set_error(HODLR3D_ERR_UNSUPPORTED,
                      "the tensor-core engine needs A x (not the transpose) in the mixed form, 17..32 "
-                     "right-hand sides, and leaves of at most 128 points, each a multiple of 4");
+                     "right-hand sides, leaves of at most 128 points, each a multiple of 4, and at "
+                     "most %d pairs per block (this tree: %d)", h3d::tc_max_entries(), h->tc_entries);
   if (tc_ok && h->engine != 1) {
     if (!h->dev_err.p) {
       H3D_CUDA(h->dev_err.ensure(sizeof(int)));
@@ -736,9 +762,13 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
       h->near_floats = tot;
       h->near_built = true;
     }
+    // [X hi | T hi | X lo | T lo], TF32 high and low parts of the B operands
+    const int64_t half_len = 32 * (h->N + std::max<int64_t>(h->sum_rank4, 1));
+    H3D_CUDA(h->tct.ensure(sizeof(float) * 2 * half_len));
     h3d::TcBuffers T{};
-    T.xt = static_cast<float*>(h->xsorted.p);
-    T.t = static_cast<float*>(h->tbuf.p);
+    T.xt = h->tct.as<float>();
+    T.t = T.xt + 32 * h->N;
+    T.lo_off = half_len;
     T.p = reinterpret_cast<float*>(h->pbuf.p);
     T.ynl = h->ynl.as<double>();
     T.err = h->dev_err.as<int>();
@@ -1017,6 +1047,7 @@ int hodlr3d_matvec_noalloc(hodlr3d_t h, const double* x, double* y, int nrhs, in
   far.pair_tgt = h->pair_tgt.as<int32_t>();
   far.pair_src = h->pair_src.as<int32_t>();
   far.tr_off = h->tr_off.as<int64_t>();
+  far.tr_off4 = h->tr_off4.as<int64_t>();
   far.part_off = h->part_off.as<int64_t>();
   far.ufac = f32 ? h->u32.as<const void*>() : h->u64.as<const void*>();
   far.vfac = f32 ? h->v32.as<const void*>() : h->v64.as<const void*>();

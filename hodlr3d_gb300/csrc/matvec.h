@@ -23,6 +23,7 @@ struct FarOp {
   const int32_t* pair_src;
   const int64_t* tr_off;      // per pair: offset of its r rows in T (times the padded nrhs)
   const int64_t* part_off;    // per pair above level d - 1: offset of its slice partials
+  const int64_t* tr_off4;     // per pair: offset of its round4(r) rows in the tensor-core T
   const void* const* ufac;    // per pair U pointer (double* or float*)
   const void* const* vfac;    // per pair V pointer
 };
@@ -68,7 +69,8 @@ int padded_nrhs(int nrhs);
 // points.  FP64 factors are column-major with leading dimension n.  In the
 // FP32 copies U is row-major with the rank padded to a multiple of 4 and V is
 // column-major with n padded to a multiple of 4 (zero padding), so that every
-// row of U and column of V starts on 16 bytes for the tensor-core kernels.
+// row of U and column of V starts on 16 bytes for the tensor-core kernels;
+// their values are in the split-exact TF32 form (tf32_split_value).
 template <typename FT, bool IS_U>
 __host__ __device__ __forceinline__ int64_t fac_idx(int64_t i, int l, int r, int64_t n) {
   if (sizeof(FT) == 8) return (int64_t)l * n + i;
@@ -77,11 +79,16 @@ __host__ __device__ __forceinline__ int64_t fac_idx(int64_t i, int l, int r, int
 }
 
 // Work buffers of the tensor-core form (32 right-hand sides, FP32):
-// xt: 32 * N, t: 32 * sum_rank, p: 32 * part_total floats; ynl: 32 * N doubles;
-// err: device flag set when an mbarrier wait gives up.
+// xt: 32 * N floats, X in tree order, x(t, c) at xt[c N + t]; t: 32 * sum of
+// round4(rank) floats, pair p's T_p (c, l) at t[32 tr_off4[p] + c round4(r) + l],
+// zero padded.  Both hold TF32 values (the high parts); the low parts are at
+// the same index plus lo_off.  p: 32 * part_total floats; ynl: 32 * N doubles;
+// err: device flag, 1 when an mbarrier wait gave up, 2 when a block's table
+// exceeded tc_max_entries().
 struct TcBuffers {
   float* xt;
   float* t;
+  int64_t lo_off;
   float* p;
   double* ynl;
   int* err;
@@ -98,6 +105,9 @@ struct TcBuffers {
 int launch_matvec_tc(cudaStream_t s, int64_t N, const int32_t* perm, const FarOp& far,
                      const NearOp& near, const TcBuffers& B, const double* X, int64_t ldx,
                      double* Y, int64_t ldy, int nrhs, MatvecProfiler* prof);
+// Largest number of table entries (pairs of all levels a block multiplies, or
+// a leaf's pairs plus 27 near-field blocks) one tensor-core block takes.
+int tc_max_entries();
 // Evaluates the FP32 near-field blocks of every leaf (row-major nk x round4(ne)
 // at near_off[27 k + slot], slots 0..25 the neighbours, 26 the leaf itself).
 int launch_near_blocks(cudaStream_t s, int64_t nleaf, const int32_t* leaf_off, const NearOp& near,
