@@ -91,6 +91,7 @@ def lib() -> ctypes.CDLL:
         "hodlr3d_assemble": ([vp], i32),
         "hodlr3d_matvec": ([vp, vp, vp, i32, i64, i32, vp], i32),
         "hodlr3d_matvec_host": ([vp, vp, vp, i32, i64, i32], i32),
+        "hodlr3d_matvec_host_rows": ([vp, vp, vp, i32, i32], i32),
         "hodlr3d_matvec_transpose": ([vp, vp, vp, i32, i64, i32, vp], i32),
         "hodlr3d_dense_rows": ([vp, vp, i64, vp, vp, i32, i64, vp], i32),
         "hodlr3d_gmres": ([vp, vp, vp, i32, i64, ctypes.POINTER(GmresParams),

@@ -4,9 +4,14 @@
 // Reference interfaces replaced: HODLR3D (include/HODLR3D.hpp:12-21,
 // src/HODLR3D.cpp), HODLR3DTree (include/HODLR3DTree.hpp, src/HODLR3DTree.cpp),
 // LowRank (src/ACA.cpp), classGMRES (include/gmres.hpp, src/gmres.cpp).
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <mutex>
+#include <thread>
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
@@ -180,7 +185,7 @@ struct hodlr3d_handle {
   double assemble_seconds = 0.0;
   int aca_batches = 0;
   // matvec work buffers
-  DevBuf xsorted, tbuf, pbuf, ynl, stage_x, stage_y;
+  DevBuf xsorted, tbuf, pbuf, ynl, stage_x, stage_y, stage_t;
   int mv_nrhs_cap = 0;
   // optional per-kernel timing of matvec launches
   struct Prof : h3d::MatvecProfiler {
@@ -216,20 +221,18 @@ struct hodlr3d_handle {
   DevBuf dev_err;   // set by kernels whose bounded waits gave up
   bool leaves_aligned = false;  // every leaf population a multiple of 4
   DevBuf knear, near_off;       // FP32 near-field blocks of the tensor-core engine
-  DevBuf tct;                   // X and T of the tensor-core engine, split into TF32 parts
+  DevBuf tct;                   // X and T of the tensor-core engine (split-exact FP32)
+  DevBuf tmaps;                 // tensor maps of the tensor-core engine: U, V, near blocks
+  bool maps_built = false;
   bool near_built = false;
+  std::vector<int32_t> h_nbr_leaf;  // host copy (tensor maps of the near-field blocks)
   int64_t near_floats = 0;
-  void* pinned_x = nullptr;
-  void* pinned_y = nullptr;
-  size_t pinned_bytes = 0;
   // GMRES work buffers
   DevBuf g_Q, g_w, g_r, g_x, g_b, g_H, g_cs, g_sn, g_beta, g_hk, g_bnorm, g_err, g_part, g_y,
       g_kcol, g_brk, g_scal, g_d, g_coef;
 
   ~hodlr3d_handle() {
     for (DevBuf* b : pools) delete b;
-    if (pinned_x) cudaFreeHost(pinned_x);
-    if (pinned_y) cudaFreeHost(pinned_y);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -656,6 +659,10 @@ int assemble(hodlr3d_t h) {
                              cudaMemcpyHostToDevice, s));
   H3D_CUDA(cudaStreamSynchronize(s));
   h->mv_nrhs_cap = 0;
+  // the tensor-core engine's near-field blocks and tensor maps (which point
+  // at the factors) are rebuilt on its next use
+  h->near_built = false;
+  h->maps_built = false;
   h->assembled = true;
   h->assemble_seconds = now_s() - t_start;
   return HODLR3D_OK;
@@ -672,6 +679,79 @@ int ensure_matvec_buffers(hodlr3d_t h, int nrhs) {
   H3D_CUDA(h->pbuf.ensure(sizeof(double) * std::max<int64_t>(h->part_total, 1) * nr));
   H3D_CUDA(h->ynl.ensure(sizeof(double) * h->N * nr));
   h->mv_nrhs_cap = nr;
+  return HODLR3D_OK;
+}
+
+// Tensor maps (2D tiled, FP32, 128-byte swizzle, zero fill outside) of the
+// tensor-core engine's A operands: per pair U_p (n x round4(r), box 32 x 128)
+// and V_p (r x round4(m), box 32 x 8), per leaf and neighbour slot the
+// near-field block (nk x round4(ne), box 32 x 128).  Maps of empty operands
+// stay zero and are never used.
+int build_tensor_maps(hodlr3d_t h, const std::vector<int64_t>& near_off) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    cudaDriverEntryPointQueryResult q;
+    H3D_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", (void**)&encode, 12000,
+                                              cudaEnableDefault, &q));
+    if (!encode || q != cudaDriverEntryPointSuccess)
+      return set_error(HODLR3D_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+  }
+  const int64_t np = h->npairs, nm = 2 * np + 27 * h->nleaf;
+  std::vector<CUtensorMap> maps((size_t)std::max<int64_t>(nm, 1));
+  std::memset(maps.data(), 0, sizeof(CUtensorMap) * maps.size());
+  std::atomic<int> bad{0};
+  std::mutex bad_mu;
+  char bad_msg[160] = {0};
+  auto enc = [&](CUtensorMap* m, const float* base, int64_t inner, int64_t rows, uint32_t box_rows) {
+    if (!base || inner <= 0 || rows <= 0) return;
+    const cuuint64_t dim[2] = {(cuuint64_t)inner, (cuuint64_t)rows};
+    const cuuint64_t stride[1] = {(cuuint64_t)inner * sizeof(float)};
+    const cuuint32_t box[2] = {32, box_rows}, es[2] = {1, 1};
+    const CUresult r = encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dim, stride, box, es,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS && !bad.exchange(1)) {
+      std::lock_guard<std::mutex> g(bad_mu);
+      std::snprintf(bad_msg, sizeof(bad_msg), "code %d, %lld x %lld at %p, box 32 x %u, map at %p",
+                    (int)r, (long long)rows, (long long)inner, (const void*)base, box_rows, (void*)m);
+    }
+  };
+  const float* knear = h->knear.as<float>();
+  const int nthr = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  std::vector<std::thread> th;
+  for (int t = 0; t < nthr; ++t)
+    th.emplace_back([&, t] {
+      cudaSetDevice(h->opt.device);  // the encoder wants the device's context current
+      for (int64_t p = t; p < np; p += nthr) {
+        const int r = h->h_rank[p];
+        if (r <= 0) continue;
+        const int j = h->h_pair_level[p];
+        int64_t a0, a1, b0, b1;
+        box_range(h, j, h->h_pair_tgt[p] - h3d::level_base(j), a0, a1);
+        box_range(h, j, h->h_pair_src[p] - h3d::level_base(j), b0, b1);
+        enc(&maps[p], h->h_u32[p], (r + 3) & ~3, a1 - a0, 128);
+        enc(&maps[np + p], h->h_v32[p], ((b1 - b0) + 3) & ~int64_t(3), r, 8);
+      }
+      for (int64_t k = t; k < h->nleaf; k += nthr) {
+        const int64_t nk = h->h_leaf_off[k + 1] - h->h_leaf_off[k];
+        for (int sl = 0; sl < 27; ++sl) {
+          const int64_t off = near_off[27 * k + sl];
+          if (off < 0) continue;
+          const int64_t nn = sl < 26 ? h->h_nbr_leaf[26 * k + sl] : k;
+          const int64_t ne = h->h_leaf_off[nn + 1] - h->h_leaf_off[nn];
+          enc(&maps[2 * np + 27 * k + sl], knear + off, (ne + 3) & ~int64_t(3), nk, 128);
+        }
+      }
+    });
+  for (auto& x : th) x.join();
+  if (bad) {
+    std::lock_guard<std::mutex> g(bad_mu);
+    return set_error(HODLR3D_ERR_CUDA, "a tensor map could not be encoded (%s)", bad_msg);
+  }
+  H3D_CUDA(h->tmaps.ensure(sizeof(CUtensorMap) * maps.size()));
+  H3D_CUDA(cudaMemcpy(h->tmaps.p, maps.data(), sizeof(CUtensorMap) * maps.size(),
+                      cudaMemcpyHostToDevice));
+  h->maps_built = true;
   return HODLR3D_OK;
 }
 
@@ -737,9 +817,10 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
     }
     if (!h->near_built) {
       // FP32 near-field blocks, evaluated once
-      std::vector<int32_t> nbl(26 * h->nleaf);
-      H3D_CUDA(cudaMemcpy(nbl.data(), h->nbr_leaf.p, sizeof(int32_t) * 26 * h->nleaf,
+      h->h_nbr_leaf.resize(26 * h->nleaf);
+      H3D_CUDA(cudaMemcpy(h->h_nbr_leaf.data(), h->nbr_leaf.p, sizeof(int32_t) * 26 * h->nleaf,
                           cudaMemcpyDeviceToHost));
+      const std::vector<int32_t>& nbl = h->h_nbr_leaf;
       std::vector<int64_t> off(27 * h->nleaf, -1);
       int64_t tot = 0;
       for (int64_t k = 0; k < h->nleaf; ++k) {
@@ -761,14 +842,13 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
       H3D_CUDA(cudaGetLastError());
       h->near_floats = tot;
       h->near_built = true;
+      H3D_TRY(build_tensor_maps(h, off));
     }
-    // [X hi | T hi | X lo | T lo], TF32 high and low parts of the B operands
-    const int64_t half_len = 32 * (h->N + std::max<int64_t>(h->sum_rank4, 1));
-    H3D_CUDA(h->tct.ensure(sizeof(float) * 2 * half_len));
+    // [X | T], the B operands in the split-exact form
+    H3D_CUDA(h->tct.ensure(sizeof(float) * 32 * (h->N + std::max<int64_t>(h->sum_rank4, 1))));
     h3d::TcBuffers T{};
     T.xt = h->tct.as<float>();
     T.t = T.xt + 32 * h->N;
-    T.lo_off = half_len;
     T.p = reinterpret_cast<float*>(h->pbuf.p);
     T.ynl = h->ynl.as<double>();
     T.err = h->dev_err.as<int>();
@@ -777,6 +857,10 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
     T.max_slice = h->max_slice;
     T.knear = h->knear.as<float>();
     T.near_off = h->near_off.as<int64_t>();
+    const CUtensorMap* tm = h->tmaps.as<CUtensorMap>();
+    T.umaps = tm;
+    T.vmaps = tm + h->npairs;
+    T.nmaps = tm + 2 * h->npairs;
     h->launches += h3d::launch_matvec_tc(s, h->N, h->perm.as<int32_t>(), far, nr, T, x, ld, y, ld,
                                          nrhs, h->profiling ? &h->prof : nullptr);
   } else {
@@ -1083,27 +1167,35 @@ int hodlr3d_matvec_host(hodlr3d_t h, const double* x, double* y, int nrhs, int64
   if (!x || !y) return set_error(HODLR3D_ERR_INVALID_ARG, "null vector");
   if (nrhs < 1 || nrhs > 64 || ld < h->N) return set_error(HODLR3D_ERR_INVALID_ARG, "bad nrhs or ld");
   const size_t bytes = sizeof(double) * h->N * nrhs;
-  if (bytes > h->pinned_bytes) {
-    if (h->pinned_x) cudaFreeHost(h->pinned_x);
-    if (h->pinned_y) cudaFreeHost(h->pinned_y);
-    h->pinned_x = h->pinned_y = nullptr;
-    h->pinned_bytes = 0;
-    H3D_CUDA(cudaMallocHost(&h->pinned_x, bytes));
-    H3D_CUDA(cudaMallocHost(&h->pinned_y, bytes));
-    h->pinned_bytes = bytes;
-  }
   H3D_CUDA(h->stage_x.ensure(bytes));
   H3D_CUDA(h->stage_y.ensure(bytes));
   cudaStream_t s = h->stream;
-  // pack the caller's columns into pinned memory, copy in, multiply, copy out
-  double* px = static_cast<double*>(h->pinned_x);
-  double* py = static_cast<double*>(h->pinned_y);
-  for (int c = 0; c < nrhs; ++c) std::memcpy(px + c * h->N, x + c * ld, sizeof(double) * h->N);
-  H3D_CUDA(cudaMemcpyAsync(h->stage_x.p, px, bytes, cudaMemcpyHostToDevice, s));
+  // the copy engines read and write the caller's (pageable) columns directly
+  const size_t col = sizeof(double) * h->N, pitch = sizeof(double) * ld;
+  H3D_CUDA(cudaMemcpy2DAsync(h->stage_x.p, col, x, pitch, col, nrhs, cudaMemcpyHostToDevice, s));
   H3D_TRY(matvec_device(h, h->stage_x.as<double>(), h->stage_y.as<double>(), nrhs, h->N, precision, s, false));
-  H3D_CUDA(cudaMemcpyAsync(py, h->stage_y.p, bytes, cudaMemcpyDeviceToHost, s));
+  H3D_CUDA(cudaMemcpy2DAsync(y, pitch, h->stage_y.p, col, col, nrhs, cudaMemcpyDeviceToHost, s));
   H3D_CUDA(cudaStreamSynchronize(s));
-  for (int c = 0; c < nrhs; ++c) std::memcpy(y + c * ld, py + c * h->N, sizeof(double) * h->N);
+  return HODLR3D_OK;
+}
+
+int hodlr3d_matvec_host_rows(hodlr3d_t h, const double* x, double* y, int nrhs, int precision) {
+  H3D_TRY(check_handle(h));
+  if (!x || !y) return set_error(HODLR3D_ERR_INVALID_ARG, "null vector");
+  if (nrhs < 1 || nrhs > 64) return set_error(HODLR3D_ERR_INVALID_ARG, "bad nrhs");
+  const size_t bytes = sizeof(double) * h->N * nrhs;
+  H3D_CUDA(h->stage_x.ensure(bytes));
+  H3D_CUDA(h->stage_y.ensure(bytes));
+  H3D_CUDA(h->stage_t.ensure(bytes));
+  cudaStream_t s = h->stream;
+  H3D_CUDA(cudaMemcpyAsync(h->stage_t.p, x, bytes, cudaMemcpyHostToDevice, s));
+  h3d::launch_transpose(s, h->stage_t.as<double>(), h->N, nrhs, h->stage_x.as<double>());
+  H3D_TRY(matvec_device(h, h->stage_x.as<double>(), h->stage_y.as<double>(), nrhs, h->N, precision, s, false));
+  h3d::launch_transpose(s, h->stage_y.as<double>(), nrhs, h->N, h->stage_t.as<double>());
+  h->launches += 2;
+  H3D_CUDA(cudaGetLastError());
+  H3D_CUDA(cudaMemcpyAsync(y, h->stage_t.p, bytes, cudaMemcpyDeviceToHost, s));
+  H3D_CUDA(cudaStreamSynchronize(s));
   return HODLR3D_OK;
 }
 

@@ -463,6 +463,29 @@ __global__ void k_dense_rows(int64_t N, const double* __restrict__ xyz, KernelDe
   }
 }
 
+namespace {
+// 32 x 32 tiles through shared memory (one padding column against bank conflicts)
+__global__ void k_transpose(const double* __restrict__ in, int64_t rows, int64_t cols,
+                            double* __restrict__ out) {
+  __shared__ double tile[32][33];
+  const int64_t r0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int64_t r = r0 + i, c = c0 + threadIdx.x;
+    if (r < rows && c < cols) tile[i][threadIdx.x] = in[r * cols + c];
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int64_t c = c0 + i, r = r0 + threadIdx.x;
+    if (r < rows && c < cols) out[c * rows + r] = tile[threadIdx.x][i];
+  }
+}
+}  // namespace
+
+void launch_transpose(cudaStream_t s, const double* in, int64_t rows, int64_t cols, double* out) {
+  const dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
+  k_transpose<<<grid, dim3(32, 8), 0, s>>>(in, rows, cols, out);
+}
+
 void launch_dense_rows(cudaStream_t s, int64_t N, const double* xyz, KernelDesc kd,
                        const int64_t* rows, int64_t nrows, const double* X, int64_t ldx,
                        double* Y, int nrhs) {

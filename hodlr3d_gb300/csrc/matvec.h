@@ -81,14 +81,13 @@ __host__ __device__ __forceinline__ int64_t fac_idx(int64_t i, int l, int r, int
 // Work buffers of the tensor-core form (32 right-hand sides, FP32):
 // xt: 32 * N floats, X in tree order, x(t, c) at xt[c N + t]; t: 32 * sum of
 // round4(rank) floats, pair p's T_p (c, l) at t[32 tr_off4[p] + c round4(r) + l],
-// zero padded.  Both hold TF32 values (the high parts); the low parts are at
-// the same index plus lo_off.  p: 32 * part_total floats; ynl: 32 * N doubles;
+// zero padded; both in the split-exact TF32 form.  p: 32 * part_total floats;
+// ynl: 32 * N doubles;
 // err: device flag, 1 when an mbarrier wait gave up, 2 when a block's table
 // exceeded tc_max_entries().
 struct TcBuffers {
   float* xt;
   float* t;
-  int64_t lo_off;
   float* p;
   double* ynl;
   int* err;
@@ -97,6 +96,13 @@ struct TcBuffers {
   int max_slice;
   const float* knear;        // FP32 near-field blocks (launch_near_blocks)
   const int64_t* near_off;   // 27 per leaf: block offsets, -1 for no neighbour
+  // 2D tensor maps (CUtensorMap, 128 bytes each) of the FP32 operands A:
+  // umaps[p]: U_p as n x round4(r), box 32 x 128; vmaps[p]: V_p as
+  // r x round4(m), box 32 x 8; nmaps[27 k + s]: near-field block s of leaf k
+  // as nk x round4(ne), box 32 x 128.  128-byte swizzle, zero fill.
+  const void* umaps;
+  const void* vmaps;
+  const void* nmaps;
 };
 
 // Tensor-core mixed-precision product A X for 17..32 right-hand sides (padded
@@ -119,6 +125,9 @@ int launch_matvec(cudaStream_t s, int64_t N, const int32_t* perm, const FarOp& f
                   const NearOp& near, const MatvecBuffers& B, const double* X, int64_t ldx,
                   double* Y, int64_t ldy, int nrhs, int precision, int trans,
                   MatvecProfiler* prof);
+
+// out[c * rows + r] = in[r * cols + c] (rows x cols row-major -> column-major)
+void launch_transpose(cudaStream_t s, const double* in, int64_t rows, int64_t cols, double* out);
 
 void launch_dense_rows(cudaStream_t s, int64_t N, const double* xyz, KernelDesc kd,
                        const int64_t* rows, int64_t nrows, const double* X, int64_t ldx,

@@ -5,9 +5,9 @@
 //
 //   ta_slice  per (level d-1 box "slice", share of its row tiles): T of the
 //             pairs of levels 1..d-1 whose input box contains the slice, as a
-//             tall GEMM [V_p1^T; V_p2^T; ...] X_slice (M = concatenated pair
-//             columns in tiles of 128, K = slice points); level d-1 pairs get
-//             T, the pairs above get slice partials
+//             tall GEMM [V_p1^T; V_p2^T; ...] X_slice (M = pair columns packed
+//             in groups of 8 rows, tiles of 128 rows, K = slice points); level
+//             d-1 pairs get T, the pairs above get slice partials
 //   tred      FP64 sum of the slice partials
 //   ta_leaf   per input leaf: the same for the leaf-level pairs
 //   ut_tc     per (slice, 128 rows): long-K GEMM over the pairs of levels < d,
@@ -16,33 +16,40 @@
 //             and its near-field blocks (K_near X_near), plus the slice sum;
 //             written once in the original order
 //
-// Each block streams a sequence of K = 32 chunks: (tile, item, k0), a tile
-// being one M = 128 output tile and an item one operand pair (a factor A and
-// its right-hand sides B) summed into it.  Operand rows are contiguous,
-// 16-byte aligned runs of FP32 values (rows of the row-major FP32 U, columns
-// of the FP32 V, rows of the FP32 near-field blocks, columns of X and T).
+// A block streams K = 32 chunks over its M = 128 output tiles.  A T tile (ta)
+// runs over one K range, its input box; the tile of ut / leaf runs over its
+// items (operand pairs: a factor A and its right-hand sides B, summed into
+// the tile) one after the other.  Three roles, synchronised by mbarriers only:
 //
-// A (the factors, streamed from HBM, in the split-exact TF32 form) is copied
-// global -> shared with cp.async 16-byte copies, a warp moving 8 rows x 64
-// contiguous bytes per instruction, into a row-major staging tile whose
-// 16-byte columns are XOR-swizzled by the row; kAhead chunks are in flight.
-// The thread owning a row (two per row, 16 K values each) reads it back,
-// splits v = hi + lo (hi = v with the low 13 bits cleared, lo = v - hi, both
-// exact TF32) and stores both parts to tensor memory.  B (the right-hand
-// sides X or T, held in global memory as TF32 high and low parts) is copied
-// to shared memory in the canonical K-major layout, [B_hi; B_lo] stacked as
-// one N = 64 operand.  Two issuer warps then issue, per K = 8 step,
-//   A_hi [B_hi | B_lo] -> accumulator D (N = 64: hi*hi, hi*lo)
-//   A_lo B_hi          -> accumulator D2 (N = 32: lo*hi)
-// (A read from tensor memory, so the tensor core reads only B from shared
-// memory; the lo*lo term, below 2^-22 of the product, is left out).  Groups
-// of kGroupChunks chunks alternate between two accumulator sets; a group is
-// read back while the next one is multiplied, its hi*hi part summed with
-// compensated (Kahan) FP32 additions (whose error matches an FP64 sum here at
-// a fraction of the cost of GB300's FP64 units) and its cross parts with
-// plain FP32 additions.
+//   producer (one warp)    copies A global -> shared with the tensor memory
+//                          accelerator: 2D tiled loads from one tensor map per
+//                          factor (box 32 K x 128 rows, or 32 x 8 for the V of
+//                          the T kernels), 128-byte swizzle, zero fill outside
+//                          the factor; up to kSlots chunks ahead
+//   workers (8 warps)      copy B (X or T, 32 columns) with 16-byte cp.async
+//                          into the canonical K-major layout; split A and B
+//                          into TF32 parts (below); read the accumulators back
+//   issuers (2 threads)    issue, per K = 8 step,
+//                            A_hi [B_hi | B_lo] -> D  (N = 64: hi*hi, hi*lo)
+//                            A_lo B_hi          -> D2 (N = 32: lo*hi)
+//                          with A read from tensor memory, so the tensor core
+//                          reads only B from shared memory
+//
+// The factors, X and T are held in the split-exact FP32 form (common.cuh): v =
+// hi + lo with hi = v with the 13 low mantissa bits cleared and lo = v - hi,
+// both exact TF32.  The worker owning a row (two per row, 16 K values each)
+// reads it from the swizzled tile, stores hi and lo to tensor memory; the
+// thread that copied a B segment writes its low part next to it (the tensor
+// core reads B_hi from the copy itself).  The lo*lo term, below 2^-22 of the
+// product, is left out.  Groups of kGroupChunks chunks alternate between two
+// accumulator sets; a group is read back while the next one is multiplied, its
+// hi*hi part summed with compensated (Kahan) FP32 additions (whose error
+// matches an FP64 sum here at a fraction of the cost of GB300's FP64 units)
+// and its cross parts with plain FP32 additions.
 //
 // Every mbarrier wait is bounded; a wait that gives up sets the error flag.
+#include <cuda.h>
+
 #include <algorithm>
 
 #include "matvec.h"
@@ -54,13 +61,15 @@ namespace {
 
 constexpr int NR = 32;                     // right-hand sides (MMA N)
 constexpr int KC = 32;                     // K per chunk
-constexpr int WORKERS = 256;               // copy, split and read back: two threads per row
-constexpr int THREADS = WORKERS + 64;      // plus two MMA issuer warps
+constexpr int WORKERS = 256;               // copy B, split and read back: two threads per row
+constexpr int ISSUER0 = WORKERS;           // warps 8, 9: MMA issuers
+constexpr int PRODUCER = WORKERS + 64;     // warp 10: A copies
+constexpr int THREADS = WORKERS + 96;
 constexpr int A_BYTES = 128 * KC * 4;      // A chunk (16 KB)
 constexpr int B_BYTES = NR * KC * 4;       // one TF32 part of a B chunk (4 KB)
-constexpr int SLOT_BYTES = A_BYTES + 2 * B_BYTES;  // copy slot: A, B hi, B lo
-constexpr int kSlots = 8;                  // copy slots
-constexpr int kAhead = kSlots - 2;         // chunks in flight ahead of the multiplied one
+constexpr int SLOT_BYTES = A_BYTES + 2 * B_BYTES;  // slot: A, B hi, B lo
+constexpr int kSlots = 8;
+constexpr int kAhead = kSlots - 2;         // B chunks in flight ahead of the multiplied one
 constexpr int TAB_OFF = kSlots * SLOT_BYTES;
 constexpr int kMaxEntries = 768;           // table entries (pairs, near blocks) of one block
 constexpr int ENTRY_BYTES = 32;
@@ -74,8 +83,16 @@ constexpr uint32_t IDESC32 = tc::idesc_tf32(128, NR);
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t TM_A = 256;
 constexpr int kGroupChunks = 2;            // chunks per accumulation group (K = 64)
+// barriers
+constexpr int BAR_FULL = 0;                // [kSlots] A of the slot landed (producer, tx)
+constexpr int BAR_EMPTY = kSlots;          // [kSlots] slot no longer read (issuer commits)
+constexpr int BAR_READY = 2 * kSlots;      // [2] chunk parity split (one arrival per worker warp)
+constexpr int BAR_MPAR = BAR_READY + 2;    // [2] chunk parity multiplied (issuer commits)
+constexpr int BAR_ACC = BAR_MPAR + 2;      // [2] accumulator set complete (issuer commits)
+constexpr int NBAR = BAR_ACC + 2;
 
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
+static_assert(SLOT_BYTES % 1024 == 0, "128-byte swizzled tiles start on 1024 bytes");
 
 __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
   const float y = x - c;
@@ -97,97 +114,92 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-// One item of a block's stream as one thread sees it: its four A rows
-// rb + 8 i (nullptr for a row outside the tile) with alen valid entries, and
-// B column c at b + c * bs with blen valid entries; the item spans blen (a
-// multiple of 4) values of K.
-struct View {
-  const float* arow[4];
-  const float* b;  // high part; the low part at b + lo_off
-  int64_t bs;
-  int alen;
-  int blen;
+__device__ __forceinline__ void expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(tc::smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// 2D tiled tensor load of the box at (x, y) into shared memory, completing on bar
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3}], [%4];\n" ::"r"(tc::smem_addr(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(tc::smem_addr(bar))
+      : "memory");
+}
+
+// This worker's B copy: k quad qb of column cb to offB of the slot (its low
+// part goes to offB + B_BYTES).
+struct CopyMap {
+  int cb, qb;
+  uint32_t offB;
 };
 
-// A table entry of the long-K kernels: rows of A at a + i * as.
+// A table entry of the long-K kernels: A is the box at (k, y) of map, B column
+// c at b + c bs; blen values of K (a multiple of 4).
 struct Item {
-  const float* a;
+  const CUtensorMap* map;
   const float* b;
-  int as;
+  int y;
   int bs;
-  int alen;
   int blen;
+  int pad;
 };
 static_assert(sizeof(Item) == ENTRY_BYTES, "entry");
 
-// A table entry of the T kernels: pair column l has its A row at
-// a + l * lda and its output (c, l) at dst[c * ld + l]; r values of l.  pad:
-// the output is T (TF32 high and low parts, zero padded to ld), else a slice
-// partial (FP32).
+// A table entry of the T kernels: pair column l is row l of map (the pair's V
+// as an r x round4(m) tensor) read from column ro on; its output (c, l) goes to
+// dst[c * ld + l].  t: dst is T (split-exact, zero padded to ld), else a
+// slice partial (FP32).
 struct PairRow {
-  const float* a;
+  const CUtensorMap* map;
   float* dst;
-  int lda;
+  int ro;
   int r;
   int ld;
-  int pad;
+  int t;
 };
 static_assert(sizeof(PairRow) == ENTRY_BYTES, "entry");
 
-struct Cursor {
-  int tile, item, k0;
-};
-
-template <class Src>
-__device__ __forceinline__ void cursor_skip(const Src& src, Cursor& cu) {
-  while (cu.tile < src.ntiles()) {
-    const int ni = src.nitems(cu.tile);
-    while (cu.item < ni && src.klen(cu.tile, cu.item) <= 0) ++cu.item;
-    if (cu.item < ni) return;
-    ++cu.tile;
-    cu.item = 0;
-  }
-}
-
-template <class Src>
-__device__ __forceinline__ void cursor_next(const Src& src, Cursor& cu) {
-  cu.k0 += KC;
-  if (cu.k0 < src.klen(cu.tile, cu.item)) return;
-  cu.k0 = 0;
-  ++cu.item;
-  cursor_skip(src, cu);
-}
-
 // Streams the chunks of src through the tensor cores, called by all THREADS
-// threads of the block.  Every worker thread calls src.finish(tile, sum, comp,
-// cross) once a tile's products are summed (the tile's value is
-// (sum - comp) + cross); returns the number of chunks (0 for every thread
-// when src is empty).  Warps synchronise only through mbarriers:
-//   bar[0..1]  ready: chunk of that parity split and copied (one arrival per
-//              worker warp)
-//   bar[2..3]  operands of chunk parity no longer read (one commit per issuer)
-//   bar[4..5]  accumulator set complete (one commit per issuer)
+// threads of the block.  src: ntile tiles of cpt chunks; src.produce(c, a,
+// bar, lane), called by the 32 lanes of the producer warp, issues the A
+// copies of chunk c into a; src.load_b(c, slot, m) issues
+// this worker's B copy of chunk c (both called for c = 0, 1, ... in order);
+// every worker calls src.finish(tile, sum, comp, cross) once a tile's
+// products are summed (the tile's value is (sum - comp) + cross).  Returns the
+// number of chunks.
 template <class Src>
-__device__ int run_stream(const Src& src, unsigned char* smem, uint64_t* bar, uint32_t tmem,
-                          int64_t lo_off, int* err) {
+__device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t tmem, int* err) {
   const int tid = threadIdx.x;
-  Cursor lc{0, 0, 0};
-  cursor_skip(src, lc);
-  if (lc.tile >= src.ntiles()) return 0;
+  const int cpt = src.cpt, nch = src.ntile * src.cpt;
+  if (nch <= 0) return 0;
 
-  if (tid >= WORKERS) {
-    // issuer warps (lane 0): warp 8 A_hi [B_hi | B_lo] -> D, warp 9 A_lo B_hi
-    // -> D2; each follows the chunk sequence with its own cursor
-    if ((tid & 31) != 0) return 1;
-    const bool second = tid >= WORKERS + 32;
-    int c = 0, g = 0, gk = 0;
-    for (;;) {
-      Cursor nx = lc;
-      cursor_next(src, nx);
-      const bool stream_end = nx.tile >= src.ntiles();
-      const bool close = nx.tile != lc.tile || gk == kGroupChunks - 1;
+  if (tid >= PRODUCER) {
+    // producer warp: lane 0 waits for the slot; the lanes issue the copies
+    const int lane = tid & 31;
+    for (int c = 0; c < nch; ++c) {
+      const int s = c % kSlots;
+      if (lane == 0 && c >= kSlots &&
+          !tc::mbar_wait(&bar[BAR_EMPTY + s], (uint32_t)(((c / kSlots) - 1) & 1), kWaitLimit))
+        atomicExch(err, 1);
+      __syncwarp();
+      src.produce(c, smem + s * SLOT_BYTES, &bar[BAR_FULL + s], lane);
+    }
+    return nch;
+  }
+
+  if (tid >= ISSUER0) {
+    // issuer warps (lane 0): warp 8 A_hi [B_hi | B_lo] -> D, warp 9 A_lo B_hi -> D2
+    if ((tid & 31) != 0) return nch;
+    const bool second = tid >= ISSUER0 + 32;
+    int g = 0, gk = 0, ct = 0;
+    for (int c = 0; c < nch; ++c) {
+      const bool close = ct == cpt - 1 || gk == kGroupChunks - 1;
       const int buf = g & 1;
-      if (!tc::mbar_wait(&bar[c & 1], (uint32_t)((c >> 1) & 1), kWaitLimit)) atomicExch(err, 1);
+      if (!tc::mbar_wait(&bar[BAR_READY + (c & 1)], (uint32_t)((c >> 1) & 1), kWaitLimit))
+        atomicExch(err, 1);
       tc::fence_after_sync();
       const uint32_t ab = tmem + TM_A + 64u * (uint32_t)(c & 1) + (second ? 32u : 0u);
       const uint32_t d = tmem + 128u * (uint32_t)buf + (second ? 64u : 0u);
@@ -197,30 +209,27 @@ __device__ int run_stream(const Src& src, unsigned char* smem, uint64_t* bar, ui
       for (int ks = 0; ks < KC / 8; ++ks)
         tc::mma_tf32_ta(d, ab + 8u * ks, bd + (uint64_t)((ks * 256) >> 4), second ? IDESC32 : IDESC64,
                         (gk > 0 || ks > 0) ? 1u : 0u);
-      tc::mma_commit(&bar[2 + (c & 1)]);
+      tc::mma_commit(&bar[BAR_MPAR + (c & 1)]);
+      tc::mma_commit(&bar[BAR_EMPTY + c % kSlots]);
       if (close) {
-        tc::mma_commit(&bar[4 + buf]);
+        tc::mma_commit(&bar[BAR_ACC + buf]);
         ++g;
         gk = 0;
       } else {
         ++gk;
       }
-      if (stream_end) return c + 1;
-      lc = nx;
-      ++c;
+      ct = ct == cpt - 1 ? 0 : ct + 1;
     }
+    return nch;
   }
 
-  // worker threads.  Warp w owns rows 32 (w % 4) .. + 31 (its TMEM lanes)
-  // and K quads 4 half .. 4 half + 3 of every chunk, half = w / 4: it copies
-  // them (lane: k quad qa of rows rb + 8 i, i = 0..3) and splits them (lane:
-  // row R), so a __syncwarp orders the two.  B: k quad qb of column cb.
+  // workers.  Warp w owns rows 32 (w % 4) .. + 31 (its TMEM lanes) and K
+  // quads 4 half .. 4 half + 3 of every chunk, half = w / 4.
   const int w = tid >> 5, lane = tid & 31, half = w >> 2;
-  const int qa = 4 * half + (lane & 3);
-  const int rb = 32 * (w & 3) + (lane >> 2);
-  const uint32_t offA = (uint32_t)rb * 128u + ((uint32_t)(qa ^ (rb & 7)) << 4);  // row rb + 8 i: + 1024 i
-  const int cb = 8 * (tid >> 6) + ((tid >> 2) & 7), qb = 4 * ((tid >> 5) & 1) + (tid & 3);
-  const uint32_t offB = A_BYTES + tc::kmajor_off(cb, 4 * qb, KC);
+  CopyMap m;
+  m.cb = 8 * (tid >> 6) + ((tid >> 2) & 7);
+  m.qb = 4 * ((tid >> 5) & 1) + (tid & 3);
+  m.offB = A_BYTES + tc::kmajor_off(m.cb, 4 * m.qb, KC);
   const int R = tid & 127;
   const uint32_t lane_base = ((uint32_t)((tid >> 5) & 3) * 32u) << 16;
 
@@ -228,44 +237,19 @@ __device__ int run_stream(const Src& src, unsigned char* smem, uint64_t* bar, ui
 #pragma unroll
   for (int j = 0; j < 16; ++j) sum[j] = comp[j] = cross[j] = 0.f;
 
-  View lv{};
-  int lv_tile = -1, lv_item = -1;
-  int nload = 0, c = 0;
-  int last = 0x7fffffff;  // index of the last chunk, once the loader has reached it
-  uint32_t ends = 0;      // bit i: chunk c + i is the last of its tile
-  auto load = [&]() {
-    if (lc.tile != lv_tile || lc.item != lv_item) {
-      src.view(lc.tile, lc.item, rb, lv);
-      lv_tile = lc.tile;
-      lv_item = lc.item;
-    }
-    unsigned char* sa = smem + (nload % kSlots) * SLOT_BYTES;
-    const int k = lc.k0 + 4 * qa;
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const bool ok = lv.arow[i] != nullptr && k < lv.alen;
-      cp_async16(sa + offA + 1024 * i, ok ? lv.arow[i] + k : lv.b, ok);
-    }
-    const int kb = lc.k0 + 4 * qb;
-    const bool ok = kb < lv.blen;
-    const float* bsrc = ok ? lv.b + cb * lv.bs + kb : lv.b;
-    cp_async16(sa + offB, bsrc, ok);
-    cp_async16(sa + offB + B_BYTES, bsrc + lo_off, ok);
-    const int t = lc.tile;
-    cursor_next(src, lc);
-    if (lc.tile != t) ends |= 1u << (nload - c);
-    if (lc.tile >= src.ntiles()) last = nload;
-    ++nload;
-  };
-
+  int nload = 0;
   for (int i = 0; i < kAhead; ++i) {
-    if (nload <= last) load();
+    if (nload < nch) {
+      src.load_b(nload, smem + (nload % kSlots) * SLOT_BYTES, m);
+      ++nload;
+    }
     cp_async_commit();
   }
 
   auto read = [&](int g) {
     const uint32_t base = tmem + 128u * (uint32_t)(g & 1) + 16u * half + lane_base;
-    if (!tc::mbar_wait(&bar[4 + (g & 1)], (uint32_t)((g >> 1) & 1), kWaitLimit)) atomicExch(err, 1);
+    if (!tc::mbar_wait(&bar[BAR_ACC + (g & 1)], (uint32_t)((g >> 1) & 1), kWaitLimit))
+      atomicExch(err, 1);
     tc::fence_after_sync();
     float hh[16], x1[16], x2[16];
     tc::tmem_ld16(base, hh);
@@ -279,21 +263,28 @@ __device__ int run_stream(const Src& src, unsigned char* smem, uint64_t* bar, ui
     }
   };
 
-  int g = 0, gk = 0, tile = 0, pend_tile = 0;
+  int g = 0, gk = 0, ct = 0, tile = 0, pend_tile = 0;
   bool pend = false;
-  for (;;) {
-    // the operands of chunk c - 2 (the copy slot refilled below and the
-    // tensor-memory A of this chunk's parity) are no longer read
-    if (c >= 2 && !tc::mbar_wait(&bar[2 + (c & 1)], (uint32_t)(((c - 2) >> 1) & 1), kWaitLimit))
+  for (int c = 0; c < nch; ++c) {
+    const int s = c % kSlots;
+    // chunk c - 2 multiplied: its slot (refilled with B below) and the
+    // tensor-memory A of this chunk's parity are free
+    if (c >= 2 &&
+        !tc::mbar_wait(&bar[BAR_MPAR + (c & 1)], (uint32_t)(((c - 2) >> 1) & 1), kWaitLimit))
       atomicExch(err, 1);
-    if (nload <= last) load();
+    if (nload < nch) {
+      src.load_b(nload, smem + (nload % kSlots) * SLOT_BYTES, m);
+      ++nload;
+    }
     cp_async_commit();
     cp_async_wait<kAhead>();
-    __syncwarp();  // the warp's copies of this chunk (the other half of each row) have landed
+    if (!tc::mbar_wait(&bar[BAR_FULL + s], (uint32_t)((c / kSlots) & 1), kWaitLimit))
+      atomicExch(err, 1);
 
-    // split the row this thread owns and store it to tensor memory
+    unsigned char* slot = smem + s * SLOT_BYTES;
     {
-      const unsigned char* sa = smem + (c % kSlots) * SLOT_BYTES + (uint32_t)R * 128u;
+      // the row this thread owns, from the 128-byte swizzled A tile
+      const unsigned char* sa = slot + (uint32_t)R * 128u;
       float hi[16], lo[16];
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
@@ -311,15 +302,23 @@ __device__ int run_stream(const Src& src, unsigned char* smem, uint64_t* bar, ui
       const uint32_t ta = tmem + TM_A + 64u * (uint32_t)(c & 1) + 16u * half + lane_base;
       tc::tmem_st16(ta, hi);
       tc::tmem_st16(ta + 32u, lo);
+      // the B segment this thread copied: low part next to it
+      unsigned char* sb = slot + m.offB;
+      const float4 xb = *reinterpret_cast<const float4*>(sb);
+      float4 lb;
+      lb.x = xb.x - tf32_rz(xb.x);
+      lb.y = xb.y - tf32_rz(xb.y);
+      lb.z = xb.z - tf32_rz(xb.z);
+      lb.w = xb.w - tf32_rz(xb.w);
+      *reinterpret_cast<float4*>(sb + B_BYTES) = lb;
       tc::tmem_wait_st();
     }
-    // B (copied by this warp's cp.async) to the tensor core's proxy; A stored
+    // B (cp.async copies and low parts) to the tensor core's proxy; A stored
     tc::fence_async_smem();
     tc::fence_before_sync();
     __syncwarp();
-    if (lane == 0) tc::mbar_arrive(&bar[c & 1]);
-    const bool tile_end = ends & 1u;
-    ends >>= 1;
+    if (lane == 0) tc::mbar_arrive(&bar[BAR_READY + (c & 1)]);
+    const bool tile_end = ct == cpt - 1;
     const bool close = tile_end || gk == kGroupChunks - 1;
     if (close) {
       if (pend) {
@@ -337,22 +336,38 @@ __device__ int run_stream(const Src& src, unsigned char* smem, uint64_t* bar, ui
     } else {
       ++gk;
     }
-    if (tile_end) ++tile;
-    if (c == last) break;
-    ++c;
+    if (tile_end) {
+      ++tile;
+      ct = 0;
+    } else {
+      ++ct;
+    }
   }
   read(g - 1);
   src.finish(pend_tile, sum, comp, cross);
   cp_async_wait<0>();
-  return c + 1;
+  return nch;
+}
+
+// 128-byte swizzled tensor copies need 1024-byte aligned destinations
+__device__ __forceinline__ bool smem_misaligned(const unsigned char* smem, int* err) {
+  if ((tc::smem_addr(smem) & 1023u) == 0) return false;
+  if (threadIdx.x == 0) atomicExch(err, 3);
+  return true;
 }
 
 __device__ __forceinline__ uint32_t block_setup(uint64_t* bar, uint32_t* tslot) {
   if (threadIdx.x < 32) tc::tmem_alloc(tslot, kTmemCols);
   if (threadIdx.x == 0) {
-    tc::mbar_init(&bar[0], WORKERS / 32);
-    tc::mbar_init(&bar[1], WORKERS / 32);
-    for (int i = 2; i < 6; ++i) tc::mbar_init(&bar[i], 2);
+    for (int i = 0; i < kSlots; ++i) {
+      tc::mbar_init(&bar[BAR_FULL + i], 1);
+      tc::mbar_init(&bar[BAR_EMPTY + i], 2);
+    }
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&bar[BAR_READY + i], WORKERS / 32);
+      tc::mbar_init(&bar[BAR_MPAR + i], 2);
+      tc::mbar_init(&bar[BAR_ACC + i], 2);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   tc::fence_before_sync();
@@ -367,114 +382,123 @@ __device__ __forceinline__ void block_teardown(uint32_t tmem) {
   if (threadIdx.x < 32) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
-// Exclusive prefix sum of the ranks tab[0..n).r into s_cum[0..n] by warp 0.
-__device__ __forceinline__ void warp0_scan(const PairRow* tab, int n, int* s_cum) {
+// Exclusive prefix sum of f(i), i < n, into out[0..n] by warp 0.
+template <class F>
+__device__ __forceinline__ void warp0_scan(int n, F f, int* out) {
   if (threadIdx.x < 32) {
     const int lane = threadIdx.x;
     int carry = 0;
     for (int base = 0; base < n; base += 32) {
-      const int v = base + lane < n ? tab[base + lane].r : 0;
+      const int v = base + lane < n ? f(base + lane) : 0;
       int incl = v;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
         const int t = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += t;
       }
-      if (base + lane < n) s_cum[base + lane] = carry + incl - v;
+      if (base + lane < n) out[base + lane] = carry + incl - v;
       carry += __shfl_sync(0xffffffffu, incl, 31);
     }
-    if (lane == 0) s_cum[n] = carry;
+    if (lane == 0) out[n] = carry;
   }
+}
+
+// index i with cum[i] <= v < cum[i + 1] (cum nondecreasing, cum[0] <= v < cum[n])
+__device__ __forceinline__ int upper_index(const int* cum, int n, int v) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (cum[mid] <= v) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
 }
 
 // ---------------------------------------------------------------------------
 // Phase A: T = [V_p^T] X over one input box.  SLICE: the pairs of levels
 // 1..d-1 over a level d-1 box; otherwise the leaf-level pairs over a leaf.
+// Pair p occupies ceil(r_p / 8) groups of 8 rows; a tile is 16 groups.
 struct SrcTa {
   const PairRow* tab;
-  const int* cum;
-  int n;
-  int rows;
-  int tile0, tstep, ntile;
+  const int* cumg;   // groups before each entry
+  int n, ngroups;
+  int tile0, tstep, ntile, cpt;
   int kin;
   const float* b;
   int64_t bs;
-  int64_t lo_off;
+  // producer state (per lane): the group of the current tile this lane copies
+  int pk = 0, pc = 0, png = 0;
+  const CUtensorMap* gmap = nullptr;
+  int gx = 0, gy = 0;
+  // worker state
+  int wk = 0;
 
-  __device__ int ntiles() const { return ntile; }
-  __device__ int nitems(int) const { return 1; }
-  __device__ int klen(int, int) const { return kin; }
-  __device__ bool locate(int t, int row, int& idx, int& l) const {
-    const int rho = (tile0 + t * tstep) * 128 + row;
-    if (rho >= rows) return false;
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (cum[mid] <= rho) lo = mid;
-      else hi = mid - 1;
-    }
-    idx = lo;
-    l = rho - cum[lo];
-    return true;
-  }
-  __device__ void view(int t, int, int rb, View& v) const {
-    int idx = 0, l = 0;
-    const bool in0 = locate(t, rb, idx, l);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      v.arow[i] = nullptr;
-      if (in0) {
-        const int rho = (tile0 + t * tstep) * 128 + rb + 8 * i;
-        if (rho < rows) {
-          while (cum[idx + 1] <= rho) ++idx;
-          v.arow[i] = tab[idx].a + (int64_t)(rho - cum[idx]) * tab[idx].lda;
-        }
+  __device__ void produce(int, unsigned char* a, uint64_t* full, int lane) {
+    if (pk == 0) {  // a new tile: lane i looks up its group
+      const int g0 = (tile0 + pc * tstep) * 16;
+      png = min(16, ngroups - g0);
+      if (lane < png) {
+        const int idx = upper_index(cumg, n, g0 + lane);
+        gmap = tab[idx].map;
+        gx = tab[idx].ro;
+        gy = (g0 + lane - cumg[idx]) * 8;
       }
     }
-    v.alen = kin;
-    v.b = b;
-    v.bs = bs;
-    v.blen = kin;
+    if (lane == 0) expect_tx(full, 1024u * (uint32_t)png);
+    __syncwarp();
+    if (lane < png) tma_load_2d(a + 1024 * lane, gmap, gx + pk, gy, full);
+    pk += KC;
+    if (pk >= cpt * KC) {
+      pk = 0;
+      ++pc;
+    }
+  }
+  __device__ void load_b(int, unsigned char* slot, const CopyMap& m) {
+    const int kb = wk + 4 * m.qb;
+    const bool ok = kb < kin;
+    cp_async16(slot + m.offB, ok ? b + m.cb * bs + kb : b, ok);
+    wk += KC;
+    if (wk >= cpt * KC) wk = 0;
   }
   __device__ void finish(int t, const float* sum, const float* comp, const float* cross) const {
-    int idx, l;
-    if (!locate(t, threadIdx.x & 127, idx, l)) return;
+    const int R = threadIdx.x & 127;
+    const int gi = (tile0 + t * tstep) * 16 + (R >> 3);
+    if (gi >= ngroups) return;
+    const int idx = upper_index(cumg, n, gi);
     const PairRow& e = tab[idx];
+    const int l = (gi - cumg[idx]) * 8 + (R & 7);
+    if (l >= e.r) return;
     const int c0 = (threadIdx.x >> 7) * 16;
-    if (!e.pad) {  // slice partial
+    if (!e.t) {  // slice partial
 #pragma unroll
       for (int j = 0; j < 16; ++j) e.dst[(int64_t)(c0 + j) * e.ld + l] = (sum[j] - comp[j]) + cross[j];
       return;
     }
-    // T as TF32 high and low parts, zero padded to ld
+    // T in the split-exact form, zero padded to ld
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
       const float v = (sum[j] - comp[j]) + cross[j];
-      const float hi = tf32_rn(v);
-      float* o = e.dst + (int64_t)(c0 + j) * e.ld + l;
-      o[0] = hi;
-      o[lo_off] = tf32_rn(v - hi);
+      const float hi = tf32_rz(v);
+      e.dst[(int64_t)(c0 + j) * e.ld + l] = hi + tf32_rn(v - hi);
     }
     if (l == e.r - 1)
       for (int lp = e.r; lp < e.ld; ++lp)
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          float* o = e.dst + (int64_t)(c0 + j) * e.ld + lp;
-          o[0] = 0.f;
-          o[lo_off] = 0.f;
-        }
+        for (int j = 0; j < 16; ++j) e.dst[(int64_t)(c0 + j) * e.ld + lp] = 0.f;
   }
 };
 
 template <bool SLICE>
-__global__ void __launch_bounds__(THREADS, 1) k_ta_tc(FarOp op, const float* __restrict__ Xt, int64_t N,
+__global__ void __launch_bounds__(THREADS, 1) k_ta_tc(FarOp op, const CUtensorMap* __restrict__ vmaps,
+                                                      const float* __restrict__ Xt, int64_t N,
                                                       float* __restrict__ T, float* __restrict__ Pp,
-                                                      int64_t lo_off, int* __restrict__ err) {
+                                                      int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ uint64_t bar[6];
+  __shared__ uint64_t bar[NBAR];
   __shared__ uint32_t tslot;
   PairRow* tab = reinterpret_cast<PairRow*>(smem + TAB_OFF);
-  int* cum = reinterpret_cast<int*>(smem + TAB_OFF + kMaxEntries * ENTRY_BYTES);
+  int* cumg = reinterpret_cast<int*>(smem + TAB_OFF + kMaxEntries * ENTRY_BYTES);
+  if (smem_misaligned(smem, err)) return;
   const int d = op.levels;
   const int64_t box = blockIdx.x;
   const int sh_in = SLICE ? 3 : 0;
@@ -505,49 +529,49 @@ __global__ void __launch_bounds__(THREADS, 1) k_ta_tc(FarOp op, const float* __r
     const int up = SLICE ? 3 * (d - 1 - j) : 0;
     const int64_t a = box >> up;
     const int64_t a0 = op.leaf_off[a << (3 * (d - j))];
-    const int64_t lda = op.leaf_off[(a + 1) << (3 * (d - j))] - a0;
     const int r = op.rank[p];
     PairRow e;
-    e.a = static_cast<const float*>(op.vfac[p]) + (i0 - a0);
-    e.lda = (int)((lda + 3) & ~int64_t(3));
+    e.map = vmaps + p;
+    e.ro = (int)(i0 - a0);
     e.r = r;
-    e.pad = 0;
     if (!SLICE || j == d - 1) {
-      e.pad = 1;
+      e.t = 1;
       e.ld = (r + 3) & ~3;
       e.dst = T + op.tr_off4[p] * NR;
     } else {
+      e.t = 0;
       e.ld = r;
       e.dst = Pp + (op.part_off[p] + (box - (a << up)) * (int64_t)r) * NR;
     }
     tab[idx] = e;
   }
   __syncthreads();
-  warp0_scan(tab, n, cum);
+  warp0_scan(n, [&](int i) { return (tab[i].r + 7) >> 3; }, cumg);
   __syncthreads();
-  const int rows = cum[n];
-  const int ntiles_all = (rows + 127) / 128;
+  const int ngroups = cumg[n];
+  const int ntiles_all = (ngroups + 15) / 16;
   if ((int)blockIdx.y >= ntiles_all) return;
   const uint32_t tmem = block_setup(bar, &tslot);
   SrcTa src;
   src.tab = tab;
-  src.cum = cum;
+  src.cumg = cumg;
   src.n = n;
-  src.rows = rows;
+  src.ngroups = ngroups;
   src.tile0 = blockIdx.y;
   src.tstep = gridDim.y;
   src.ntile = (ntiles_all - (int)blockIdx.y + (int)gridDim.y - 1) / (int)gridDim.y;
   src.kin = kin;
+  src.cpt = (kin + KC - 1) / KC;
   src.b = Xt + i0;
   src.bs = N;
-  src.lo_off = lo_off;
-  run_stream(src, smem, bar, tmem, lo_off, err);
+  run_stream(src, smem, bar, tmem, err);
   block_teardown(tmem);
 }
 
-// FP64 sum of slice partials into the padded T: T_p[c][l] = sum_s P_p[s][c][l]
+// FP64 sum of slice partials into the padded T (split-exact form):
+// T_p[c][l] = sum_s P_p[s][c][l]
 __global__ void k_tred_tc(FarOp op, const int32_t* __restrict__ pairs, const float* __restrict__ Pp,
-                          float* __restrict__ T, int64_t lo_off) {
+                          float* __restrict__ T) {
   const int p = pairs[blockIdx.x];
   const int r = op.rank[p], rp = (r + 3) & ~3;
   const int64_t ns = int64_t(1) << (3 * (op.levels - 1 - op.pair_level[p]));
@@ -558,42 +582,71 @@ __global__ void k_tred_tc(FarOp op, const int32_t* __restrict__ pairs, const flo
     double acc = 0.0;
     if (l < r)
       for (int64_t s = 0; s < ns; ++s) acc += (double)src[s * r * NR + c * r + l];
-    const float hi = tf32_rn((float)acc);
-    dst[o] = hi;
-    dst[o + lo_off] = tf32_rn((float)(acc - (double)hi));
+    dst[o] = tf32_split_value(acc);
   }
 }
 
-// Items of one output tile (phase B).
+// Items of one output tile (phase B): item i takes chunks [cofs[i], cofs[i + 1]).
 struct SrcItems {
   const Item* items;
+  const int* cofs;
   int n;
   int nrows;
-  __device__ int ntiles() const { return 1; }
-  __device__ int nitems(int) const { return n; }
-  __device__ int klen(int, int i) const { return items[i].blen; }
-  __device__ void view(int, int i, int rb, View& v) const {
-    const Item& it = items[i];
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-      v.arow[r] = rb + 8 * r < nrows ? it.a + (int64_t)(rb + 8 * r) * it.as : nullptr;
-    v.alen = it.alen;
-    v.b = it.b;
-    v.bs = it.bs;
-    v.blen = it.blen;
+  int ntile, cpt;
+  // producer cursor (lane 0): item, K offset, the item's map, row and K
+  int pi = -1, pk = 0, py = 0, plen = 0;
+  const CUtensorMap* pmap = nullptr;
+  // worker cursor: item, K offset, the item's B column base, stride and K
+  int wi = -1, wk = 0, wbs = 0, wlen = 0;
+  const float* wb = nullptr;
+
+  // next item with K after item i
+  __device__ int next_item(int i) const {
+    ++i;
+    while (cofs[i + 1] == cofs[i]) ++i;
+    return i;
+  }
+  __device__ void produce(int, unsigned char* a, uint64_t* full, int lane) {
+    if (lane != 0) return;
+    if (pk >= plen) {
+      pi = next_item(pi);
+      const Item& it = items[pi];
+      pmap = it.map;
+      py = it.y;
+      plen = it.blen;
+      pk = 0;
+    }
+    expect_tx(full, (uint32_t)A_BYTES);
+    tma_load_2d(a, pmap, pk, py, full);
+    pk += KC;
+  }
+  __device__ void load_b(int, unsigned char* slot, const CopyMap& m) {
+    if (wk >= wlen) {
+      wi = next_item(wi);
+      const Item& it = items[wi];
+      wb = it.b + (int64_t)m.cb * it.bs;
+      wbs = it.bs;
+      wlen = it.blen;
+      wk = 0;
+    }
+    const int kb = wk + 4 * m.qb;
+    const bool ok = kb < wlen;
+    cp_async16(slot + m.offB, ok ? wb + kb : wb, ok);
+    wk += KC;
   }
 };
 
-__device__ __forceinline__ Item pair_item(const FarOp& op, int p, int64_t row0, const float* T) {
+__device__ __forceinline__ Item pair_item(const FarOp& op, const CUtensorMap* umaps, int p, int y,
+                                          const float* T) {
   const int r = op.rank[p];
   const int rp = (r + 3) & ~3;
   Item it;
-  it.a = static_cast<const float*>(op.ufac[p]) + row0 * rp;
-  it.as = rp;
-  it.alen = rp;
+  it.map = umaps + p;
+  it.y = y;
   it.b = T + op.tr_off4[p] * NR;
   it.bs = rp;
-  it.blen = rp;
+  it.blen = r > 0 ? rp : 0;
+  it.pad = 0;
   return it;
 }
 
@@ -611,13 +664,15 @@ struct SrcUt : SrcItems {
 };
 
 // Phase B over the levels above the leaves: one block per (slice, 128 rows).
-__global__ void __launch_bounds__(THREADS, 1) k_ut_tc(FarOp op, const float* __restrict__ T,
-                                                      int64_t N, double* __restrict__ Ynl,
-                                                      int64_t lo_off, int* __restrict__ err) {
+__global__ void __launch_bounds__(THREADS, 1) k_ut_tc(FarOp op, const CUtensorMap* __restrict__ umaps,
+                                                      const float* __restrict__ T, int64_t N,
+                                                      double* __restrict__ Ynl, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ uint64_t bar[6];
+  __shared__ uint64_t bar[NBAR];
   __shared__ uint32_t tslot;
   Item* items = reinterpret_cast<Item*>(smem + TAB_OFF);
+  int* cofs = reinterpret_cast<int*>(smem + TAB_OFF + kMaxEntries * ENTRY_BYTES);
+  if (smem_misaligned(smem, err)) return;
   const int d = op.levels;
   const int64_t sb = blockIdx.x;
   const int64_t s0 = op.leaf_off[sb << 3], s1 = op.leaf_off[(sb + 1) << 3];
@@ -644,18 +699,22 @@ __global__ void __launch_bounds__(THREADS, 1) k_ut_tc(FarOp op, const float* __r
     }
     const int64_t a = sb >> (3 * (d - 1 - j));
     const int64_t a0 = op.leaf_off[a << (3 * (d - j))];
-    items[idx] = pair_item(op, (int)(op.il_ptr[gb] + (idx - base)), r0 - a0, T);
+    items[idx] = pair_item(op, umaps, (int)(op.il_ptr[gb] + (idx - base)), (int)(r0 - a0), T);
   }
   __syncthreads();
+  warp0_scan(n, [&](int i) { return (items[i].blen + KC - 1) / KC; }, cofs);
   const uint32_t tmem = block_setup(bar, &tslot);
   SrcUt src;
   src.items = items;
+  src.cofs = cofs;
   src.n = n;
   src.nrows = nrows;
+  src.ntile = 1;
+  src.cpt = cofs[n];
   src.ynl = Ynl;
   src.N = N;
   src.r0 = r0;
-  if (run_stream(src, smem, bar, tmem, lo_off, err) == 0 && threadIdx.x < WORKERS) {
+  if (run_stream(src, smem, bar, tmem, err) == 0 && threadIdx.x < WORKERS) {
     float z[16] = {};
     src.finish(0, z, z, z);
   }
@@ -686,18 +745,21 @@ struct SrcLeaf : SrcItems {
 
 // Phase B at the leaf level plus the near field: one block per output leaf
 // of at most 128 points.
-__global__ void __launch_bounds__(THREADS, 1) k_leaf_tc(FarOp op, NearOp nr, const float* __restrict__ T,
+__global__ void __launch_bounds__(THREADS, 1) k_leaf_tc(FarOp op, NearOp nr,
+                                                        const CUtensorMap* __restrict__ umaps,
+                                                        const CUtensorMap* __restrict__ nmaps,
+                                                        const float* __restrict__ T,
                                                         const float* __restrict__ Xt, int64_t N,
-                                                        const float* __restrict__ Knear,
-                                                        const int64_t* __restrict__ near_off,
                                                         const double* __restrict__ Ynl,
                                                         const int32_t* __restrict__ perm, int nrhs,
                                                         double* __restrict__ Y, int64_t ldy,
-                                                        int64_t lo_off, int* __restrict__ err) {
+                                                        int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ uint64_t bar[6];
+  __shared__ uint64_t bar[NBAR];
   __shared__ uint32_t tslot;
   Item* items = reinterpret_cast<Item*>(smem + TAB_OFF);
+  int* cofs = reinterpret_cast<int*>(smem + TAB_OFF + kMaxEntries * ENTRY_BYTES);
+  if (smem_misaligned(smem, err)) return;
   const int d = op.levels;
   const int64_t k = blockIdx.x;
   const int64_t t0 = op.leaf_off[k];
@@ -714,33 +776,33 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_tc(FarOp op, NearOp nr, con
   for (int i = threadIdx.x; i < n; i += THREADS) {
     Item it;
     if (i < npair) {
-      it = pair_item(op, (int)(q0 + i), 0, T);
+      it = pair_item(op, umaps, (int)(q0 + i), 0, T);
     } else {
       const int sl = i - npair;  // neighbour slots 0..25, then the leaf itself
       const int64_t nn = sl < 26 ? (int64_t)nr.nbr_leaf[k * 26 + sl] : k;
-      const int64_t off = near_off[k * 27 + sl];
-      it.a = Knear;
+      it.map = nmaps + k * 27 + sl;
       it.b = Xt;
-      it.as = it.bs = it.alen = it.blen = 0;
-      if (nn >= 0 && off >= 0) {
+      it.y = 0;
+      it.bs = it.blen = it.pad = 0;
+      if (nn >= 0) {
         const int64_t e0 = op.leaf_off[nn];
-        const int ne = (int)(op.leaf_off[nn + 1] - e0);
-        it.a = Knear + off;
-        it.as = (ne + 3) & ~3;
-        it.alen = it.as;
         it.b = Xt + e0;
         it.bs = (int)N;
-        it.blen = ne;
+        it.blen = (int)(op.leaf_off[nn + 1] - e0);
       }
     }
     items[i] = it;
   }
   __syncthreads();
+  warp0_scan(n, [&](int i) { return (items[i].blen + KC - 1) / KC; }, cofs);
   const uint32_t tmem = block_setup(bar, &tslot);
   SrcLeaf src;
   src.items = items;
+  src.cofs = cofs;
   src.n = n;
   src.nrows = nk;
+  src.ntile = 1;
+  src.cpt = cofs[n];
   src.ynl = Ynl;
   src.perm = perm;
   src.y = Y;
@@ -749,24 +811,21 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_tc(FarOp op, NearOp nr, con
   src.t0 = t0;
   src.nrhs = nrhs;
   src.d = d;
-  if (run_stream(src, smem, bar, tmem, lo_off, err) == 0 && threadIdx.x < WORKERS) {
+  if (run_stream(src, smem, bar, tmem, err) == 0 && threadIdx.x < WORKERS) {
     float z[16] = {};
     src.finish(0, z, z, z);
   }
   block_teardown(tmem);
 }
 
-// X (original order, column-major) -> Xt[c * N + t] in tree order, FP32
+// X (original order, column-major) -> Xt[c * N + t] in tree order, split-exact FP32
 __global__ void k_gather_xt(int64_t N, int nrhs, const double* __restrict__ X, int64_t ldx,
-                            const int32_t* __restrict__ perm, float* __restrict__ Xt, int64_t lo_off) {
+                            const int32_t* __restrict__ perm, float* __restrict__ Xt) {
   const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (o >= N * NR) return;
   const int c = (int)(o / N);
   const int64_t t = o - (int64_t)c * N;
-  const double x = c < nrhs ? X[c * ldx + perm[t]] : 0.0;
-  const float hi = tf32_rn((float)x);
-  Xt[o] = hi;
-  Xt[o + lo_off] = tf32_rn((float)(x - (double)hi));
+  Xt[o] = c < nrhs ? tf32_split_value(X[c * ldx + perm[t]]) : 0.f;
 }
 
 // Near-field blocks of every leaf: for neighbour slot s (0..25, 26 = the leaf
@@ -820,10 +879,12 @@ int launch_matvec_tc(cudaStream_t s, int64_t N, const int32_t* perm, const FarOp
     cudaFuncSetAttribute(k_leaf_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     attr = true;
   }
+  const CUtensorMap* umaps = static_cast<const CUtensorMap*>(B.umaps);
+  const CUtensorMap* vmaps = static_cast<const CUtensorMap*>(B.vmaps);
+  const CUtensorMap* nmaps = static_cast<const CUtensorMap*>(B.nmaps);
   int launches = 0;
   if (prof) prof->begin(s);
-  k_gather_xt<<<(unsigned)((N * NR + 255) / 256), 256, 0, s>>>(N, nrhs, X, ldx, perm, B.xt,
-                                                               B.lo_off);
+  k_gather_xt<<<(unsigned)((N * NR + 255) / 256), 256, 0, s>>>(N, nrhs, X, ldx, perm, B.xt);
   ++launches;
   if (prof) prof->mark(s, "gather");
   const int d = far.levels;
@@ -832,30 +893,29 @@ int launch_matvec_tc(cudaStream_t s, int64_t N, const int32_t* perm, const FarOp
     // several blocks share a slice's row tiles when slices are few
     const int split = (int)std::max<int64_t>(1, std::min<int64_t>(32, (16 * 152) / nslice));
     k_ta_tc<true><<<dim3((unsigned)nslice, (unsigned)split), THREADS, SMEM_BYTES, s>>>(
-        far, B.xt, N, B.t, B.p, B.lo_off, B.err);
+        far, vmaps, B.xt, N, B.t, B.p, B.err);
     ++launches;
     if (prof) prof->mark(s, "ta_slice");
     if (B.n_upper > 0) {
-      k_tred_tc<<<(unsigned)B.n_upper, 128, 0, s>>>(far, B.upper_pairs, B.p, B.t, B.lo_off);
+      k_tred_tc<<<(unsigned)B.n_upper, 128, 0, s>>>(far, B.upper_pairs, B.p, B.t);
       ++launches;
       if (prof) prof->mark(s, "tred");
     }
   }
-  k_ta_tc<false><<<dim3((unsigned)far.nleaf, 1), THREADS, SMEM_BYTES, s>>>(far, B.xt, N, B.t, B.p,
-                                                                           B.lo_off, B.err);
+  k_ta_tc<false><<<dim3((unsigned)far.nleaf, 1), THREADS, SMEM_BYTES, s>>>(far, vmaps, B.xt, N, B.t,
+                                                                           B.p, B.err);
   ++launches;
   if (prof) prof->mark(s, "ta_leaf");
   if (d >= 2) {
     const int64_t nslice = int64_t(1) << (3 * (d - 1));
     const int tiles = (B.max_slice + 127) / 128;
     k_ut_tc<<<dim3((unsigned)nslice, (unsigned)std::max(1, tiles)), THREADS, SMEM_BYTES, s>>>(
-        far, B.t, N, B.ynl, B.lo_off, B.err);
+        far, umaps, B.t, N, B.ynl, B.err);
     ++launches;
     if (prof) prof->mark(s, "ut_tc");
   }
-  k_leaf_tc<<<(unsigned)far.nleaf, THREADS, SMEM_BYTES, s>>>(far, near, B.t, B.xt, N, B.knear,
-                                                             B.near_off, B.ynl, perm, nrhs, Y, ldy,
-                                                             B.lo_off, B.err);
+  k_leaf_tc<<<(unsigned)far.nleaf, THREADS, SMEM_BYTES, s>>>(far, near, umaps, nmaps, B.t, B.xt, N,
+                                                             B.ynl, perm, nrhs, Y, ldy, B.err);
   ++launches;
   if (prof) prof->mark(s, "leaf_tc");
   return launches;

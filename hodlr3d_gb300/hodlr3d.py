@@ -79,12 +79,29 @@ class HODLR3D:
         check(self._L.hodlr3d_assemble(self.handle))
         self.assembled = True
 
-    def MatVecProduct(self, b, precision="fp64") -> np.ndarray:
-        """Ab = A b for host arrays b of shape (N,) or (N, nrhs) (HODLR3D::MatVecProduct)."""
-        x, nrhs, shape = self._host_cols(b)
+    def MatVecProduct(self, b, precision="fp64", out=None) -> np.ndarray:
+        """Ab = A b for host arrays b of shape (N,) or (N, nrhs) (HODLR3D::MatVecProduct).
+
+        A C-ordered (N, nrhs) array goes to the GPU as it is (rows of
+        right-hand sides, reordered there); other layouts by columns.  out: an
+        optional float64 array of b's shape and layout to write the result to."""
+        a = np.asarray(b, dtype=np.float64)
+        if a.ndim not in (1, 2) or a.shape[0] != self.N:
+            raise ValueError(f"expected shape ({self.N},) or ({self.N}, nrhs), got {np.shape(b)}")
+        if a.ndim == 2 and a.shape[1] > 1 and a.flags.c_contiguous:
+            y = np.empty_like(a) if out is None else out
+            if y.shape != a.shape or y.dtype != np.float64 or not y.flags.c_contiguous:
+                raise ValueError("out must be a C-ordered float64 array of b's shape")
+            check(self._L.hodlr3d_matvec_host_rows(self.handle, a.ctypes.data, y.ctypes.data,
+                                                   a.shape[1], _prec(precision)))
+            return y
+        x, nrhs, shape = self._host_cols(a)
         y = np.empty_like(x)
         check(self._L.hodlr3d_matvec_host(self.handle, x.ctypes.data, y.ctypes.data, nrhs, self.N,
                                           _prec(precision)))
+        if out is not None:
+            out[...] = y.T.reshape(shape)
+            return out
         return y.T.reshape(shape)
 
     # ---- device API (torch tensors on this GPU) --------------------------

@@ -128,9 +128,15 @@ int hodlr3d_matvec(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld
  * the GPU race.  Device pointers, enqueued on `stream`. */
 int hodlr3d_matvec_noalloc(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
                            int precision, void* stream);
-/* Same with host pointers: copies in, multiplies, copies out, synchronises. */
+/* Same with host pointers (pageable or pinned): copies in, multiplies,
+ * copies out, synchronises. */
 int hodlr3d_matvec_host(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
                         int precision);
+/* Same for host arrays stored by rows: x and y are n x nrhs, element (i, c)
+ * at [i * nrhs + c] (the layout of a C-ordered (n, nrhs) array); the GPU
+ * reorders them.  No reference counterpart (the reference multiplies one
+ * vector at a time). */
+int hodlr3d_matvec_host_rows(hodlr3d_t h, const double* x, double* y, int nrhs, int precision);
 /* y = A^T x with the transposed operator (V (U^T x) on compressed pairs,
  * transposed near field).  No reference counterpart (the reference has no
  * transpose product); device pointers. */

@@ -102,6 +102,22 @@ def test_multi_rhs_columns_match_single(gcase):
         assert np.linalg.norm(Y[:, c] - y1) <= 1e-14 * np.linalg.norm(y1)
 
 
+def test_host_layouts_agree(gcase):
+    """Rows (C order, hodlr3d_matvec_host_rows) and columns (Fortran order,
+    hodlr3d_matvec_host) of the same right-hand sides give the same product,
+    with and without a caller-provided output array."""
+    from hodlr3d_gb300.workloads import charges_normal
+    g, H, _ = gcase
+    for prec in ("fp64", "mixed"):
+        Q = np.ascontiguousarray(charges_normal(H.N, nrhs=20, seed=4))
+        Yc = H.MatVecProduct(Q, precision=prec)
+        Yf = H.MatVecProduct(np.asfortranarray(Q), precision=prec)
+        out = np.empty_like(Q)
+        Yo = H.MatVecProduct(Q, precision=prec, out=out)
+        assert Yo is out
+        assert np.array_equal(Yc, Yf) and np.array_equal(Yc, out)
+
+
 def test_transpose_matches_oracle(gcase):
     import torch
     from oracle.oracle import Oracle
