@@ -16,17 +16,18 @@
 //             and its near-field blocks (K_near X_near), plus the slice sum;
 //             written once in the original order
 //
-// A block streams K = 32 chunks over its M = 128 output tiles.  A T tile (ta)
+// A block streams K = 64 chunks over its M = 128 output tiles.  A T tile (ta)
 // runs over one K range, its input box; the tile of ut / leaf runs over its
 // items (operand pairs: a factor A and its right-hand sides B, summed into
 // the tile) one after the other.  Three roles, synchronised by mbarriers only:
 //
 //   producer (one warp)    copies A global -> shared with the tensor memory
 //                          accelerator: 2D tiled loads from one tensor map per
-//                          factor (box 32 K x 128 rows, or 32 x 8 for the V of
-//                          the T kernels), 128-byte swizzle, zero fill outside
-//                          the factor; up to kSlots chunks ahead
-//   workers (8 warps)      copy B (X or T, 32 columns) with 16-byte cp.async
+//                          factor (boxes of 32 K x 128 rows, or 32 x 8 for the
+//                          V of the T kernels, two K halves per chunk),
+//                          128-byte swizzle, zero fill outside the factor; up
+//                          to kSlots chunks ahead
+//   workers (16 warps)     copy B (X or T, 32 columns) with 16-byte cp.async
 //                          into the canonical K-major layout; split A and B
 //                          into TF32 parts (below); read the accumulators back
 //   issuers (2 threads)    issue, per K = 8 step,
@@ -37,12 +38,14 @@
 //
 // The factors, X and T are held in the split-exact FP32 form (common.cuh): v =
 // hi + lo with hi = v with the 13 low mantissa bits cleared and lo = v - hi,
-// both exact TF32.  The worker owning a row (two per row, 16 K values each)
-// reads it from the swizzled tile, stores hi and lo to tensor memory; the
+// both exact TF32.  The workers owning a row (four per row, 16 K values each)
+// read it from the swizzled tile, store hi and lo to tensor memory; the
 // thread that copied a B segment writes its low part next to it (the tensor
 // core reads B_hi from the copy itself).  The lo*lo term, below 2^-22 of the
 // product, is left out.  Groups of kGroupChunks chunks alternate between two
-// accumulator sets; a group is read back while the next one is multiplied, its
+// accumulator sets (8 hi*hi MMAs per group, so that the truncating FP32
+// accumulation of the tensor core sees few additions); a group is read back
+// while the next one is multiplied, its
 // hi*hi part summed with compensated (Kahan) FP32 additions (whose error
 // matches an FP64 sum here at a fraction of the cost of GB300's FP64 units)
 // and its cross parts with plain FP32 additions.
@@ -60,16 +63,19 @@ namespace h3d {
 namespace {
 
 constexpr int NR = 32;                     // right-hand sides (MMA N)
-constexpr int KC = 32;                     // K per chunk
-constexpr int WORKERS = 256;               // copy B, split and read back: two threads per row
-constexpr int ISSUER0 = WORKERS;           // warps 8, 9: MMA issuers
-constexpr int PRODUCER = WORKERS + 64;     // warp 10: A copies
+constexpr int KC = 64;                     // K per chunk (two 32-wide boxes of A)
+constexpr int WORKERS = 512;               // copy B, split and read back: four threads per row
+constexpr int NCOL = 8;                    // accumulator columns (right-hand sides) per worker
+constexpr int ISSUER0 = WORKERS;           // warps 16, 17: MMA issuers
+constexpr int PRODUCER = WORKERS + 64;     // warp 18: A copies
 constexpr int THREADS = WORKERS + 96;
-constexpr int A_BYTES = 128 * KC * 4;      // A chunk (16 KB)
-constexpr int B_BYTES = NR * KC * 4;       // one TF32 part of a B chunk (4 KB)
+constexpr int A_HALF = 128 * 32 * 4;       // one 32-wide box of A (16 KB)
+constexpr int A_BYTES = 2 * A_HALF;        // A chunk (32 KB)
+constexpr int B_BYTES = NR * KC * 4;       // one TF32 part of a B chunk (8 KB)
 constexpr int SLOT_BYTES = A_BYTES + 2 * B_BYTES;  // slot: A, B hi, B lo
-constexpr int kSlots = 8;
-constexpr int kAhead = kSlots - 2;         // B chunks in flight ahead of the multiplied one
+constexpr int kSlots = 4;
+constexpr int kABuf = 2;                   // tensor-memory A buffers (chunks multiplied ahead)
+constexpr int kAhead = kSlots - kABuf;     // B chunks in flight ahead of the split one
 constexpr int TAB_OFF = kSlots * SLOT_BYTES;
 constexpr int kMaxEntries = 768;           // table entries (pairs, near blocks) of one block
 constexpr int ENTRY_BYTES = 32;
@@ -77,21 +83,24 @@ constexpr int SMEM_BYTES = TAB_OFF + kMaxEntries * ENTRY_BYTES + (kMaxEntries + 
 constexpr uint32_t kWaitLimit = 1u << 22;
 constexpr uint32_t IDESC64 = tc::idesc_tf32(128, 2 * NR);
 constexpr uint32_t IDESC32 = tc::idesc_tf32(128, NR);
-// tensor memory: accumulator set b at column 128 b (D: hi*hi 0..31, hi*lo
-// 32..63; D2: lo*hi 64..95); A of chunk parity a at 256 + 64 a (hi 0..31,
-// lo 32..63)
+// tensor memory: accumulator set b at column 96 b (D: hi*hi 0..31, hi*lo
+// 32..63; D2: lo*hi 64..95); A of chunk c at 192 + 128 (c % kABuf) (hi
+// 0..63, lo 64..127)
 constexpr uint32_t kTmemCols = 512;
-constexpr uint32_t TM_A = 256;
-constexpr int kGroupChunks = 2;            // chunks per accumulation group (K = 64)
+constexpr uint32_t TM_ACC = 96;
+constexpr uint32_t TM_A = 192;
+constexpr uint32_t TM_ASTRIDE = 2 * KC;
+constexpr int kGroupChunks = 1;            // chunks per accumulation group (K = 64)
 // barriers
 constexpr int BAR_FULL = 0;                // [kSlots] A of the slot landed (producer, tx)
 constexpr int BAR_EMPTY = kSlots;          // [kSlots] slot no longer read (issuer commits)
-constexpr int BAR_READY = 2 * kSlots;      // [2] chunk parity split (one arrival per worker warp)
-constexpr int BAR_MPAR = BAR_READY + 2;    // [2] chunk parity multiplied (issuer commits)
-constexpr int BAR_ACC = BAR_MPAR + 2;      // [2] accumulator set complete (issuer commits)
+constexpr int BAR_READY = 2 * kSlots;      // [kABuf] chunk c % kABuf split (one arrival per worker warp)
+constexpr int BAR_MPAR = BAR_READY + kABuf;  // [kABuf] chunk c % kABuf multiplied (issuer commits)
+constexpr int BAR_ACC = BAR_MPAR + kABuf;  // [2] accumulator set complete (issuer commits)
 constexpr int NBAR = BAR_ACC + 2;
 
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
+static_assert(TM_A + TM_ASTRIDE * kABuf <= kTmemCols, "tensor memory");
 static_assert(SLOT_BYTES % 1024 == 0, "128-byte swizzled tiles start on 1024 bytes");
 
 __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
@@ -198,18 +207,18 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
     for (int c = 0; c < nch; ++c) {
       const bool close = ct == cpt - 1 || gk == kGroupChunks - 1;
       const int buf = g & 1;
-      if (!tc::mbar_wait(&bar[BAR_READY + (c & 1)], (uint32_t)((c >> 1) & 1), kWaitLimit))
+      if (!tc::mbar_wait(&bar[BAR_READY + c % kABuf], (uint32_t)((c / kABuf) & 1), kWaitLimit))
         atomicExch(err, 1);
       tc::fence_after_sync();
-      const uint32_t ab = tmem + TM_A + 64u * (uint32_t)(c & 1) + (second ? 32u : 0u);
-      const uint32_t d = tmem + 128u * (uint32_t)buf + (second ? 64u : 0u);
+      const uint32_t ab = tmem + TM_A + TM_ASTRIDE * (uint32_t)(c % kABuf) + (second ? (uint32_t)KC : 0u);
+      const uint32_t d = tmem + TM_ACC * (uint32_t)buf + (second ? 64u : 0u);
       const uint64_t bd =
           tc::make_desc(tc::smem_addr(smem + (c % kSlots) * SLOT_BYTES + A_BYTES), 128, KC * 32);
 #pragma unroll
       for (int ks = 0; ks < KC / 8; ++ks)
         tc::mma_tf32_ta(d, ab + 8u * ks, bd + (uint64_t)((ks * 256) >> 4), second ? IDESC32 : IDESC64,
                         (gk > 0 || ks > 0) ? 1u : 0u);
-      tc::mma_commit(&bar[BAR_MPAR + (c & 1)]);
+      tc::mma_commit(&bar[BAR_MPAR + c % kABuf]);
       tc::mma_commit(&bar[BAR_EMPTY + c % kSlots]);
       if (close) {
         tc::mma_commit(&bar[BAR_ACC + buf]);
@@ -223,41 +232,43 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
     return nch;
   }
 
-  // workers.  Warp w owns rows 32 (w % 4) .. + 31 (its TMEM lanes) and K
-  // quads 4 half .. 4 half + 3 of every chunk, half = w / 4.
-  const int w = tid >> 5, lane = tid & 31, half = w >> 2;
+  // workers.  Warp w owns rows 32 (w % 4) .. + 31 (its TMEM lanes), K quads
+  // 4 kq .. 4 kq + 3 of every chunk and accumulator columns 8 kq .. 8 kq + 7,
+  // kq = w / 4; each copies B's k quad qb of column cb.
+  const int w = tid >> 5, lane = tid & 31, kq = w >> 2;
+  const bool copies_b = true;
   CopyMap m;
-  m.cb = 8 * (tid >> 6) + ((tid >> 2) & 7);
-  m.qb = 4 * ((tid >> 5) & 1) + (tid & 3);
+  m.cb = 8 * (tid >> 7) + ((tid >> 2) & 7);
+  m.qb = 4 * ((tid >> 5) & 3) + (tid & 3);
   m.offB = A_BYTES + tc::kmajor_off(m.cb, 4 * m.qb, KC);
   const int R = tid & 127;
   const uint32_t lane_base = ((uint32_t)((tid >> 5) & 3) * 32u) << 16;
 
-  float sum[16], comp[16], cross[16];
+  float sum[NCOL], comp[NCOL], cross[NCOL];
 #pragma unroll
-  for (int j = 0; j < 16; ++j) sum[j] = comp[j] = cross[j] = 0.f;
+  for (int j = 0; j < NCOL; ++j) sum[j] = comp[j] = cross[j] = 0.f;
 
   int nload = 0;
   for (int i = 0; i < kAhead; ++i) {
     if (nload < nch) {
-      src.load_b(nload, smem + (nload % kSlots) * SLOT_BYTES, m);
+      if (copies_b) src.load_b(nload, smem + (nload % kSlots) * SLOT_BYTES, m);
       ++nload;
     }
     cp_async_commit();
   }
 
   auto read = [&](int g) {
-    const uint32_t base = tmem + 128u * (uint32_t)(g & 1) + 16u * half + lane_base;
+    const uint32_t base = tmem + TM_ACC * (uint32_t)(g & 1) + (uint32_t)(NCOL * kq) + lane_base;
     if (!tc::mbar_wait(&bar[BAR_ACC + (g & 1)], (uint32_t)((g >> 1) & 1), kWaitLimit))
       atomicExch(err, 1);
     tc::fence_after_sync();
-    float hh[16], x1[16], x2[16];
-    tc::tmem_ld16(base, hh);
-    tc::tmem_ld16(base + 32u, x1);
-    tc::tmem_ld16(base + 64u, x2);
+    float hh[NCOL], x1[NCOL], x2[NCOL];
+    tc::tmem_ld8(base, hh);
+    tc::tmem_ld8(base + 32u, x1);
+    tc::tmem_ld8(base + 64u, x2);
     tc::fence_before_sync();
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
+    for (int j = 0; j < NCOL; ++j) {
       kahan_add(sum[j], comp[j], hh[j]);
       cross[j] += x1[j] + x2[j];
     }
@@ -267,13 +278,13 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
   bool pend = false;
   for (int c = 0; c < nch; ++c) {
     const int s = c % kSlots;
-    // chunk c - 2 multiplied: its slot (refilled with B below) and the
-    // tensor-memory A of this chunk's parity are free
-    if (c >= 2 &&
-        !tc::mbar_wait(&bar[BAR_MPAR + (c & 1)], (uint32_t)(((c - 2) >> 1) & 1), kWaitLimit))
+    // chunk c - kABuf multiplied: its slot (refilled with B below) and its
+    // tensor-memory A buffer (this chunk's) are free
+    if (c >= kABuf && !tc::mbar_wait(&bar[BAR_MPAR + c % kABuf],
+                                     (uint32_t)(((c / kABuf) - 1) & 1), kWaitLimit))
       atomicExch(err, 1);
     if (nload < nch) {
-      src.load_b(nload, smem + (nload % kSlots) * SLOT_BYTES, m);
+      if (copies_b) src.load_b(nload, smem + (nload % kSlots) * SLOT_BYTES, m);
       ++nload;
     }
     cp_async_commit();
@@ -283,12 +294,12 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
 
     unsigned char* slot = smem + s * SLOT_BYTES;
     {
-      // the row this thread owns, from the 128-byte swizzled A tile
-      const unsigned char* sa = slot + (uint32_t)R * 128u;
+      // the row this thread owns, from the 128-byte swizzled A box of its K half
+      const unsigned char* sa = slot + (kq >> 1) * A_HALF + (uint32_t)R * 128u;
       float hi[16], lo[16];
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
-        const int qq = 4 * half + j;
+        const int qq = 4 * (kq & 1) + j;
         const float4 x = *reinterpret_cast<const float4*>(sa + ((uint32_t)(qq ^ (R & 7)) << 4));
         hi[4 * j] = tf32_rz(x.x);
         hi[4 * j + 1] = tf32_rz(x.y);
@@ -299,25 +310,27 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
         lo[4 * j + 2] = x.z - hi[4 * j + 2];
         lo[4 * j + 3] = x.w - hi[4 * j + 3];
       }
-      const uint32_t ta = tmem + TM_A + 64u * (uint32_t)(c & 1) + 16u * half + lane_base;
+      const uint32_t ta = tmem + TM_A + TM_ASTRIDE * (uint32_t)(c % kABuf) + 16u * kq + lane_base;
       tc::tmem_st16(ta, hi);
-      tc::tmem_st16(ta + 32u, lo);
-      // the B segment this thread copied: low part next to it
-      unsigned char* sb = slot + m.offB;
-      const float4 xb = *reinterpret_cast<const float4*>(sb);
-      float4 lb;
-      lb.x = xb.x - tf32_rz(xb.x);
-      lb.y = xb.y - tf32_rz(xb.y);
-      lb.z = xb.z - tf32_rz(xb.z);
-      lb.w = xb.w - tf32_rz(xb.w);
-      *reinterpret_cast<float4*>(sb + B_BYTES) = lb;
+      tc::tmem_st16(ta + (uint32_t)KC, lo);
+      if (copies_b) {
+        // the B segment this thread copied: low part next to it
+        unsigned char* sb = slot + m.offB;
+        const float4 xb = *reinterpret_cast<const float4*>(sb);
+        float4 lb;
+        lb.x = xb.x - tf32_rz(xb.x);
+        lb.y = xb.y - tf32_rz(xb.y);
+        lb.z = xb.z - tf32_rz(xb.z);
+        lb.w = xb.w - tf32_rz(xb.w);
+        *reinterpret_cast<float4*>(sb + B_BYTES) = lb;
+      }
       tc::tmem_wait_st();
     }
     // B (cp.async copies and low parts) to the tensor core's proxy; A stored
     tc::fence_async_smem();
     tc::fence_before_sync();
     __syncwarp();
-    if (lane == 0) tc::mbar_arrive(&bar[BAR_READY + (c & 1)]);
+    if (lane == 0) tc::mbar_arrive(&bar[BAR_READY + c % kABuf]);
     const bool tile_end = ct == cpt - 1;
     const bool close = tile_end || gk == kGroupChunks - 1;
     if (close) {
@@ -326,7 +339,7 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
         if (pend_tile != tile) {
           src.finish(pend_tile, sum, comp, cross);
 #pragma unroll
-          for (int j = 0; j < 16; ++j) sum[j] = comp[j] = cross[j] = 0.f;
+          for (int j = 0; j < NCOL; ++j) sum[j] = comp[j] = cross[j] = 0.f;
         }
       }
       pend = true;
@@ -363,11 +376,11 @@ __device__ __forceinline__ uint32_t block_setup(uint64_t* bar, uint32_t* tslot) 
       tc::mbar_init(&bar[BAR_FULL + i], 1);
       tc::mbar_init(&bar[BAR_EMPTY + i], 2);
     }
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < kABuf; ++i) {
       tc::mbar_init(&bar[BAR_READY + i], WORKERS / 32);
       tc::mbar_init(&bar[BAR_MPAR + i], 2);
-      tc::mbar_init(&bar[BAR_ACC + i], 2);
     }
+    for (int i = 0; i < 2; ++i) tc::mbar_init(&bar[BAR_ACC + i], 2);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   tc::fence_before_sync();
@@ -444,9 +457,12 @@ struct SrcTa {
         gy = (g0 + lane - cumg[idx]) * 8;
       }
     }
-    if (lane == 0) expect_tx(full, 1024u * (uint32_t)png);
+    if (lane == 0) expect_tx(full, 2048u * (uint32_t)png);
     __syncwarp();
-    if (lane < png) tma_load_2d(a + 1024 * lane, gmap, gx + pk, gy, full);
+    if (lane < png) {
+      tma_load_2d(a + 1024 * lane, gmap, gx + pk, gy, full);
+      tma_load_2d(a + A_HALF + 1024 * lane, gmap, gx + pk + 32, gy, full);
+    }
     pk += KC;
     if (pk >= cpt * KC) {
       pk = 0;
@@ -468,15 +484,15 @@ struct SrcTa {
     const PairRow& e = tab[idx];
     const int l = (gi - cumg[idx]) * 8 + (R & 7);
     if (l >= e.r) return;
-    const int c0 = (threadIdx.x >> 7) * 16;
+    const int c0 = (threadIdx.x >> 7) * NCOL;
     if (!e.t) {  // slice partial
 #pragma unroll
-      for (int j = 0; j < 16; ++j) e.dst[(int64_t)(c0 + j) * e.ld + l] = (sum[j] - comp[j]) + cross[j];
+      for (int j = 0; j < NCOL; ++j) e.dst[(int64_t)(c0 + j) * e.ld + l] = (sum[j] - comp[j]) + cross[j];
       return;
     }
     // T in the split-exact form, zero padded to ld
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
+    for (int j = 0; j < NCOL; ++j) {
       const float v = (sum[j] - comp[j]) + cross[j];
       const float hi = tf32_rz(v);
       e.dst[(int64_t)(c0 + j) * e.ld + l] = hi + tf32_rn(v - hi);
@@ -484,7 +500,7 @@ struct SrcTa {
     if (l == e.r - 1)
       for (int lp = e.r; lp < e.ld; ++lp)
 #pragma unroll
-        for (int j = 0; j < 16; ++j) e.dst[(int64_t)(c0 + j) * e.ld + lp] = 0.f;
+        for (int j = 0; j < NCOL; ++j) e.dst[(int64_t)(c0 + j) * e.ld + lp] = 0.f;
   }
 };
 
@@ -618,6 +634,7 @@ struct SrcItems {
     }
     expect_tx(full, (uint32_t)A_BYTES);
     tma_load_2d(a, pmap, pk, py, full);
+    tma_load_2d(a + A_HALF, pmap, pk + 32, py, full);
     pk += KC;
   }
   __device__ void load_b(int, unsigned char* slot, const CopyMap& m) {
@@ -654,10 +671,10 @@ struct SrcUt : SrcItems {
   double* ynl;
   int64_t N, r0;
   __device__ void finish(int, const float* sum, const float* comp, const float* cross) const {
-    const int row = threadIdx.x & 127, c0 = (threadIdx.x >> 7) * 16;
+    const int row = threadIdx.x & 127, c0 = (threadIdx.x >> 7) * NCOL;
     if (row >= nrows) return;
 #pragma unroll
-    for (int j = 0; j < 16; ++j)
+    for (int j = 0; j < NCOL; ++j)
       ynl[(int64_t)(c0 + j) * N + r0 + row] =
           ((double)sum[j] - (double)comp[j]) + (double)cross[j];
   }
@@ -715,7 +732,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_ut_tc(FarOp op, const CUtensorMa
   src.N = N;
   src.r0 = r0;
   if (run_stream(src, smem, bar, tmem, err) == 0 && threadIdx.x < WORKERS) {
-    float z[16] = {};
+    float z[NCOL] = {};
     src.finish(0, z, z, z);
   }
   block_teardown(tmem);
@@ -728,12 +745,12 @@ struct SrcLeaf : SrcItems {
   int64_t N, ldy, t0;
   int nrhs, d;
   __device__ void finish(int, const float* sum, const float* comp, const float* cross) const {
-    const int row = threadIdx.x & 127, c0 = (threadIdx.x >> 7) * 16;
+    const int row = threadIdx.x & 127, c0 = (threadIdx.x >> 7) * NCOL;
     if (row >= nrows) return;
     const int64_t t = t0 + row;
     const int64_t orig = perm[t];
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
+    for (int j = 0; j < NCOL; ++j) {
       const int c = c0 + j;
       if (c < nrhs) {
         const double yn = d >= 2 ? ynl[(int64_t)c * N + t] : 0.0;
@@ -812,7 +829,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_tc(FarOp op, NearOp nr,
   src.nrhs = nrhs;
   src.d = d;
   if (run_stream(src, smem, bar, tmem, err) == 0 && threadIdx.x < WORKERS) {
-    float z[16] = {};
+    float z[NCOL] = {};
     src.finish(0, z, z, z);
   }
   block_teardown(tmem);
