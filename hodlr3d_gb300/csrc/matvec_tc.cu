@@ -8,7 +8,7 @@
 //             tall GEMM [V_p1^T; V_p2^T; ...] X_slice (M = pair columns packed
 //             in groups of 8 rows, tiles of 128 rows, K = slice points); level
 //             d-1 pairs get T, the pairs above get slice partials
-//   tred      FP64 sum of the slice partials
+//   tred      compensated sum of the slice partials
 //   ta_leaf   per input leaf: the same for the leaf-level pairs
 //   ut_tc     per (slice, 128 rows): long-K GEMM over the pairs of levels < d,
 //             sum of U_p[rows] T_p
@@ -79,8 +79,11 @@ constexpr int kAhead = kSlots - kABuf;     // B chunks in flight ahead of the sp
 constexpr int TAB_OFF = kSlots * SLOT_BYTES;
 constexpr int kMaxEntries = 768;           // table entries (pairs, near blocks) of one block
 constexpr int ENTRY_BYTES = 32;
-constexpr int SMEM_BYTES = TAB_OFF + kMaxEntries * ENTRY_BYTES + (kMaxEntries + 1) * 4;
-constexpr uint32_t kWaitLimit = 1u << 22;
+constexpr int RING_OFF = TAB_OFF + kMaxEntries * ENTRY_BYTES + (kMaxEntries + 1) * 4;
+constexpr int kRing = 16;                  // tiles whose 8-row groups the T kernels keep
+constexpr int SMEM_BYTES = RING_OFF + kRing * 16 * 4;
+constexpr uint32_t kWaitLimit = 1u << 17;   // polls of up to kWaitHintNs each: about 1 s
+constexpr uint32_t kWaitHintNs = 8192;
 constexpr uint32_t IDESC64 = tc::idesc_tf32(128, 2 * NR);
 constexpr uint32_t IDESC32 = tc::idesc_tf32(128, NR);
 // tensor memory: accumulator set b at column 96 b (D: hi*hi 0..31, hi*lo
@@ -191,7 +194,7 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
     for (int c = 0; c < nch; ++c) {
       const int s = c % kSlots;
       if (lane == 0 && c >= kSlots &&
-          !tc::mbar_wait(&bar[BAR_EMPTY + s], (uint32_t)(((c / kSlots) - 1) & 1), kWaitLimit))
+          !tc::mbar_wait_sleep(&bar[BAR_EMPTY + s], (uint32_t)(((c / kSlots) - 1) & 1), kWaitLimit, kWaitHintNs))
         atomicExch(err, 1);
       __syncwarp();
       src.produce(c, smem + s * SLOT_BYTES, &bar[BAR_FULL + s], lane);
@@ -207,7 +210,7 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
     for (int c = 0; c < nch; ++c) {
       const bool close = ct == cpt - 1 || gk == kGroupChunks - 1;
       const int buf = g & 1;
-      if (!tc::mbar_wait(&bar[BAR_READY + c % kABuf], (uint32_t)((c / kABuf) & 1), kWaitLimit))
+      if (!tc::mbar_wait_sleep(&bar[BAR_READY + c % kABuf], (uint32_t)((c / kABuf) & 1), kWaitLimit, kWaitHintNs))
         atomicExch(err, 1);
       tc::fence_after_sync();
       const uint32_t ab = tmem + TM_A + TM_ASTRIDE * (uint32_t)(c % kABuf) + (second ? (uint32_t)KC : 0u);
@@ -259,7 +262,7 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
 
   auto read = [&](int g) {
     const uint32_t base = tmem + TM_ACC * (uint32_t)(g & 1) + (uint32_t)(NCOL * kq) + lane_base;
-    if (!tc::mbar_wait(&bar[BAR_ACC + (g & 1)], (uint32_t)((g >> 1) & 1), kWaitLimit))
+    if (!tc::mbar_wait_sleep(&bar[BAR_ACC + (g & 1)], (uint32_t)((g >> 1) & 1), kWaitLimit, kWaitHintNs))
       atomicExch(err, 1);
     tc::fence_after_sync();
     float hh[NCOL], x1[NCOL], x2[NCOL];
@@ -280,8 +283,8 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
     const int s = c % kSlots;
     // chunk c - kABuf multiplied: its slot (refilled with B below) and its
     // tensor-memory A buffer (this chunk's) are free
-    if (c >= kABuf && !tc::mbar_wait(&bar[BAR_MPAR + c % kABuf],
-                                     (uint32_t)(((c / kABuf) - 1) & 1), kWaitLimit))
+    if (c >= kABuf && !tc::mbar_wait_sleep(&bar[BAR_MPAR + c % kABuf],
+                                     (uint32_t)(((c / kABuf) - 1) & 1), kWaitLimit, kWaitHintNs))
       atomicExch(err, 1);
     if (nload < nch) {
       if (copies_b) src.load_b(nload, smem + (nload % kSlots) * SLOT_BYTES, m);
@@ -289,7 +292,7 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
     }
     cp_async_commit();
     cp_async_wait<kAhead>();
-    if (!tc::mbar_wait(&bar[BAR_FULL + s], (uint32_t)((c / kSlots) & 1), kWaitLimit))
+    if (!tc::mbar_wait_sleep(&bar[BAR_FULL + s], (uint32_t)((c / kSlots) & 1), kWaitLimit, kWaitHintNs))
       atomicExch(err, 1);
 
     unsigned char* slot = smem + s * SLOT_BYTES;
@@ -434,6 +437,7 @@ __device__ __forceinline__ int upper_index(const int* cum, int n, int v) {
 struct SrcTa {
   const PairRow* tab;
   const int* cumg;   // groups before each entry
+  int* ring;         // [kRing][16]: entry << 8 | group within the pair, of tile t % kRing
   int n, ngroups;
   int tile0, tstep, ntile, cpt;
   int kin;
@@ -455,7 +459,10 @@ struct SrcTa {
         gmap = tab[idx].map;
         gx = tab[idx].ro;
         gy = (g0 + lane - cumg[idx]) * 8;
+        // for the workers' finish of this tile (read kRing / cpt chunks later at most)
+        ring[(pc % kRing) * 16 + lane] = (idx << 8) | (g0 + lane - cumg[idx]);
       }
+      __syncwarp();  // the ring entries before lane 0's arrival (release) below
     }
     if (lane == 0) expect_tx(full, 2048u * (uint32_t)png);
     __syncwarp();
@@ -480,9 +487,9 @@ struct SrcTa {
     const int R = threadIdx.x & 127;
     const int gi = (tile0 + t * tstep) * 16 + (R >> 3);
     if (gi >= ngroups) return;
-    const int idx = upper_index(cumg, n, gi);
-    const PairRow& e = tab[idx];
-    const int l = (gi - cumg[idx]) * 8 + (R & 7);
+    const int code = ring[(t % kRing) * 16 + (R >> 3)];
+    const PairRow& e = tab[code >> 8];
+    const int l = (code & 255) * 8 + (R & 7);
     if (l >= e.r) return;
     const int c0 = (threadIdx.x >> 7) * NCOL;
     if (!e.t) {  // slice partial
@@ -571,6 +578,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_ta_tc(FarOp op, const CUtensorMa
   SrcTa src;
   src.tab = tab;
   src.cumg = cumg;
+  src.ring = reinterpret_cast<int*>(smem + RING_OFF);
   src.n = n;
   src.ngroups = ngroups;
   src.tile0 = blockIdx.y;
@@ -584,8 +592,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_ta_tc(FarOp op, const CUtensorMa
   block_teardown(tmem);
 }
 
-// FP64 sum of slice partials into the padded T (split-exact form):
-// T_p[c][l] = sum_s P_p[s][c][l]
+// Sum of slice partials into the padded T (split-exact form), compensated
+// FP32: T_p[c][l] = sum_s P_p[s][c][l]
 __global__ void k_tred_tc(FarOp op, const int32_t* __restrict__ pairs, const float* __restrict__ Pp,
                           float* __restrict__ T) {
   const int p = pairs[blockIdx.x];
@@ -595,10 +603,10 @@ __global__ void k_tred_tc(FarOp op, const int32_t* __restrict__ pairs, const flo
   float* dst = T + op.tr_off4[p] * NR;
   for (int o = threadIdx.x; o < rp * NR; o += blockDim.x) {
     const int c = o / rp, l = o - c * rp;
-    double acc = 0.0;
+    float sum = 0.f, comp = 0.f;
     if (l < r)
-      for (int64_t s = 0; s < ns; ++s) acc += (double)src[s * r * NR + c * r + l];
-    dst[o] = tf32_split_value(acc);
+      for (int64_t s = 0; s < ns; ++s) kahan_add(sum, comp, src[s * r * NR + c * r + l]);
+    dst[o] = tf32_split_value((double)sum - (double)comp);
   }
 }
 
@@ -914,7 +922,7 @@ int launch_matvec_tc(cudaStream_t s, int64_t N, const int32_t* perm, const FarOp
     ++launches;
     if (prof) prof->mark(s, "ta_slice");
     if (B.n_upper > 0) {
-      k_tred_tc<<<(unsigned)B.n_upper, 128, 0, s>>>(far, B.upper_pairs, B.p, B.t);
+      k_tred_tc<<<(unsigned)B.n_upper, 256, 0, s>>>(far, B.upper_pairs, B.p, B.t);
       ++launches;
       if (prof) prof->mark(s, "tred");
     }

@@ -111,6 +111,23 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
   return false;
 }
 
+// Same, with each poll suspending the thread for up to hint_ns nanoseconds
+// (it resumes when the phase completes): waiting warps leave the issue slots
+// to the others.  Gives up after `limit` polls and returns false.
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, uint32_t limit,
+                                                uint32_t hint_ns) {
+  const uint32_t a = smem_addr(bar);
+  for (uint32_t it = 0; it < limit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+        "selp.b32 %0, 1, 0, p;\n}\n"
+        : "=r"(done) : "r"(a), "r"(parity), "r"(hint_ns) : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
 __device__ __forceinline__ void fence_before_sync() {
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
 }
