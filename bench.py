@@ -120,7 +120,7 @@ def max_over_ranks(ws, v: float) -> float:
 
 
 # ----------------------------------------------------------------------------
-def cpu_sample(pts, tol_pow, steps, warmup, threads, n_leaves=16):
+def cpu_sample(pts, tol_pow, steps, warmup, threads, n_leaves=16, qchoice=16, diag=float("nan")):
     """Times the reference algorithm (the CPU oracle, CUR form with the kernel
     entries re-evaluated as src/HODLR3DTree.cpp:1660-1755 does) on a bounded
     sample: the far field of the ancestors of n_leaves spread-out leaves at
@@ -128,7 +128,7 @@ def cpu_sample(pts, tol_pow, steps, warmup, threads, n_leaves=16):
     Returns seconds per full matvec (one right-hand side) per step."""
     from oracle import oracle as orc
     orc.set_threads(threads)
-    o = orc.Oracle(pts, 4, 1.0, tol_pow, 16)
+    o = orc.Oracle(pts, 4, 1.0, tol_pow, qchoice, diag)
     d = o.levels
     nleaf = 8 ** d
     leaves = np.linspace(0, nleaf - 1, n_leaves).astype(np.int64)
@@ -163,7 +163,8 @@ def run_reference(args):
     from hodlr3d_gb300.workloads import grid_cell_centres
     pts = grid_cell_centres(args.n)
     threads = os.cpu_count() or 1
-    secs, desc = cpu_sample(pts, args.tol_pow, args.steps, args.warmup, threads)
+    secs, desc = cpu_sample(pts, args.tol_pow, args.steps, args.warmup, threads, qchoice=args.qchoice,
+                            diag=args.diag)
     s = float(np.mean(secs))
     v = 1.0 / s
     line = {
@@ -180,9 +181,11 @@ def run_reference(args):
 
 
 def config(args):
+    kern = ("kernel 1/r with quadrature diagonal (Qchoice 16)" if args.qchoice == 16 and args.diag != args.diag
+            else f"kernel Qchoice {args.qchoice}" + ("" if args.diag != args.diag else f", diagonal {args.diag:g}"))
     return {"workload": f"HODLR3D matvec, {args.n}^3 grid cell centres on [-1,1]^3, leaf 64 "
-                        f"(nP1D 4), kernel 1/r with quadrature diagonal (Qchoice 16), ACA tol "
-                        f"1e-{args.tol_pow}, {args.nrhs} right-hand sides N(0,1)",
+                        f"(nP1D 4), {kern}, ACA tol 1e-{args.tol_pow}, {args.nrhs} right-hand "
+                        f"sides N(0,1)",
             "N": args.n ** 3, "nrhs": args.nrhs, "precision": "mixed (FP32 factors and near field, "
             "FP64 accumulation across tiles)", "tol_pow": args.tol_pow,
             "l2": "inputs larger than L2 (the FP32 factors alone exceed 129 MB by two orders)"}
@@ -199,7 +202,8 @@ def measured_traffic(kernel, args):
     except (OSError, ValueError):
         return None
     e = rec.get(kernel)
-    if not e or e.get("n") != args.n or e.get("nrhs") != args.nrhs or e.get("tol_pow") != args.tol_pow:
+    if (not e or e.get("n") != args.n or e.get("nrhs") != args.nrhs or e.get("tol_pow") != args.tol_pow
+            or e.get("qchoice") != args.qchoice or args.diag == args.diag):
         return None
     return e["bytes_per_launch"]
 
@@ -275,13 +279,13 @@ def run_ours(args):
     pts = grid_cell_centres(args.n)
     N = len(pts)
     t = time.perf_counter()
-    H = HODLR3D(4, 1.0, args.tol_pow, 16, pts, device=local)
+    H = HODLR3D(4, 1.0, args.tol_pow, args.qchoice, pts, device=local, diag_override=args.diag)
     H.assemble()
     torch.cuda.synchronize()
     t_setup = time.perf_counter() - t
     st = H.stats()
     nrhs = args.nrhs
-    X = torch.tensor(charges_normal(N, nrhs, seed=11), device=dev)
+    X = torch.tensor(charges_normal(N, nrhs, seed=11), device=dev).reshape(N, nrhs)
     x1 = X[:, 0].contiguous()
     stream = torch.cuda.current_stream()
 
@@ -348,7 +352,7 @@ def run_ours(args):
             "whole_matvec_GBps": sum(ran.values()) / (ms * 1e-3) / 1e9}
 
     # ---- GMRES: b = A x_true, x_true U[0,1) ------------------------------
-    xt = torch.tensor(charges_uniform(N, nrhs, seed=21), device=dev)
+    xt = torch.tensor(charges_uniform(N, nrhs, seed=21), device=dev).reshape(N, nrhs)
     B = H.matvec(xt, "fp64")
     torch.cuda.synchronize()
     t = time.perf_counter()
@@ -388,7 +392,7 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        secs, desc = cpu_sample(pts, args.tol_pow, 1, 0, threads)
+        secs, desc = cpu_sample(pts, args.tol_pow, 1, 0, threads, qchoice=args.qchoice, diag=args.diag)
         cpu = {"value": 1.0 / float(np.mean(secs)), "unit": "RHS/s", "cores": threads,
                "kind": "port", "sample": desc}
 
@@ -422,6 +426,9 @@ def main():
     ap.add_argument("--n", type=int, default=64)
     ap.add_argument("--nrhs", type=int, default=32)
     ap.add_argument("--tol-pow", type=int, default=10)
+    ap.add_argument("--qchoice", type=int, default=16, help="kernel (the reference's Qchoice)")
+    ap.add_argument("--diag", type=float, default=float("nan"),
+                    help="diagonal value override (e.g. 1 for exp(-r), Qchoice 1)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -803,14 +803,19 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
   B.n_upper = h->n_upper;
   B.max_slice = h->max_slice;
   const int nrp = h3d::padded_nrhs(nrhs);
-  const bool tc_ok = precision == HODLR3D_MIXED && nrp == 32 && !trans && h->max_leaf <= 128 &&
+  // the tensor-core engine takes the forward mixed product in batches of up to
+  // 32 right-hand sides (fewer are zero padded: streaming the factors costs
+  // the same, and it beats the CUDA-core kernels from one right-hand side on)
+  const bool tc_ok = precision == HODLR3D_MIXED && !trans && h->max_leaf <= 128 &&
                      h->leaves_aligned && h->tc_entries <= h3d::tc_max_entries();
+  (void)nrp;
   if (h->engine == 2 && !tc_ok)
     return set_error(HODLR3D_ERR_UNSUPPORTED,
-                     "the tensor-core engine needs A x (not the transpose) in the mixed form, 17..32 "
-                     "right-hand sides, leaves of at most 128 points, each a multiple of 4, and at "
-                     "most %d pairs per block (this tree: %d)", h3d::tc_max_entries(), h->tc_entries);
+                     "the tensor-core engine needs A x (not the transpose) in the mixed form, "
+                     "leaves of at most 128 points, each a multiple of 4, and at most %d pairs per "
+                     "block (this tree: %d)", h3d::tc_max_entries(), h->tc_entries);
   if (tc_ok && h->engine != 1) {
+    H3D_TRY(ensure_matvec_buffers(h, 32));  // slice partials and level sums of 32 columns
     if (!h->dev_err.p) {
       H3D_CUDA(h->dev_err.ensure(sizeof(int)));
       H3D_CUDA(cudaMemsetAsync(h->dev_err.p, 0, sizeof(int), s));
@@ -861,8 +866,10 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
     T.umaps = tm;
     T.vmaps = tm + h->npairs;
     T.nmaps = tm + 2 * h->npairs;
-    h->launches += h3d::launch_matvec_tc(s, h->N, h->perm.as<int32_t>(), far, nr, T, x, ld, y, ld,
-                                         nrhs, h->profiling ? &h->prof : nullptr);
+    for (int c0 = 0; c0 < nrhs; c0 += 32)
+      h->launches += h3d::launch_matvec_tc(s, h->N, h->perm.as<int32_t>(), far, nr, T, x + c0 * ld,
+                                           ld, y + c0 * ld, ld, std::min(32, nrhs - c0),
+                                           h->profiling ? &h->prof : nullptr);
   } else {
     h->launches += h3d::launch_matvec(s, h->N, h->perm.as<int32_t>(), far, nr, B, x, ld, y, ld, nrhs,
                                       precision, trans ? 1 : 0, h->profiling ? &h->prof : nullptr);
