@@ -263,8 +263,8 @@ __global__ void __launch_bounds__(BS) k_aca(const AcaTask* __restrict__ tasks, i
 // Copies the first r columns of U and V of every task into the final pools.
 // FP64 (at dst_off): U (n x r) then V (m x r), column-major.  FP32 (at
 // dst_off32, optional): U row-major with the rank padded to rp = round4(r),
-// then V column-major with the leading dimension padded to mp = round4(m),
-// padding zero -- every row of U and column of V starts on 16 bytes.
+// padding zero -- every row starts on 16 bytes (the FP32 V is written after
+// the assembly, grouped by source box: launch_v32_grouped).
 __global__ void k_aca_compact(const AcaTask* __restrict__ tasks, const int32_t* __restrict__ rank,
                               const int64_t* __restrict__ dst_off,
                               const int64_t* __restrict__ dst_off32, const double* __restrict__ ws,
@@ -279,18 +279,28 @@ __global__ void k_aca_compact(const AcaTask* __restrict__ tasks, const int32_t* 
   for (int64_t i = threadIdx.x; i < nv; i += blockDim.x) out64[o + nu + i] = V[i];
   if (!out32) return;
   const int rp = (r + 3) & ~3;
-  const int64_t mp = (T.m + 3) & ~3;
   float* u32 = out32 + dst_off32[blockIdx.x];
-  float* v32 = u32 + (int64_t)T.n * rp;
   for (int64_t e = threadIdx.x; e < (int64_t)T.n * rp; e += blockDim.x) {
     const int64_t i = e / rp;
     const int l = (int)(e - i * rp);
     u32[e] = l < r ? tf32_split_value(U[(int64_t)l * T.n + i]) : 0.f;
   }
+}
+
+// FP32 V of every pair (split-exact form) from its FP64 V (m x r,
+// column-major): column-major with the leading dimension padded to
+// mp = round4(m), padding zero, at v32[p]; one block per pair.
+__global__ void k_v32(const double* const* __restrict__ v64, float* const* __restrict__ v32,
+                      const int32_t* __restrict__ msize, const int32_t* __restrict__ rank) {
+  const int64_t p = blockIdx.x;
+  const int r = rank[p];
+  if (r <= 0) return;
+  const int64_t m = msize[p], mp = (m + 3) & ~int64_t(3);
+  const double* src = v64[p];
+  float* dst = v32[p];
   for (int64_t e = threadIdx.x; e < mp * r; e += blockDim.x) {
-    const int l = (int)(e / mp);
-    const int64_t i = e - (int64_t)l * mp;
-    v32[e] = i < T.m ? tf32_split_value(V[(int64_t)l * T.m + i]) : 0.f;
+    const int64_t l = e / mp, i = e - l * mp;
+    dst[e] = i < m ? tf32_split_value(src[l * m + i]) : 0.f;
   }
 }
 
@@ -322,6 +332,13 @@ cudaError_t launch_aca_compact(cudaStream_t s, int ntasks, const AcaTask* tasks,
                                float* out32) {
   if (ntasks == 0) return cudaSuccess;
   k_aca_compact<<<ntasks, 256, 0, s>>>(tasks, rank, dst_off, dst_off32, ws, out64, out32);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_v32(cudaStream_t s, int64_t npairs, const double* const* v64, float* const* v32,
+                       const int32_t* msize, const int32_t* rank) {
+  if (npairs <= 0) return cudaSuccess;
+  k_v32<<<(unsigned)npairs, 256, 0, s>>>(v64, v32, msize, rank);
   return cudaGetLastError();
 }
 

@@ -176,6 +176,12 @@ struct hodlr3d_handle {
   std::vector<int32_t> h_fac_pool;      // per pair: pool index
   std::vector<double*> h_u64, h_v64;
   std::vector<float*> h_u32, h_v32;
+  // FP32 V of the pairs of each source box, contiguous in the order of its
+  // reverse list: per box (all levels numbered together) the float offset in
+  // v32_pool of its first pair and its rows (the sum of the ranks)
+  DevBuf* v32_pool = nullptr;
+  std::vector<int64_t> h_vbox_off;
+  std::vector<int32_t> h_vbox_rows;
   DevBuf rank, u64, v64, u32, v32, tr_off, tr_off4, part_off, items, upper, pair_level;
   int64_t sum_rank = 0, sum_rank4 = 0, part_total = 0, n_items = 0, n_upper = 0, factor_entries = 0;
   int tc_entries = 0;  // largest table of a tensor-core block
@@ -388,6 +394,62 @@ struct HostTask {
   bool leaf;
 };
 
+// FP32 copies of V grouped by source box: the pairs whose source is box b
+// (its reverse list) get consecutive column-major round4(m_b) x r blocks, so
+// that the V of all pairs of a source box form one (sum of ranks) x
+// round4(m_b) row-major matrix (one tensor map per box for the tensor-core
+// T kernels); converted from the FP64 factors after the assembly.
+int group_v32(hodlr3d_t h) {
+  const int64_t np = h->npairs;
+  cudaStream_t s = h->stream;
+  std::vector<int32_t> rev(std::max<int64_t>(np, 1));
+  if (np)
+    H3D_CUDA(cudaMemcpy(rev.data(), h->rev.p, sizeof(int32_t) * np, cudaMemcpyDeviceToHost));
+  const int64_t nbox = (int64_t)h->h_il_ptr.size() - 1;
+  h->h_vbox_off.assign(nbox + 1, 0);
+  h->h_vbox_rows.assign(nbox, 0);
+  std::vector<int64_t> voff(np, 0);
+  std::vector<int32_t> msize(np, 0);
+  int64_t cursor = 0;
+  for (int64_t b = 0; b < nbox; ++b) {
+    int j = 0;
+    while (j < h->levels && h3d::level_base(j + 1) <= b) ++j;
+    int64_t a0, a1;
+    box_range(h, j, b - h3d::level_base(j), a0, a1);
+    const int64_t m = a1 - a0, mp = (m + 3) & ~int64_t(3);
+    h->h_vbox_off[b] = cursor;
+    for (int64_t q = h->h_il_ptr[b]; q < h->h_il_ptr[b + 1]; ++q) {
+      const int p = rev[q];
+      voff[p] = cursor;
+      msize[p] = (int32_t)m;
+      cursor += (int64_t)h->h_rank[p] * mp;
+      h->h_vbox_rows[b] += h->h_rank[p];
+    }
+  }
+  h->h_vbox_off[nbox] = cursor;
+  h->v32_pool = new DevBuf();
+  h->pools.push_back(h->v32_pool);
+  H3D_CUDA(h->v32_pool->ensure(sizeof(float) * std::max<int64_t>(cursor, 4)));
+  float* base = h->v32_pool->as<float>();
+  for (int64_t p = 0; p < np; ++p) h->h_v32[p] = base + voff[p];
+  if (np) {
+    DevBuf d64, d32, dm, dr;
+    H3D_CUDA(d64.ensure(sizeof(void*) * np));
+    H3D_CUDA(d32.ensure(sizeof(void*) * np));
+    H3D_CUDA(dm.ensure(sizeof(int32_t) * np));
+    H3D_CUDA(dr.ensure(sizeof(int32_t) * np));
+    H3D_CUDA(cudaMemcpy(d64.p, h->h_v64.data(), sizeof(void*) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(cudaMemcpy(d32.p, h->h_v32.data(), sizeof(void*) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(cudaMemcpy(dm.p, msize.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(cudaMemcpy(dr.p, h->h_rank.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(h3d::launch_v32(s, np, d64.as<const double* const>(), d32.as<float* const>(),
+                             dm.as<int32_t>(), dr.as<int32_t>()));
+    ++h->launches;
+    H3D_CUDA(cudaStreamSynchronize(s));
+  }
+  return HODLR3D_OK;
+}
+
 int run_aca_batch(hodlr3d_t h, std::vector<HostTask>& batch, std::vector<HostTask>& retry,
                   bool small_kernel) {
   cudaStream_t s = h->stream;
@@ -460,7 +522,7 @@ int run_aca_batch(hodlr3d_t h, std::vector<HostTask>& batch, std::vector<HostTas
     dst[i] = total;
     total += (int64_t)rk[i] * (batch[i].n + batch[i].m);
     dst32[i] = total32;
-    total32 += (int64_t)batch[i].n * ((rk[i] + 3) & ~3) + (int64_t)((batch[i].m + 3) & ~3) * rk[i];
+    total32 += (int64_t)batch[i].n * ((rk[i] + 3) & ~3);
   }
   DevBuf* pool64 = new DevBuf();
   h->pools.push_back(pool64);
@@ -489,11 +551,7 @@ int run_aca_batch(hodlr3d_t h, std::vector<HostTask>& batch, std::vector<HostTas
     double* base64 = pool64->as<double>() + dst[i];
     h->h_u64[p] = base64;
     h->h_v64[p] = base64 + (int64_t)r * batch[i].n;
-    if (pool32) {
-      float* base32 = pool32->as<float>() + dst32[i];
-      h->h_u32[p] = base32;
-      h->h_v32[p] = base32 + (int64_t)batch[i].n * ((r + 3) & ~3);
-    }
+    if (pool32) h->h_u32[p] = pool32->as<float>() + dst32[i];
     const int32_t* pr = pvh.data() + tasks[i].piv_off;
     h->h_piv_rows[p].assign(pr, pr + r);
     h->h_piv_cols[p].assign(pr + tasks[i].cap, pr + tasks[i].cap + r);
@@ -515,6 +573,7 @@ int assemble(hodlr3d_t h) {
   h->h_v32.assign(np, nullptr);
   for (DevBuf* b : h->pools) delete b;
   h->pools.clear();
+  h->v32_pool = nullptr;
   h->aca_batches = 0;
   const int cap0 = h->opt.rank_cap > 0 ? h->opt.rank_cap : 256;
   std::vector<HostTask> todo;
@@ -562,6 +621,7 @@ int assemble(hodlr3d_t h) {
     }
     todo.swap(retry);
   }
+  if (h->opt.keep_fp32) H3D_TRY(group_v32(h));
   // per-pair tables for the matvec: T offsets, slice work items of the
   // non-leaf pairs, partial offsets of the pairs above level d - 1
   const int d = h->levels;
@@ -683,10 +743,10 @@ int ensure_matvec_buffers(hodlr3d_t h, int nrhs) {
 }
 
 // Tensor maps (2D tiled, FP32, 128-byte swizzle, zero fill outside) of the
-// tensor-core engine's A operands: per pair U_p (n x round4(r), box 32 x 128)
-// and V_p (r x round4(m), box 32 x 8), per leaf and neighbour slot the
-// near-field block (nk x round4(ne), box 32 x 128).  Maps of empty operands
-// stay zero and are never used.
+// tensor-core engine's A operands, box 32 x 128: per pair U_p (n x round4(r)),
+// per source box the V of its pairs (sum of ranks x round4(m)), per leaf and
+// neighbour slot the near-field block (nk x round4(ne)).  Maps of empty
+// operands stay zero and are never used.
 int build_tensor_maps(hodlr3d_t h, const std::vector<int64_t>& near_off) {
   static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
   if (!encode) {
@@ -696,7 +756,8 @@ int build_tensor_maps(hodlr3d_t h, const std::vector<int64_t>& near_off) {
     if (!encode || q != cudaDriverEntryPointSuccess)
       return set_error(HODLR3D_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
   }
-  const int64_t np = h->npairs, nm = 2 * np + 27 * h->nleaf;
+  const int64_t np = h->npairs, nbox = (int64_t)h->h_vbox_rows.size();
+  const int64_t nm = np + nbox + 27 * h->nleaf;
   std::vector<CUtensorMap> maps((size_t)std::max<int64_t>(nm, 1));
   std::memset(maps.data(), 0, sizeof(CUtensorMap) * maps.size());
   std::atomic<int> bad{0};
@@ -726,11 +787,18 @@ int build_tensor_maps(hodlr3d_t h, const std::vector<int64_t>& near_off) {
         const int r = h->h_rank[p];
         if (r <= 0) continue;
         const int j = h->h_pair_level[p];
-        int64_t a0, a1, b0, b1;
+        int64_t a0, a1;
         box_range(h, j, h->h_pair_tgt[p] - h3d::level_base(j), a0, a1);
-        box_range(h, j, h->h_pair_src[p] - h3d::level_base(j), b0, b1);
         enc(&maps[p], h->h_u32[p], (r + 3) & ~3, a1 - a0, 128);
-        enc(&maps[np + p], h->h_v32[p], ((b1 - b0) + 3) & ~int64_t(3), r, 8);
+      }
+      for (int64_t b = t; b < nbox; b += nthr) {
+        if (h->h_vbox_rows[b] <= 0) continue;
+        int j = 0;
+        while (j < h->levels && h3d::level_base(j + 1) <= b) ++j;
+        int64_t b0, b1;
+        box_range(h, j, b - h3d::level_base(j), b0, b1);
+        enc(&maps[np + b], h->v32_pool->as<float>() + h->h_vbox_off[b], ((b1 - b0) + 3) & ~int64_t(3),
+            h->h_vbox_rows[b], 128);
       }
       for (int64_t k = t; k < h->nleaf; k += nthr) {
         const int64_t nk = h->h_leaf_off[k + 1] - h->h_leaf_off[k];
@@ -739,7 +807,7 @@ int build_tensor_maps(hodlr3d_t h, const std::vector<int64_t>& near_off) {
           if (off < 0) continue;
           const int64_t nn = sl < 26 ? h->h_nbr_leaf[26 * k + sl] : k;
           const int64_t ne = h->h_leaf_off[nn + 1] - h->h_leaf_off[nn];
-          enc(&maps[2 * np + 27 * k + sl], knear + off, (ne + 3) & ~int64_t(3), nk, 128);
+          enc(&maps[np + nbox + 27 * k + sl], knear + off, (ne + 3) & ~int64_t(3), nk, 128);
         }
       }
     });
@@ -865,7 +933,7 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
     const CUtensorMap* tm = h->tmaps.as<CUtensorMap>();
     T.umaps = tm;
     T.vmaps = tm + h->npairs;
-    T.nmaps = tm + 2 * h->npairs;
+    T.nmaps = tm + h->npairs + (int64_t)h->h_vbox_rows.size();
     for (int c0 = 0; c0 < nrhs; c0 += 32)
       h->launches += h3d::launch_matvec_tc(s, h->N, h->perm.as<int32_t>(), far, nr, T, x + c0 * ld,
                                            ld, y + c0 * ld, ld, std::min(32, nrhs - c0),

@@ -70,7 +70,8 @@ int padded_nrhs(int nrhs);
 // FP32 copies U is row-major with the rank padded to a multiple of 4 and V is
 // column-major with n padded to a multiple of 4 (zero padding), so that every
 // row of U and column of V starts on 16 bytes for the tensor-core kernels;
-// their values are in the split-exact TF32 form (tf32_split_value).
+// their values are in the split-exact TF32 form (tf32_split_value), and the
+// FP32 V of the pairs of one source box are stored one after the other.
 template <typename FT, bool IS_U>
 __host__ __device__ __forceinline__ int64_t fac_idx(int64_t i, int l, int r, int64_t n) {
   if (sizeof(FT) == 8) return (int64_t)l * n + i;
@@ -96,10 +97,12 @@ struct TcBuffers {
   int max_slice;
   const float* knear;        // FP32 near-field blocks (launch_near_blocks)
   const int64_t* near_off;   // 27 per leaf: block offsets, -1 for no neighbour
-  // 2D tensor maps (CUtensorMap, 128 bytes each) of the FP32 operands A:
-  // umaps[p]: U_p as n x round4(r), box 32 x 128; vmaps[p]: V_p as
-  // r x round4(m), box 32 x 8; nmaps[27 k + s]: near-field block s of leaf k
-  // as nk x round4(ne), box 32 x 128.  128-byte swizzle, zero fill.
+  // 2D tensor maps (CUtensorMap, 128 bytes each) of the FP32 operands A, box
+  // 32 x 128, 128-byte swizzle, zero fill: umaps[p]: U_p as n x round4(r);
+  // vmaps[b] (boxes of all levels numbered together): the V of the pairs
+  // whose source is box b, stacked in the order of its reverse list, as
+  // (sum of ranks) x round4(m); nmaps[27 k + s]: near-field block s of leaf k
+  // as nk x round4(ne).
   const void* umaps;
   const void* vmaps;
   const void* nmaps;

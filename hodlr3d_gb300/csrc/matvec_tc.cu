@@ -5,9 +5,10 @@
 //
 //   ta_slice  per (level d-1 box "slice", share of its row tiles): T of the
 //             pairs of levels 1..d-1 whose input box contains the slice, as a
-//             tall GEMM [V_p1^T; V_p2^T; ...] X_slice (M = pair columns packed
-//             in groups of 8 rows, tiles of 128 rows, K = slice points); level
-//             d-1 pairs get T, the pairs above get slice partials
+//             tall GEMM [V_p1^T; V_p2^T; ...] X_slice per level (M = the pair
+//             columns of the source box, stored one after the other, in tiles
+//             of 128 rows, K = slice points); level d-1 pairs get T, the pairs
+//             above get slice partials
 //   tred      compensated sum of the slice partials
 //   ta_leaf   per input leaf: the same for the leaf-level pairs
 //   ut_tc     per (slice, 128 rows): long-K GEMM over the pairs of levels < d,
@@ -80,9 +81,7 @@ constexpr int kAhead = kSlots - kABuf;     // B chunks in flight ahead of the sp
 constexpr int TAB_OFF = kSlots * SLOT_BYTES;
 constexpr int kMaxEntries = 768;           // table entries (pairs, near blocks) of one block
 constexpr int ENTRY_BYTES = 32;
-constexpr int RING_OFF = TAB_OFF + kMaxEntries * ENTRY_BYTES + (kMaxEntries + 1) * 4;
-constexpr int kRing = 16;                  // tiles whose 8-row groups the T kernels keep
-constexpr int SMEM_BYTES = RING_OFF + kRing * 16 * 4;
+constexpr int SMEM_BYTES = TAB_OFF + kMaxEntries * ENTRY_BYTES + (kMaxEntries + 1) * 4;
 constexpr uint32_t kWaitLimit = 1u << 17;   // polls of up to kWaitHintNs each: about 1 s
 constexpr uint32_t kWaitHintNs = 8192;
 constexpr uint32_t IDESC64 = tc::idesc_tf32(128, 2 * NR);
@@ -161,17 +160,15 @@ struct Item {
 };
 static_assert(sizeof(Item) == ENTRY_BYTES, "entry");
 
-// A table entry of the T kernels: pair column l is row l of map (the pair's V
-// as an r x round4(m) tensor) read from column ro on; its output (c, l) goes to
-// dst[c * ld + l].  t: dst is T (split-exact, zero padded to ld), else a
-// slice partial (FP32).
+// A table entry of the T kernels: its output (c, l), l < r, goes to
+// dst[c * ld + l]; t: dst is T (split-exact, zero padded to ld), else a slice
+// partial (FP32).
 struct PairRow {
-  const CUtensorMap* map;
   float* dst;
-  int ro;
   int r;
   int ld;
   int t;
+  int pad[3];
 };
 static_assert(sizeof(PairRow) == ENTRY_BYTES, "entry");
 
@@ -434,43 +431,46 @@ __device__ __forceinline__ int upper_index(const int* cum, int n, int v) {
 // ---------------------------------------------------------------------------
 // Phase A: T = [V_p^T] X over one input box.  SLICE: the pairs of levels
 // 1..d-1 over a level d-1 box; otherwise the leaf-level pairs over a leaf.
-// Pair p occupies ceil(r_p / 8) groups of 8 rows; a tile is 16 groups.
+// The pairs of a level are the rows of their source box's V (one tensor map);
+// a tile is 128 of those rows, tiles of the levels one after the other.
+// lv[0][j]: first table entry of level j (lv[0][nlev] = n); lv[1][j]: first
+// tile of level j (lv[1][nlev] = all tiles); lv[2][j]: column of the input
+// box within the source box; lv[3][j]: the source box (all levels numbered
+// together).
+constexpr int kMaxLevels = 16;
 struct SrcTa {
   const PairRow* tab;
-  const int* cumg;   // groups before each entry
-  int* ring;         // [kRing][16]: entry << 8 | group within the pair, of tile t % kRing
-  int n, ngroups;
+  const int* cum;  // ranks before each entry
+  const int (*lv)[kMaxLevels + 1];
+  const CUtensorMap* vmaps;
+  int n, nlev;
   int tile0, tstep, ntile, cpt;
   int kin;
   const float* b;
   int64_t bs;
-  // producer state (per lane): the group of the current tile this lane copies
-  int pk = 0, pc = 0, png = 0;
-  const CUtensorMap* gmap = nullptr;
-  int gx = 0, gy = 0;
+  // producer state (lane 0): the box of its current tile
+  int pk = 0, pc = 0, px = 0, py = 0;
+  const CUtensorMap* pmap = nullptr;
   // worker state
   int wk = 0;
 
+  __device__ int level_of(int tg) const {
+    int j = 0;
+    while (j + 1 < nlev && lv[1][j + 1] <= tg) ++j;
+    return j;
+  }
   __device__ void produce(int, unsigned char* a, uint64_t* full, int lane) {
-    if (pk == 0) {  // a new tile: lane i looks up its group
-      const int g0 = (tile0 + pc * tstep) * 16;
-      png = min(16, ngroups - g0);
-      if (lane < png) {
-        const int idx = upper_index(cumg, n, g0 + lane);
-        gmap = tab[idx].map;
-        gx = tab[idx].ro;
-        gy = (g0 + lane - cumg[idx]) * 8;
-        // for the workers' finish of this tile (read kRing / cpt chunks later at most)
-        ring[(pc % kRing) * 16 + lane] = (idx << 8) | (g0 + lane - cumg[idx]);
-      }
-      __syncwarp();  // the ring entries before lane 0's arrival (release) below
+    if (lane != 0) return;
+    if (pk == 0) {
+      const int tg = tile0 + pc * tstep;
+      const int j = level_of(tg);
+      pmap = vmaps + lv[3][j];
+      px = lv[2][j];
+      py = (tg - lv[1][j]) * 128;
     }
-    if (lane == 0) expect_tx(full, 2048u * (uint32_t)png);
-    __syncwarp();
-    if (lane < png) {
-      tma_load_2d(a + 1024 * lane, gmap, gx + pk, gy, full);
-      tma_load_2d(a + A_HALF + 1024 * lane, gmap, gx + pk + 32, gy, full);
-    }
+    expect_tx(full, (uint32_t)A_BYTES);
+    tma_load_2d(a, pmap, px + pk, py, full);
+    tma_load_2d(a + A_HALF, pmap, px + pk + 32, py, full);
     pk += KC;
     if (pk >= cpt * KC) {
       pk = 0;
@@ -485,30 +485,31 @@ struct SrcTa {
     if (wk >= cpt * KC) wk = 0;
   }
   __device__ void finish(int t, const float* sum, const float* comp, const float* cross) const {
-    const int R = threadIdx.x & 127;
-    const int gi = (tile0 + t * tstep) * 16 + (R >> 3);
-    if (gi >= ngroups) return;
-    const int code = ring[(t % kRing) * 16 + (R >> 3)];
-    const PairRow& e = tab[code >> 8];
-    const int l = (code & 255) * 8 + (R & 7);
-    if (l >= e.r) return;
+    const int tg = tile0 + t * tstep;
+    const int j = level_of(tg);
+    const int rho = (tg - lv[1][j]) * 128 + (threadIdx.x & 127);
+    const int base = cum[lv[0][j]];
+    if (base + rho >= cum[lv[0][j + 1]]) return;
+    const int idx = upper_index(cum, n, base + rho);
+    const PairRow& e = tab[idx];
+    const int l = base + rho - cum[idx];
     const int c0 = (threadIdx.x >> 7) * NCOL;
     if (!e.t) {  // slice partial
 #pragma unroll
-      for (int j = 0; j < NCOL; ++j) e.dst[(int64_t)(c0 + j) * e.ld + l] = (sum[j] - comp[j]) + cross[j];
+      for (int j2 = 0; j2 < NCOL; ++j2) e.dst[(int64_t)(c0 + j2) * e.ld + l] = (sum[j2] - comp[j2]) + cross[j2];
       return;
     }
     // T in the split-exact form, zero padded to ld
 #pragma unroll
-    for (int j = 0; j < NCOL; ++j) {
-      const float v = (sum[j] - comp[j]) + cross[j];
+    for (int j2 = 0; j2 < NCOL; ++j2) {
+      const float v = (sum[j2] - comp[j2]) + cross[j2];
       const float hi = tf32_rz(v);
-      e.dst[(int64_t)(c0 + j) * e.ld + l] = hi + tf32_rn(v - hi);
+      e.dst[(int64_t)(c0 + j2) * e.ld + l] = hi + tf32_rn(v - hi);
     }
     if (l == e.r - 1)
       for (int lp = e.r; lp < e.ld; ++lp)
 #pragma unroll
-        for (int j = 0; j < NCOL; ++j) e.dst[(int64_t)(c0 + j) * e.ld + lp] = 0.f;
+        for (int j2 = 0; j2 < NCOL; ++j2) e.dst[(int64_t)(c0 + j2) * e.ld + lp] = 0.f;
   }
 };
 
@@ -520,9 +521,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_ta_tc(FarOp op, const CUtensorMa
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ uint64_t bar[NBAR];
   __shared__ uint32_t tslot;
-  PairRow* tab = reinterpret_cast<PairRow*>(smem + TAB_OFF);
-  int* cumg = reinterpret_cast<int*>(smem + TAB_OFF + kMaxEntries * ENTRY_BYTES);
+  __shared__ int lv[4][kMaxLevels + 1];
   if (smem_misaligned(smem, err)) return;
+  PairRow* tab = reinterpret_cast<PairRow*>(smem + TAB_OFF);
+  int* cum = reinterpret_cast<int*>(smem + TAB_OFF + kMaxEntries * ENTRY_BYTES);
   const int d = op.levels;
   const int64_t box = blockIdx.x;
   const int sh_in = SLICE ? 3 : 0;
@@ -530,6 +532,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_ta_tc(FarOp op, const CUtensorMa
   const int kin = (int)(i1 - i0);
   if (kin <= 0) return;
   const int jlo = SLICE ? 1 : d, jhi = SLICE ? d - 1 : d;
+  const int nlev = jhi - jlo + 1;
+  if (nlev > kMaxLevels) {
+    if (threadIdx.x == 0) atomicExch(err, 2);
+    return;
+  }
   int n = 0;
   for (int j = jlo; j <= jhi; ++j) {
     const int64_t gb = level_base(j) + (box >> (SLICE ? 3 * (d - 1 - j) : 0));
@@ -552,12 +559,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_ta_tc(FarOp op, const CUtensorMa
     const int p = op.rev[op.il_ptr[gb] + (idx - base)];
     const int up = SLICE ? 3 * (d - 1 - j) : 0;
     const int64_t a = box >> up;
-    const int64_t a0 = op.leaf_off[a << (3 * (d - j))];
     const int r = op.rank[p];
     PairRow e;
-    e.map = vmaps + p;
-    e.ro = (int)(i0 - a0);
     e.r = r;
+    e.pad[0] = e.pad[1] = e.pad[2] = 0;
     if (!SLICE || j == d - 1) {
       e.t = 1;
       e.ld = (r + 3) & ~3;
@@ -570,18 +575,37 @@ __global__ void __launch_bounds__(THREADS, 1) k_ta_tc(FarOp op, const CUtensorMa
     tab[idx] = e;
   }
   __syncthreads();
-  warp0_scan(n, [&](int i) { return (tab[i].r + 7) >> 3; }, cumg);
+  warp0_scan(n, [&](int i) { return tab[i].r; }, cum);
   __syncthreads();
-  const int ngroups = cumg[n];
-  const int ntiles_all = (ngroups + 15) / 16;
+  if (threadIdx.x == 0) {
+    int first = 0, tiles = 0;
+    for (int j = jlo; j <= jhi; ++j) {
+      const int k = j - jlo;
+      const int up = SLICE ? 3 * (d - 1 - j) : 0;
+      const int64_t a = box >> up;
+      const int64_t gb = level_base(j) + a;
+      const int cnt = (int)(op.il_ptr[gb + 1] - op.il_ptr[gb]);
+      lv[0][k] = first;
+      lv[1][k] = tiles;
+      lv[2][k] = (int)(i0 - op.leaf_off[a << (3 * (d - j))]);
+      lv[3][k] = (int)gb;
+      tiles += (cum[first + cnt] - cum[first] + 127) / 128;
+      first += cnt;
+    }
+    lv[0][nlev] = first;
+    lv[1][nlev] = tiles;
+  }
+  __syncthreads();
+  const int ntiles_all = lv[1][nlev];
   if ((int)blockIdx.y >= ntiles_all) return;
   const uint32_t tmem = block_setup(bar, &tslot);
   SrcTa src;
   src.tab = tab;
-  src.cumg = cumg;
-  src.ring = reinterpret_cast<int*>(smem + RING_OFF);
+  src.cum = cum;
+  src.lv = lv;
+  src.vmaps = vmaps;
   src.n = n;
-  src.ngroups = ngroups;
+  src.nlev = nlev;
   src.tile0 = blockIdx.y;
   src.tstep = gridDim.y;
   src.ntile = (ntiles_all - (int)blockIdx.y + (int)gridDim.y - 1) / (int)gridDim.y;
