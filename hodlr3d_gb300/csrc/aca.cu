@@ -263,8 +263,8 @@ __global__ void __launch_bounds__(BS) k_aca(const AcaTask* __restrict__ tasks, i
 // Copies the first r columns of U and V of every task into the final pools.
 // FP64 (at dst_off): U (n x r) then V (m x r), column-major.  FP32 (at
 // dst_off32, optional): U row-major with the rank padded to rp = round4(r),
-// padding zero -- every row starts on 16 bytes (the FP32 V is written after
-// the assembly, grouped by source box: launch_v32_grouped).
+// padding zero -- every row starts on 16 bytes (the hodlr3d assembly writes
+// its FP32 copies after the ACA instead, grouped by box: k_u32, k_v32).
 __global__ void k_aca_compact(const AcaTask* __restrict__ tasks, const int32_t* __restrict__ rank,
                               const int64_t* __restrict__ dst_off,
                               const int64_t* __restrict__ dst_off32, const double* __restrict__ ws,
@@ -284,6 +284,27 @@ __global__ void k_aca_compact(const AcaTask* __restrict__ tasks, const int32_t* 
     const int64_t i = e / rp;
     const int l = (int)(e - i * rp);
     u32[e] = l < r ? tf32_split_value(U[(int64_t)l * T.n + i]) : 0.f;
+  }
+}
+
+// FP32 U of every pair (split-exact form) from its FP64 U (n x r,
+// column-major): row-major with row stride us[p] (the sum of the padded ranks
+// of the pairs of its target box, whose U share the rows), its r columns
+// followed by zeros up to round4(r), at u32[p]; one block per pair.
+__global__ void k_u32(const double* const* __restrict__ u64, float* const* __restrict__ u32,
+                      const int32_t* __restrict__ nsize, const int32_t* __restrict__ us,
+                      const int32_t* __restrict__ rank) {
+  const int64_t p = blockIdx.x;
+  const int r = rank[p];
+  if (r <= 0) return;
+  const int rp = (r + 3) & ~3;
+  const int64_t n = nsize[p], st = us[p];
+  const double* src = u64[p];
+  float* dst = u32[p];
+  for (int64_t e = threadIdx.x; e < n * rp; e += blockDim.x) {
+    const int64_t i = e / rp;
+    const int l = (int)(e - i * rp);
+    dst[i * st + l] = l < r ? tf32_split_value(src[(int64_t)l * n + i]) : 0.f;
   }
 }
 
@@ -332,6 +353,13 @@ cudaError_t launch_aca_compact(cudaStream_t s, int ntasks, const AcaTask* tasks,
                                float* out32) {
   if (ntasks == 0) return cudaSuccess;
   k_aca_compact<<<ntasks, 256, 0, s>>>(tasks, rank, dst_off, dst_off32, ws, out64, out32);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_u32(cudaStream_t s, int64_t npairs, const double* const* u64, float* const* u32,
+                       const int32_t* nsize, const int32_t* us, const int32_t* rank) {
+  if (npairs <= 0) return cudaSuccess;
+  k_u32<<<(unsigned)npairs, 256, 0, s>>>(u64, u32, nsize, us, rank);
   return cudaGetLastError();
 }
 

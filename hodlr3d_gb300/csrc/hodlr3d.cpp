@@ -182,7 +182,16 @@ struct hodlr3d_handle {
   DevBuf* v32_pool = nullptr;
   std::vector<int64_t> h_vbox_off;
   std::vector<int32_t> h_vbox_rows;
-  DevBuf rank, u64, v64, u32, v32, tr_off, tr_off4, part_off, items, upper, pair_level;
+  // FP32 U of the pairs of each target box side by side: one row-major
+  // n_b x R_b matrix per box (R_b = sum of the padded ranks of its pairs) at
+  // u32_pool + h_ubox_off[b]; pair p at column h_coff[p], row stride
+  // h_ustride[p] = R_b.  The tensor-core T uses the same grouping: T of box b
+  // is 32 x R_b at 32-wide offset h_tbox_off[b].
+  DevBuf* u32_pool = nullptr;
+  std::vector<int64_t> h_ubox_off, h_tbox_off;
+  std::vector<int32_t> h_rbox, h_ustride, h_coff;
+  DevBuf ustride, tc_toff, tc_tld, tc_tbox, tc_rbox;
+  DevBuf rank, u64, v64, u32, v32, tr_off, part_off, items, upper, pair_level;
   int64_t sum_rank = 0, sum_rank4 = 0, part_total = 0, n_items = 0, n_upper = 0, factor_entries = 0;
   int tc_entries = 0;  // largest table of a tensor-core block
   int64_t u_entries = 0, v_entries = 0;
@@ -394,12 +403,17 @@ struct HostTask {
   bool leaf;
 };
 
-// FP32 copies of V grouped by source box: the pairs whose source is box b
-// (its reverse list) get consecutive column-major round4(m_b) x r blocks, so
-// that the V of all pairs of a source box form one (sum of ranks) x
-// round4(m_b) row-major matrix (one tensor map per box for the tensor-core
-// T kernels); converted from the FP64 factors after the assembly.
-int group_v32(hodlr3d_t h) {
+// FP32 copies of the factors (split-exact form), grouped by box:
+// * U by target box: the pairs of box b (consecutive pair numbers) side by
+//   side, U_p at columns [h_coff[p], + round4(r_p)) of one row-major
+//   n_b x R_b matrix;
+// * V by source box: the pairs whose source is box b (its reverse list) one
+//   after the other, consecutive column-major round4(m_b) x r blocks, so that
+//   they form one (sum of ranks) x round4(m_b) row-major matrix.
+// Per-pair pointers keep working for the CUDA-core kernels (U row stride
+// h_ustride[p]); the tensor-core kernels read one tensor map per box.
+// Converted from the FP64 factors after the assembly.
+int group_fp32(hodlr3d_t h) {
   const int64_t np = h->npairs;
   cudaStream_t s = h->stream;
   std::vector<int32_t> rev(std::max<int64_t>(np, 1));
@@ -408,44 +422,104 @@ int group_v32(hodlr3d_t h) {
   const int64_t nbox = (int64_t)h->h_il_ptr.size() - 1;
   h->h_vbox_off.assign(nbox + 1, 0);
   h->h_vbox_rows.assign(nbox, 0);
+  h->h_ubox_off.assign(nbox + 1, 0);
+  h->h_tbox_off.assign(nbox + 1, 0);
+  h->h_rbox.assign(nbox, 0);
+  h->h_ustride.assign(np, 0);
+  h->h_coff.assign(np, 0);
   std::vector<int64_t> voff(np, 0);
-  std::vector<int32_t> msize(np, 0);
-  int64_t cursor = 0;
+  std::vector<int32_t> msize(np, 0), nsize(np, 0);
+  int64_t vcur = 0, ucur = 0, tcur = 0;
   for (int64_t b = 0; b < nbox; ++b) {
     int j = 0;
     while (j < h->levels && h3d::level_base(j + 1) <= b) ++j;
     int64_t a0, a1;
     box_range(h, j, b - h3d::level_base(j), a0, a1);
     const int64_t m = a1 - a0, mp = (m + 3) & ~int64_t(3);
-    h->h_vbox_off[b] = cursor;
+    h->h_vbox_off[b] = vcur;
     for (int64_t q = h->h_il_ptr[b]; q < h->h_il_ptr[b + 1]; ++q) {
       const int p = rev[q];
-      voff[p] = cursor;
+      voff[p] = vcur;
       msize[p] = (int32_t)m;
-      cursor += (int64_t)h->h_rank[p] * mp;
+      vcur += (int64_t)h->h_rank[p] * mp;
       h->h_vbox_rows[b] += h->h_rank[p];
     }
+    // the pairs with target b are the pair numbers il_ptr[b] .. il_ptr[b+1]
+    int32_t R = 0;
+    for (int64_t p = h->h_il_ptr[b]; p < h->h_il_ptr[b + 1]; ++p) {
+      h->h_coff[p] = R;
+      nsize[p] = (int32_t)m;
+      R += (h->h_rank[p] + 3) & ~3;
+    }
+    h->h_rbox[b] = R;
+    for (int64_t p = h->h_il_ptr[b]; p < h->h_il_ptr[b + 1]; ++p) h->h_ustride[p] = R;
+    h->h_ubox_off[b] = ucur;
+    ucur += m * R;
+    h->h_tbox_off[b] = tcur;
+    tcur += 32 * (int64_t)R;
   }
-  h->h_vbox_off[nbox] = cursor;
+  h->h_vbox_off[nbox] = vcur;
+  h->h_ubox_off[nbox] = ucur;
+  h->h_tbox_off[nbox] = tcur;
   h->v32_pool = new DevBuf();
   h->pools.push_back(h->v32_pool);
-  H3D_CUDA(h->v32_pool->ensure(sizeof(float) * std::max<int64_t>(cursor, 4)));
-  float* base = h->v32_pool->as<float>();
-  for (int64_t p = 0; p < np; ++p) h->h_v32[p] = base + voff[p];
+  H3D_CUDA(h->v32_pool->ensure(sizeof(float) * std::max<int64_t>(vcur, 4)));
+  h->u32_pool = new DevBuf();
+  h->pools.push_back(h->u32_pool);
+  H3D_CUDA(h->u32_pool->ensure(sizeof(float) * std::max<int64_t>(ucur, 4)));
+  float* vbase = h->v32_pool->as<float>();
+  float* ubase = h->u32_pool->as<float>();
+  for (int64_t b = 0; b < nbox; ++b)
+    for (int64_t p = h->h_il_ptr[b]; p < h->h_il_ptr[b + 1]; ++p)
+      h->h_u32[p] = ubase + h->h_ubox_off[b] + h->h_coff[p];
+  for (int64_t p = 0; p < np; ++p) h->h_v32[p] = vbase + voff[p];
   if (np) {
-    DevBuf d64, d32, dm, dr;
+    DevBuf d64, d32, dm, dr, du64, du32, dn, dus;
     H3D_CUDA(d64.ensure(sizeof(void*) * np));
     H3D_CUDA(d32.ensure(sizeof(void*) * np));
     H3D_CUDA(dm.ensure(sizeof(int32_t) * np));
     H3D_CUDA(dr.ensure(sizeof(int32_t) * np));
+    H3D_CUDA(du64.ensure(sizeof(void*) * np));
+    H3D_CUDA(du32.ensure(sizeof(void*) * np));
+    H3D_CUDA(dn.ensure(sizeof(int32_t) * np));
+    H3D_CUDA(dus.ensure(sizeof(int32_t) * np));
     H3D_CUDA(cudaMemcpy(d64.p, h->h_v64.data(), sizeof(void*) * np, cudaMemcpyHostToDevice));
     H3D_CUDA(cudaMemcpy(d32.p, h->h_v32.data(), sizeof(void*) * np, cudaMemcpyHostToDevice));
     H3D_CUDA(cudaMemcpy(dm.p, msize.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice));
     H3D_CUDA(cudaMemcpy(dr.p, h->h_rank.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(cudaMemcpy(du64.p, h->h_u64.data(), sizeof(void*) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(cudaMemcpy(du32.p, h->h_u32.data(), sizeof(void*) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(cudaMemcpy(dn.p, nsize.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(cudaMemcpy(dus.p, h->h_ustride.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice));
     H3D_CUDA(h3d::launch_v32(s, np, d64.as<const double* const>(), d32.as<float* const>(),
                              dm.as<int32_t>(), dr.as<int32_t>()));
-    ++h->launches;
+    H3D_CUDA(h3d::launch_u32(s, np, du64.as<const double* const>(), du32.as<float* const>(),
+                             dn.as<int32_t>(), dus.as<int32_t>(), dr.as<int32_t>()));
+    h->launches += 2;
     H3D_CUDA(cudaStreamSynchronize(s));
+  }
+  // device tables: U row strides; tensor-core T offsets per pair and per box
+  std::vector<int64_t> toff(std::max<int64_t>(np, 1), 0);
+  std::vector<int32_t> tld(std::max<int64_t>(np, 1), 0);
+  for (int64_t b = 0; b < nbox; ++b)
+    for (int64_t p = h->h_il_ptr[b]; p < h->h_il_ptr[b + 1]; ++p) {
+      toff[p] = h->h_tbox_off[b] + h->h_coff[p];
+      tld[p] = h->h_rbox[b];
+    }
+  const size_t npb = std::max<int64_t>(np, 1), nbb = std::max<int64_t>(nbox, 1);
+  H3D_CUDA(h->ustride.ensure(sizeof(int32_t) * npb));
+  H3D_CUDA(h->tc_toff.ensure(sizeof(int64_t) * npb));
+  H3D_CUDA(h->tc_tld.ensure(sizeof(int32_t) * npb));
+  H3D_CUDA(h->tc_tbox.ensure(sizeof(int64_t) * nbb));
+  H3D_CUDA(h->tc_rbox.ensure(sizeof(int32_t) * nbb));
+  if (np) {
+    H3D_CUDA(cudaMemcpy(h->ustride.p, h->h_ustride.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(cudaMemcpy(h->tc_toff.p, toff.data(), sizeof(int64_t) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(cudaMemcpy(h->tc_tld.p, tld.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice));
+  }
+  if (nbox) {
+    H3D_CUDA(cudaMemcpy(h->tc_tbox.p, h->h_tbox_off.data(), sizeof(int64_t) * nbox, cudaMemcpyHostToDevice));
+    H3D_CUDA(cudaMemcpy(h->tc_rbox.p, h->h_rbox.data(), sizeof(int32_t) * nbox, cudaMemcpyHostToDevice));
   }
   return HODLR3D_OK;
 }
@@ -527,12 +601,7 @@ int run_aca_batch(hodlr3d_t h, std::vector<HostTask>& batch, std::vector<HostTas
   DevBuf* pool64 = new DevBuf();
   h->pools.push_back(pool64);
   H3D_CUDA(pool64->ensure(sizeof(double) * std::max<int64_t>(total, 1)));
-  DevBuf* pool32 = nullptr;
-  if (h->opt.keep_fp32) {
-    pool32 = new DevBuf();
-    h->pools.push_back(pool32);
-    H3D_CUDA(pool32->ensure(sizeof(float) * std::max<int64_t>(total32, 4)));
-  }
+  DevBuf* pool32 = nullptr;  // FP32 copies are written after the assembly, grouped by box
   DevBuf d_off32;
   H3D_CUDA(d_off.ensure(sizeof(int64_t) * nt));
   H3D_CUDA(d_off32.ensure(sizeof(int64_t) * nt));
@@ -551,7 +620,6 @@ int run_aca_batch(hodlr3d_t h, std::vector<HostTask>& batch, std::vector<HostTas
     double* base64 = pool64->as<double>() + dst[i];
     h->h_u64[p] = base64;
     h->h_v64[p] = base64 + (int64_t)r * batch[i].n;
-    if (pool32) h->h_u32[p] = pool32->as<float>() + dst32[i];
     const int32_t* pr = pvh.data() + tasks[i].piv_off;
     h->h_piv_rows[p].assign(pr, pr + r);
     h->h_piv_cols[p].assign(pr + tasks[i].cap, pr + tasks[i].cap + r);
@@ -574,6 +642,7 @@ int assemble(hodlr3d_t h) {
   for (DevBuf* b : h->pools) delete b;
   h->pools.clear();
   h->v32_pool = nullptr;
+  h->u32_pool = nullptr;
   h->aca_batches = 0;
   const int cap0 = h->opt.rank_cap > 0 ? h->opt.rank_cap : 256;
   std::vector<HostTask> todo;
@@ -621,18 +690,17 @@ int assemble(hodlr3d_t h) {
     }
     todo.swap(retry);
   }
-  if (h->opt.keep_fp32) H3D_TRY(group_v32(h));
+  if (h->opt.keep_fp32) H3D_TRY(group_fp32(h));
   // per-pair tables for the matvec: T offsets, slice work items of the
   // non-leaf pairs, partial offsets of the pairs above level d - 1
   const int d = h->levels;
-  std::vector<int64_t> tr(np), tr4(np), po(np, -1);
+  std::vector<int64_t> tr(np), po(np, -1);
   std::vector<int32_t> items, upper;
   int64_t acc = 0, acc4 = 0, pacc = 0, fe = 0, ue = 0, ve = 0;
   h->max_rank = 0;
   for (int64_t p = 0; p < np; ++p) {
     tr[p] = acc;
     acc += h->h_rank[p];
-    tr4[p] = acc4;
     acc4 += (h->h_rank[p] + 3) & ~3;
     h->max_rank = std::max(h->max_rank, h->h_rank[p]);
     const int j = h->h_pair_level[p];
@@ -694,7 +762,6 @@ int assemble(hodlr3d_t h) {
   H3D_CUDA(h->u32.ensure(sizeof(void*) * npb));
   H3D_CUDA(h->v32.ensure(sizeof(void*) * npb));
   H3D_CUDA(h->tr_off.ensure(sizeof(int64_t) * npb));
-  H3D_CUDA(h->tr_off4.ensure(sizeof(int64_t) * npb));
   H3D_CUDA(h->part_off.ensure(sizeof(int64_t) * npb));
   H3D_CUDA(h->items.ensure(sizeof(int32_t) * std::max<size_t>(items.size(), 2)));
   H3D_CUDA(h->upper.ensure(sizeof(int32_t) * std::max<size_t>(upper.size(), 1)));
@@ -706,7 +773,6 @@ int assemble(hodlr3d_t h) {
     H3D_CUDA(cudaMemcpyAsync(h->u32.p, h->h_u32.data(), sizeof(void*) * np, cudaMemcpyHostToDevice, s));
     H3D_CUDA(cudaMemcpyAsync(h->v32.p, h->h_v32.data(), sizeof(void*) * np, cudaMemcpyHostToDevice, s));
     H3D_CUDA(cudaMemcpyAsync(h->tr_off.p, tr.data(), sizeof(int64_t) * np, cudaMemcpyHostToDevice, s));
-    H3D_CUDA(cudaMemcpyAsync(h->tr_off4.p, tr4.data(), sizeof(int64_t) * np, cudaMemcpyHostToDevice, s));
     H3D_CUDA(cudaMemcpyAsync(h->part_off.p, po.data(), sizeof(int64_t) * np, cudaMemcpyHostToDevice, s));
     H3D_CUDA(cudaMemcpyAsync(h->pair_level.p, h->h_pair_level.data(), sizeof(int32_t) * np,
                              cudaMemcpyHostToDevice, s));
@@ -743,10 +809,10 @@ int ensure_matvec_buffers(hodlr3d_t h, int nrhs) {
 }
 
 // Tensor maps (2D tiled, FP32, 128-byte swizzle, zero fill outside) of the
-// tensor-core engine's A operands, box 32 x 128: per pair U_p (n x round4(r)),
-// per source box the V of its pairs (sum of ranks x round4(m)), per leaf and
-// neighbour slot the near-field block (nk x round4(ne)).  Maps of empty
-// operands stay zero and are never used.
+// tensor-core engine's A operands, box 32 x 128: per target box the U of its
+// pairs side by side (n x R_b), per source box the V of its pairs (sum of
+// ranks x round4(m)), per leaf and neighbour slot the near-field block
+// (nk x round4(ne)).  Maps of empty operands stay zero and are never used.
 int build_tensor_maps(hodlr3d_t h, const std::vector<int64_t>& near_off) {
   static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
   if (!encode) {
@@ -756,8 +822,8 @@ int build_tensor_maps(hodlr3d_t h, const std::vector<int64_t>& near_off) {
     if (!encode || q != cudaDriverEntryPointSuccess)
       return set_error(HODLR3D_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
   }
-  const int64_t np = h->npairs, nbox = (int64_t)h->h_vbox_rows.size();
-  const int64_t nm = np + nbox + 27 * h->nleaf;
+  const int64_t nbox = (int64_t)h->h_vbox_rows.size();
+  const int64_t nm = 2 * nbox + 27 * h->nleaf;
   std::vector<CUtensorMap> maps((size_t)std::max<int64_t>(nm, 1));
   std::memset(maps.data(), 0, sizeof(CUtensorMap) * maps.size());
   std::atomic<int> bad{0};
@@ -783,22 +849,16 @@ int build_tensor_maps(hodlr3d_t h, const std::vector<int64_t>& near_off) {
   for (int t = 0; t < nthr; ++t)
     th.emplace_back([&, t] {
       cudaSetDevice(h->opt.device);  // the encoder wants the device's context current
-      for (int64_t p = t; p < np; p += nthr) {
-        const int r = h->h_rank[p];
-        if (r <= 0) continue;
-        const int j = h->h_pair_level[p];
-        int64_t a0, a1;
-        box_range(h, j, h->h_pair_tgt[p] - h3d::level_base(j), a0, a1);
-        enc(&maps[p], h->h_u32[p], (r + 3) & ~3, a1 - a0, 128);
-      }
       for (int64_t b = t; b < nbox; b += nthr) {
-        if (h->h_vbox_rows[b] <= 0) continue;
         int j = 0;
         while (j < h->levels && h3d::level_base(j + 1) <= b) ++j;
         int64_t b0, b1;
         box_range(h, j, b - h3d::level_base(j), b0, b1);
-        enc(&maps[np + b], h->v32_pool->as<float>() + h->h_vbox_off[b], ((b1 - b0) + 3) & ~int64_t(3),
-            h->h_vbox_rows[b], 128);
+        if (h->h_rbox[b] > 0)
+          enc(&maps[b], h->u32_pool->as<float>() + h->h_ubox_off[b], h->h_rbox[b], b1 - b0, 128);
+        if (h->h_vbox_rows[b] > 0)
+          enc(&maps[nbox + b], h->v32_pool->as<float>() + h->h_vbox_off[b],
+              ((b1 - b0) + 3) & ~int64_t(3), h->h_vbox_rows[b], 128);
       }
       for (int64_t k = t; k < h->nleaf; k += nthr) {
         const int64_t nk = h->h_leaf_off[k + 1] - h->h_leaf_off[k];
@@ -807,7 +867,7 @@ int build_tensor_maps(hodlr3d_t h, const std::vector<int64_t>& near_off) {
           if (off < 0) continue;
           const int64_t nn = sl < 26 ? h->h_nbr_leaf[26 * k + sl] : k;
           const int64_t ne = h->h_leaf_off[nn + 1] - h->h_leaf_off[nn];
-          enc(&maps[np + nbox + 27 * k + sl], knear + off, (ne + 3) & ~int64_t(3), nk, 128);
+          enc(&maps[2 * nbox + 27 * k + sl], knear + off, (ne + 3) & ~int64_t(3), nk, 128);
         }
       }
     });
@@ -846,7 +906,11 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
   far.pair_tgt = h->pair_tgt.as<int32_t>();
   far.pair_src = h->pair_src.as<int32_t>();
   far.tr_off = h->tr_off.as<int64_t>();
-  far.tr_off4 = h->tr_off4.as<int64_t>();
+  far.ustride = h->ustride.as<int32_t>();
+  far.tc_toff = h->tc_toff.as<int64_t>();
+  far.tc_tld = h->tc_tld.as<int32_t>();
+  far.tc_tbox = h->tc_tbox.as<int64_t>();
+  far.tc_rbox = h->tc_rbox.as<int32_t>();
   far.part_off = h->part_off.as<int64_t>();
   far.ufac = f32 ? h->u32.as<const void*>() : h->u64.as<const void*>();
   far.vfac = f32 ? h->v32.as<const void*>() : h->v64.as<const void*>();
@@ -931,9 +995,10 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
     T.knear = h->knear.as<float>();
     T.near_off = h->near_off.as<int64_t>();
     const CUtensorMap* tm = h->tmaps.as<CUtensorMap>();
+    const int64_t nbox = (int64_t)h->h_vbox_rows.size();
     T.umaps = tm;
-    T.vmaps = tm + h->npairs;
-    T.nmaps = tm + h->npairs + (int64_t)h->h_vbox_rows.size();
+    T.vmaps = tm + nbox;
+    T.nmaps = tm + 2 * nbox;
     for (int c0 = 0; c0 < nrhs; c0 += 32)
       h->launches += h3d::launch_matvec_tc(s, h->N, h->perm.as<int32_t>(), far, nr, T, x + c0 * ld,
                                            ld, y + c0 * ld, ld, std::min(32, nrhs - c0),
@@ -1206,7 +1271,11 @@ int hodlr3d_matvec_noalloc(hodlr3d_t h, const double* x, double* y, int nrhs, in
   far.pair_tgt = h->pair_tgt.as<int32_t>();
   far.pair_src = h->pair_src.as<int32_t>();
   far.tr_off = h->tr_off.as<int64_t>();
-  far.tr_off4 = h->tr_off4.as<int64_t>();
+  far.ustride = h->ustride.as<int32_t>();
+  far.tc_toff = h->tc_toff.as<int64_t>();
+  far.tc_tld = h->tc_tld.as<int32_t>();
+  far.tc_tbox = h->tc_tbox.as<int64_t>();
+  far.tc_rbox = h->tc_rbox.as<int32_t>();
   far.part_off = h->part_off.as<int64_t>();
   far.ufac = f32 ? h->u32.as<const void*>() : h->u64.as<const void*>();
   far.vfac = f32 ? h->v32.as<const void*>() : h->v64.as<const void*>();

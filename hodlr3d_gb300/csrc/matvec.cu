@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(256) k_vtx(FarOp op, const int32_t* __restrict
       for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
         const int ll = e >> 6, ii = e & 63;
         fs[ll][ii] = (l0 + ll < r && ii < ni)
-                         ? F[fac_idx<FT, TRANS>((i0 - box0) + ii, l0 + ll, r, ld)]
+                         ? F[fac_idx<FT, TRANS>((i0 - box0) + ii, l0 + ll, r, ld, (sizeof(FT) == 4 ? (int64_t)op.ustride[p] : 0))]
                          : (FT)0;
       }
       for (int e = threadIdx.x; e < 64 * NR; e += blockDim.x) {
@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(256) k_ut(FarOp op, const FT* __restrict__ T,
           if (live) {
 #pragma unroll 4
             for (int l = 0; l < nl; ++l) {
-              const FT u = F[fac_idx<FT, !TRANS>(row - box0, l0 + l, r, ld)];
+              const FT u = F[fac_idx<FT, !TRANS>(row - box0, l0 + l, r, ld, (sizeof(FT) == 4 ? (int64_t)op.ustride[p] : 0))];
 #pragma unroll
               for (int c = 0; c < C::CG; ++c) part[c] += u * ts[l][g * C::CG + c];
             }
@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(256) k_leaf(FarOp op, NearOp nr, const FT* __r
           __syncthreads();
           for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
             const int ll = e >> 6, ii = e & 63;
-            fs[ll][ii] = (ll < nl && ii < na) ? Fin[fac_idx<FT, TRANS>(a0 + ii, l0 + ll, r, ni)] : (FT)0;
+            fs[ll][ii] = (ll < nl && ii < na) ? Fin[fac_idx<FT, TRANS>(a0 + ii, l0 + ll, r, ni, (sizeof(FT) == 4 ? (int64_t)op.ustride[p] : 0))] : (FT)0;
           }
           for (int e = threadIdx.x; e < 64 * NR; e += blockDim.x) {
             const int ii = e / NR, c = e - ii * NR;
@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(256) k_leaf(FarOp op, NearOp nr, const FT* __r
         if (live) {
 #pragma unroll 4
           for (int l = 0; l < nl; ++l) {
-            const FT u = Fout[fac_idx<FT, !TRANS>(row - t0, l0 + l, r, t1 - t0)];
+            const FT u = Fout[fac_idx<FT, !TRANS>(row - t0, l0 + l, r, t1 - t0, (sizeof(FT) == 4 ? (int64_t)op.ustride[p] : 0))];
 #pragma unroll
             for (int c = 0; c < C::CG; ++c) part[c] += u * ts[l][g * C::CG + c];
           }

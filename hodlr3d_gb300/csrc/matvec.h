@@ -23,7 +23,14 @@ struct FarOp {
   const int32_t* pair_src;
   const int64_t* tr_off;      // per pair: offset of its r rows in T (times the padded nrhs)
   const int64_t* part_off;    // per pair above level d - 1: offset of its slice partials
-  const int64_t* tr_off4;     // per pair: offset of its round4(r) rows in the tensor-core T
+  const int32_t* ustride;     // per pair: row stride of its FP32 U (the FP32 U of a box share rows)
+  // tensor-core T, grouped by target box: box b's T is 32 x R_b (R_b = sum of
+  // round4(r) over its pairs) at tc_tbox[b], element (c, k) at + c R_b + k;
+  // pair p's columns start at tc_toff[p] (row stride tc_tld[p] = R_b)
+  const int64_t* tc_toff;
+  const int32_t* tc_tld;
+  const int64_t* tc_tbox;
+  const int32_t* tc_rbox;
   const void* const* ufac;    // per pair U pointer (double* or float*)
   const void* const* vfac;    // per pair V pointer
 };
@@ -67,22 +74,24 @@ int padded_nrhs(int nrhs);
 
 // Index of element (i, l) of a pair's factor with rank r over a box of n
 // points.  FP64 factors are column-major with leading dimension n.  In the
-// FP32 copies U is row-major with the rank padded to a multiple of 4 and V is
+// FP32 copies U is row-major with row stride us (the FP32 U of the pairs of a
+// target box sit side by side, each rank padded to a multiple of 4) and V is
 // column-major with n padded to a multiple of 4 (zero padding), so that every
 // row of U and column of V starts on 16 bytes for the tensor-core kernels;
 // their values are in the split-exact TF32 form (tf32_split_value), and the
 // FP32 V of the pairs of one source box are stored one after the other.
 template <typename FT, bool IS_U>
-__host__ __device__ __forceinline__ int64_t fac_idx(int64_t i, int l, int r, int64_t n) {
+__host__ __device__ __forceinline__ int64_t fac_idx(int64_t i, int l, int r, int64_t n, int64_t us) {
   if (sizeof(FT) == 8) return (int64_t)l * n + i;
-  if (IS_U) return i * (int64_t)((r + 3) & ~3) + l;
+  if (IS_U) return i * us + l;
   return (int64_t)l * ((n + 3) & ~3) + i;
 }
 
 // Work buffers of the tensor-core form (32 right-hand sides, FP32):
 // xt: 32 * N floats, X in tree order, x(t, c) at xt[c N + t]; t: 32 * sum of
-// round4(rank) floats, pair p's T_p (c, l) at t[32 tr_off4[p] + c round4(r) + l],
-// zero padded; both in the split-exact TF32 form.  p: 32 * part_total floats;
+// round4(rank) floats, pair p's T_p (c, l) at t[tc_toff[p] + c tc_tld[p] + l],
+// zero padded (grouped by target box: FarOp::tc_*); both in the
+// split-exact TF32 form.  p: 32 * part_total floats;
 // ynl: 32 * N doubles;
 // err: device flag, 1 when an mbarrier wait gave up, 2 when a block's table
 // exceeded tc_max_entries().
@@ -98,11 +107,12 @@ struct TcBuffers {
   const float* knear;        // FP32 near-field blocks (launch_near_blocks)
   const int64_t* near_off;   // 27 per leaf: block offsets, -1 for no neighbour
   // 2D tensor maps (CUtensorMap, 128 bytes each) of the FP32 operands A, box
-  // 32 x 128, 128-byte swizzle, zero fill: umaps[p]: U_p as n x round4(r);
-  // vmaps[b] (boxes of all levels numbered together): the V of the pairs
-  // whose source is box b, stacked in the order of its reverse list, as
-  // (sum of ranks) x round4(m); nmaps[27 k + s]: near-field block s of leaf k
-  // as nk x round4(ne).
+  // 32 x 128, 128-byte swizzle, zero fill; boxes of all levels numbered
+  // together: umaps[b]: the U of the pairs of target box b side by side, as
+  // n x R_b (FarOp::tc_rbox); vmaps[b]: the V of the pairs whose source is box
+  // b, stacked in the order of its reverse list, as (sum of ranks) x
+  // round4(m); nmaps[27 k + s]: near-field block s of leaf k as
+  // nk x round4(ne).
   const void* umaps;
   const void* vmaps;
   const void* nmaps;

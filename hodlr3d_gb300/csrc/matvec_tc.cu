@@ -161,8 +161,8 @@ struct Item {
 static_assert(sizeof(Item) == ENTRY_BYTES, "entry");
 
 // A table entry of the T kernels: its output (c, l), l < r, goes to
-// dst[c * ld + l]; t: dst is T (split-exact, zero padded to ld), else a slice
-// partial (FP32).
+// dst[c * ld + l]; t: dst is T (split-exact, zero padded to round4(r)), else
+// a slice partial (FP32).
 struct PairRow {
   float* dst;
   int r;
@@ -507,7 +507,7 @@ struct SrcTa {
       e.dst[(int64_t)(c0 + j2) * e.ld + l] = hi + tf32_rn(v - hi);
     }
     if (l == e.r - 1)
-      for (int lp = e.r; lp < e.ld; ++lp)
+      for (int lp = e.r; lp < ((e.r + 3) & ~3); ++lp)
 #pragma unroll
         for (int j2 = 0; j2 < NCOL; ++j2) e.dst[(int64_t)(c0 + j2) * e.ld + lp] = 0.f;
   }
@@ -565,8 +565,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_ta_tc(FarOp op, const CUtensorMa
     e.pad[0] = e.pad[1] = e.pad[2] = 0;
     if (!SLICE || j == d - 1) {
       e.t = 1;
-      e.ld = (r + 3) & ~3;
-      e.dst = T + op.tr_off4[p] * NR;
+      e.ld = op.tc_tld[p];
+      e.dst = T + op.tc_toff[p];
     } else {
       e.t = 0;
       e.ld = r;
@@ -625,13 +625,14 @@ __global__ void k_tred_tc(FarOp op, const int32_t* __restrict__ pairs, const flo
   const int r = op.rank[p], rp = (r + 3) & ~3;
   const int64_t ns = int64_t(1) << (3 * (op.levels - 1 - op.pair_level[p]));
   const float* src = Pp + op.part_off[p] * NR;
-  float* dst = T + op.tr_off4[p] * NR;
+  float* dst = T + op.tc_toff[p];
+  const int64_t ld = op.tc_tld[p];
   for (int o = threadIdx.x; o < rp * NR; o += blockDim.x) {
     const int c = o / rp, l = o - c * rp;
     float sum = 0.f, comp = 0.f;
     if (l < r)
       for (int64_t s = 0; s < ns; ++s) kahan_add(sum, comp, src[s * r * NR + c * r + l]);
-    dst[o] = tf32_split_value((double)sum - (double)comp);
+    dst[c * ld + l] = tf32_split_value((double)sum - (double)comp);
   }
 }
 
@@ -686,16 +687,16 @@ struct SrcItems {
   }
 };
 
-__device__ __forceinline__ Item pair_item(const FarOp& op, const CUtensorMap* umaps, int p, int y,
-                                          const float* T) {
-  const int r = op.rank[p];
-  const int rp = (r + 3) & ~3;
+// The item of all pairs of target box gb (all levels numbered together):
+// their U side by side (one tensor map), rows from y, times their T (32 x R).
+__device__ __forceinline__ Item box_item(const FarOp& op, const CUtensorMap* umaps, int64_t gb, int y,
+                                         const float* T) {
   Item it;
-  it.map = umaps + p;
+  it.map = umaps + gb;
   it.y = y;
-  it.b = T + op.tr_off4[p] * NR;
-  it.bs = rp;
-  it.blen = r > 0 ? rp : 0;
+  it.b = T + op.tc_tbox[gb];
+  it.bs = op.tc_rbox[gb];
+  it.blen = op.tc_rbox[gb];
   it.pad = 0;
   return it;
 }
@@ -729,27 +730,17 @@ __global__ void __launch_bounds__(THREADS, 1) k_ut_tc(FarOp op, const CUtensorMa
   const int64_t r0 = s0 + 128 * (int64_t)blockIdx.y;
   const int nrows = (int)min((int64_t)128, s1 - r0);
   if (nrows <= 0) return;
-  int n = 0;
-  for (int j = 1; j <= d - 1; ++j) {
-    const int64_t gb = level_base(j) + (sb >> (3 * (d - 1 - j)));
-    n += (int)(op.il_ptr[gb + 1] - op.il_ptr[gb]);
-  }
+  // one item per level: all pairs of the ancestor of the slice at that level
+  const int n = d - 1;
   if (n > kMaxEntries) {
     if (threadIdx.x == 0) atomicExch(err, 2);
     return;
   }
-  for (int idx = threadIdx.x; idx < n; idx += THREADS) {
-    int j = 1, base = 0;
-    int64_t gb = 0;
-    for (;; ++j) {
-      gb = level_base(j) + (sb >> (3 * (d - 1 - j)));
-      const int cnt = (int)(op.il_ptr[gb + 1] - op.il_ptr[gb]);
-      if (idx < base + cnt) break;
-      base += cnt;
-    }
+  if (threadIdx.x < n) {
+    const int j = 1 + threadIdx.x;
     const int64_t a = sb >> (3 * (d - 1 - j));
     const int64_t a0 = op.leaf_off[a << (3 * (d - j))];
-    items[idx] = pair_item(op, umaps, (int)(op.il_ptr[gb] + (idx - base)), (int)(r0 - a0), T);
+    items[threadIdx.x] = box_item(op, umaps, level_base(j) + a, (int)(r0 - a0), T);
   }
   __syncthreads();
   warp0_scan(n, [&](int i) { return (items[i].blen + KC - 1) / KC; }, cofs);
@@ -815,20 +806,15 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_tc(FarOp op, NearOp nr,
   const int64_t t0 = op.leaf_off[k];
   const int nk = (int)(op.leaf_off[k + 1] - t0);
   if (nk <= 0) return;
-  const int64_t lk = level_base(d) + k;
-  const int64_t q0 = op.il_ptr[lk];
-  const int npair = (int)(op.il_ptr[lk + 1] - q0);
-  const int n = npair + 27;
-  if (n > kMaxEntries) {
-    if (threadIdx.x == 0) atomicExch(err, 2);
-    return;
-  }
+  // items: all leaf-level pairs of the leaf (one item), then its 27 near-field
+  // blocks (neighbour slots 0..25, then the leaf itself)
+  const int n = 28;
   for (int i = threadIdx.x; i < n; i += THREADS) {
     Item it;
-    if (i < npair) {
-      it = pair_item(op, umaps, (int)(q0 + i), 0, T);
+    if (i == 0) {
+      it = box_item(op, umaps, level_base(d) + k, 0, T);
     } else {
-      const int sl = i - npair;  // neighbour slots 0..25, then the leaf itself
+      const int sl = i - 1;
       const int64_t nn = sl < 26 ? (int64_t)nr.nbr_leaf[k * 26 + sl] : k;
       it.map = nmaps + k * 27 + sl;
       it.b = Xt;
