@@ -451,8 +451,9 @@ struct SrcTa {
   // producer state (lane 0): the box of its current tile
   int pk = 0, pc = 0, px = 0, py = 0;
   const CUtensorMap* pmap = nullptr;
-  // worker state
-  int wk = 0;
+  // worker state: K offset of the next B copy; the level and table entry of
+  // this thread's row in the last finished tile (rows only move forward)
+  int wk = 0, flev = -1, fidx = 0;
 
   __device__ int level_of(int tg) const {
     int j = 0;
@@ -484,13 +485,18 @@ struct SrcTa {
     wk += KC;
     if (wk >= cpt * KC) wk = 0;
   }
-  __device__ void finish(int t, const float* sum, const float* comp, const float* cross) const {
+  __device__ void finish(int t, const float* sum, const float* comp, const float* cross) {
     const int tg = tile0 + t * tstep;
     const int j = level_of(tg);
     const int rho = (tg - lv[1][j]) * 128 + (threadIdx.x & 127);
     const int base = cum[lv[0][j]];
     if (base + rho >= cum[lv[0][j + 1]]) return;
-    const int idx = upper_index(cum, n, base + rho);
+    if (j != flev) {  // first tile of a level: search; later tiles: step forward
+      fidx = upper_index(cum, n, base + rho);
+      flev = j;
+    }
+    while (cum[fidx + 1] <= base + rho) ++fidx;
+    const int idx = fidx;
     const PairRow& e = tab[idx];
     const int l = base + rho - cum[idx];
     const int c0 = (threadIdx.x >> 7) * NCOL;
