@@ -314,7 +314,7 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
       const uint32_t ta = tmem + TM_A + TM_ASTRIDE * (uint32_t)(c % kABuf) + 16u * kq + lane_base;
       tc::tmem_st16(ta, hi);
       tc::tmem_st16(ta + (uint32_t)KC, lo);
-      if (copies_b) {
+      if (copies_b && src.fresh_b(c)) {
         // the B segment this thread copied: low part next to it
         unsigned char* sb = slot + m.offB;
         const float4 xb = *reinterpret_cast<const float4*>(sb);
@@ -455,6 +455,10 @@ struct SrcTa {
   // this thread's row in the last finished tile (rows only move forward)
   int wk = 0, flev = -1, fidx = 0;
 
+  // B is X over the input box: when kSlots is a multiple of cpt, slot s always
+  // holds K range s % cpt, so B is copied and split in the first kSlots chunks
+  // only and read from the slot afterwards
+  __device__ bool fresh_b(int c) const { return c < kSlots || kSlots % cpt != 0; }
   __device__ int level_of(int tg) const {
     int j = 0;
     while (j + 1 < nlev && lv[1][j + 1] <= tg) ++j;
@@ -478,10 +482,12 @@ struct SrcTa {
       ++pc;
     }
   }
-  __device__ void load_b(int, unsigned char* slot, const CopyMap& m) {
-    const int kb = wk + 4 * m.qb;
-    const bool ok = kb < kin;
-    cp_async16(slot + m.offB, ok ? b + m.cb * bs + kb : b, ok);
+  __device__ void load_b(int c, unsigned char* slot, const CopyMap& m) {
+    if (fresh_b(c)) {
+      const int kb = wk + 4 * m.qb;
+      const bool ok = kb < kin;
+      cp_async16(slot + m.offB, ok ? b + m.cb * bs + kb : b, ok);
+    }
     wk += KC;
     if (wk >= cpt * KC) wk = 0;
   }
@@ -656,6 +662,7 @@ struct SrcItems {
   int wi = -1, wk = 0, wbs = 0, wlen = 0;
   const float* wb = nullptr;
 
+  __device__ bool fresh_b(int) const { return true; }
   // next item with K after item i
   __device__ int next_item(int i) const {
     ++i;
