@@ -260,15 +260,12 @@ __global__ void __launch_bounds__(BS) k_aca(const AcaTask* __restrict__ tasks, i
   }
 }
 
-// Copies the first r columns of U and V of every task into the final pools.
-// FP64 (at dst_off): U (n x r) then V (m x r), column-major.  FP32 (at
-// dst_off32, optional): U row-major with the rank padded to rp = round4(r),
-// padding zero -- every row starts on 16 bytes (the hodlr3d assembly writes
-// its FP32 copies after the ACA instead, grouped by box: k_u32, k_v32).
+// Copies the first r columns of U and V of every task into the final FP64
+// pool at dst_off: U (n x r) then V (m x r), column-major.  (The FP32 copies
+// are written after the assembly, grouped by box: k_u32, k_v32.)
 __global__ void k_aca_compact(const AcaTask* __restrict__ tasks, const int32_t* __restrict__ rank,
-                              const int64_t* __restrict__ dst_off,
-                              const int64_t* __restrict__ dst_off32, const double* __restrict__ ws,
-                              double* __restrict__ out64, float* __restrict__ out32) {
+                              const int64_t* __restrict__ dst_off, const double* __restrict__ ws,
+                              double* __restrict__ out64) {
   const AcaTask T = tasks[blockIdx.x];
   const int r = rank[blockIdx.x];
   const double* U = ws + T.ws_off;
@@ -277,14 +274,6 @@ __global__ void k_aca_compact(const AcaTask* __restrict__ tasks, const int32_t* 
   const int64_t nu = (int64_t)r * T.n, nv = (int64_t)r * T.m;
   for (int64_t i = threadIdx.x; i < nu; i += blockDim.x) out64[o + i] = U[i];
   for (int64_t i = threadIdx.x; i < nv; i += blockDim.x) out64[o + nu + i] = V[i];
-  if (!out32) return;
-  const int rp = (r + 3) & ~3;
-  float* u32 = out32 + dst_off32[blockIdx.x];
-  for (int64_t e = threadIdx.x; e < (int64_t)T.n * rp; e += blockDim.x) {
-    const int64_t i = e / rp;
-    const int l = (int)(e - i * rp);
-    u32[e] = l < r ? tf32_split_value(U[(int64_t)l * T.n + i]) : 0.f;
-  }
 }
 
 // FP32 U of every pair (split-exact form) from its FP64 U (n x r,
@@ -348,11 +337,9 @@ cudaError_t launch_aca(cudaStream_t s, int block, int grid, const AcaTask* tasks
 }
 
 cudaError_t launch_aca_compact(cudaStream_t s, int ntasks, const AcaTask* tasks,
-                               const int32_t* rank, const int64_t* dst_off,
-                               const int64_t* dst_off32, const double* ws, double* out64,
-                               float* out32) {
-  if (ntasks == 0) return cudaSuccess;
-  k_aca_compact<<<ntasks, 256, 0, s>>>(tasks, rank, dst_off, dst_off32, ws, out64, out32);
+                               const int32_t* rank, const int64_t* dst_off, const double* ws,
+                               double* out64) {
+  k_aca_compact<<<ntasks, 256, 0, s>>>(tasks, rank, dst_off, ws, out64);
   return cudaGetLastError();
 }
 

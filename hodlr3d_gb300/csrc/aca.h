@@ -32,9 +32,8 @@ cudaError_t launch_aca(cudaStream_t s, int block, int grid, const AcaTask* tasks
                        unsigned char* flags, int32_t* piv, int32_t* out_rank, int32_t* out_status,
                        int cap_max);
 cudaError_t launch_aca_compact(cudaStream_t s, int ntasks, const AcaTask* tasks,
-                               const int32_t* rank, const int64_t* dst_off,
-                               const int64_t* dst_off32, const double* ws, double* out64,
-                               float* out32);
+                               const int32_t* rank, const int64_t* dst_off, const double* ws,
+                               double* out64);
 // FP32 U of every pair from its FP64 U (see k_u32 in aca.cu)
 cudaError_t launch_u32(cudaStream_t s, int64_t npairs, const double* const* u64, float* const* u32,
                        const int32_t* nsize, const int32_t* us, const int32_t* rank);

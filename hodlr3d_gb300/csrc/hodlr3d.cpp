@@ -579,8 +579,8 @@ int run_aca_batch(hodlr3d_t h, std::vector<HostTask>& batch, std::vector<HostTas
   H3D_CUDA(cudaStreamSynchronize(s));
   H3D_CUDA(cudaGetLastError());
   // finished tasks -> exact-size pools; capacity overflows -> retried with twice the capacity
-  std::vector<int64_t> dst(nt, 0), dst32(nt, 0);
-  int64_t total = 0, total32 = 0;
+  std::vector<int64_t> dst(nt, 0);
+  int64_t total = 0;
   for (int i = 0; i < nt; ++i) {
     if (st[i] == h3d::kAcaNonFinite)
       return set_error(HODLR3D_ERR_NONFINITE,
@@ -595,22 +595,15 @@ int run_aca_batch(hodlr3d_t h, std::vector<HostTask>& batch, std::vector<HostTas
     }
     dst[i] = total;
     total += (int64_t)rk[i] * (batch[i].n + batch[i].m);
-    dst32[i] = total32;
-    total32 += (int64_t)batch[i].n * ((rk[i] + 3) & ~3);
   }
   DevBuf* pool64 = new DevBuf();
   h->pools.push_back(pool64);
   H3D_CUDA(pool64->ensure(sizeof(double) * std::max<int64_t>(total, 1)));
-  DevBuf* pool32 = nullptr;  // FP32 copies are written after the assembly, grouped by box
-  DevBuf d_off32;
   H3D_CUDA(d_off.ensure(sizeof(int64_t) * nt));
-  H3D_CUDA(d_off32.ensure(sizeof(int64_t) * nt));
   H3D_CUDA(cudaMemcpyAsync(d_off.p, dst.data(), sizeof(int64_t) * nt, cudaMemcpyHostToDevice, s));
-  H3D_CUDA(cudaMemcpyAsync(d_off32.p, dst32.data(), sizeof(int64_t) * nt, cudaMemcpyHostToDevice, s));
   H3D_CUDA(cudaMemcpyAsync(d_rank.p, rk.data(), sizeof(int32_t) * nt, cudaMemcpyHostToDevice, s));
   H3D_CUDA(h3d::launch_aca_compact(s, nt, d_tasks.as<h3d::AcaTask>(), d_rank.as<int32_t>(),
-                                   d_off.as<int64_t>(), d_off32.as<int64_t>(), d_ws.as<double>(),
-                                   pool64->as<double>(), pool32 ? pool32->as<float>() : nullptr));
+                                   d_off.as<int64_t>(), d_ws.as<double>(), pool64->as<double>()));
   ++h->launches;
   for (int i = 0; i < nt; ++i) {
     if (st[i] == h3d::kAcaCapReached) continue;
