@@ -232,7 +232,7 @@ struct hodlr3d_handle {
   };
   bool profiling = false;
   Prof prof;
-  int engine = 0;   // 0 auto, 1 SIMT kernels, 2 tensor-core kernels
+  int engine = 0;   // 0 auto, 1 SIMT kernels, 2 tensor-core kernels, 3 few-column kernels
   DevBuf dev_err;   // set by kernels whose bounded waits gave up
   bool leaves_aligned = false;  // every leaf population a multiple of 4
   DevBuf knear, near_off;       // FP32 near-field blocks of the tensor-core engine
@@ -241,7 +241,14 @@ struct hodlr3d_handle {
   bool maps_built = false;
   bool near_built = false;
   std::vector<int32_t> h_nbr_leaf;  // host copy (tensor maps of the near-field blocks)
+  std::vector<int64_t> h_near_off;  // 27 per leaf: near-block offsets, -1 for no neighbour
   int64_t near_floats = 0;
+  // few-column engine (matvec_gemv.cu): tables over the grouped FP32 layouts
+  bool gemv_built = false;
+  bool gemv_ok = false;          // tree and layouts fit the few-column kernels
+  DevBuf gv_ubox_off, gv_vbox_off, gv_vbox_rows, gv_vrow0, gv_vrow_t, gv_tbase, gv_vpofs,
+      gv_upofs, gv_vt_items, gv_vt_upper, gv_ut_items, gv_ut_upper, gv_x, gv_t, gv_tt, gv_p, gv_pt;
+  int64_t gv_n_vt_items = 0, gv_n_vt_upper = 0, gv_n_ut_items = 0, gv_n_ut_upper = 0;
   // GMRES work buffers
   DevBuf g_Q, g_w, g_r, g_x, g_b, g_H, g_cs, g_sn, g_beta, g_hk, g_bnorm, g_err, g_part, g_y,
       g_kcol, g_brk, g_scal, g_d, g_coef;
@@ -782,6 +789,7 @@ int assemble(hodlr3d_t h) {
   // at the factors) are rebuilt on its next use
   h->near_built = false;
   h->maps_built = false;
+  h->gemv_built = false;
   h->assembled = true;
   h->assemble_seconds = now_s() - t_start;
   return HODLR3D_OK;
@@ -876,6 +884,148 @@ int build_tensor_maps(hodlr3d_t h, const std::vector<int64_t>& near_off) {
   return HODLR3D_OK;
 }
 
+// FP32 near-field blocks of every leaf (both FP32 engines), evaluated once
+// per assembly: leaf k, slot s (0..25 the neighbours, 26 itself) is a
+// row-major nk x round4(ne) block at h_near_off[27 k + s].
+int ensure_near_blocks(hodlr3d_t h, const h3d::NearOp& nr, cudaStream_t s) {
+  if (h->near_built) return HODLR3D_OK;
+  h->h_nbr_leaf.resize(26 * h->nleaf);
+  H3D_CUDA(cudaMemcpy(h->h_nbr_leaf.data(), h->nbr_leaf.p, sizeof(int32_t) * 26 * h->nleaf,
+                      cudaMemcpyDeviceToHost));
+  const std::vector<int32_t>& nbl = h->h_nbr_leaf;
+  std::vector<int64_t>& off = h->h_near_off;
+  off.assign(27 * h->nleaf, -1);
+  int64_t tot = 0;
+  for (int64_t k = 0; k < h->nleaf; ++k) {
+    const int64_t nk = h->h_leaf_off[k + 1] - h->h_leaf_off[k];
+    for (int sl = 0; sl < 27; ++sl) {
+      const int64_t nn = sl < 26 ? nbl[26 * k + sl] : k;
+      if (nn < 0) continue;
+      const int64_t ne = h->h_leaf_off[nn + 1] - h->h_leaf_off[nn];
+      off[27 * k + sl] = tot;
+      tot += nk * ((ne + 3) & ~int64_t(3));
+    }
+  }
+  H3D_CUDA(h->knear.ensure(sizeof(float) * std::max<int64_t>(tot, 4)));
+  H3D_CUDA(h->near_off.ensure(sizeof(int64_t) * off.size()));
+  H3D_CUDA(cudaMemcpy(h->near_off.p, off.data(), sizeof(int64_t) * off.size(),
+                      cudaMemcpyHostToDevice));
+  h->launches += h3d::launch_near_blocks(s, h->nleaf, h->leaf_off.as<int32_t>(), nr,
+                                         h->near_off.as<int64_t>(), h->knear.as<float>());
+  H3D_CUDA(cudaGetLastError());
+  h->near_floats = tot;
+  h->near_built = true;
+  h->maps_built = false;
+  return HODLR3D_OK;
+}
+
+// Work lists and index tables of the few-column engine (matvec_gemv.cu) over
+// the grouped FP32 layouts; leaves it off (gemv_ok false) when the tree does
+// not fit its shared memory or 32-bit row numbers.
+int ensure_gemv(hodlr3d_t h, cudaStream_t s) {
+  if (h->gemv_built) return HODLR3D_OK;
+  h->gemv_built = true;
+  h->gemv_ok = false;
+  const int ml4 = (h->max_leaf + 3) & ~3;
+  if (h3d::gemv_vy_smem(ml4, 4) > 200 * 1024) return HODLR3D_OK;
+  const int64_t np = h->npairs;
+  const int64_t nbox = (int64_t)h->h_vbox_rows.size();
+  const int64_t trows = h->h_tbox_off[nbox] / 32;
+  std::vector<int64_t> vrow0(nbox + 1, 0), tbase(nbox, 0), vpofs(nbox, -1), upofs(nbox, -1);
+  for (int64_t b = 0; b < nbox; ++b) {
+    tbase[b] = h->h_tbox_off[b] / 32;
+    vrow0[b + 1] = vrow0[b] + h->h_vbox_rows[b];
+  }
+  const int64_t vrows = vrow0[nbox];
+  if (trows >= INT32_MAX || vrows >= INT32_MAX) return HODLR3D_OK;
+  std::vector<int32_t> rev(std::max<int64_t>(np, 1)), tgt(std::max<int64_t>(np, 1));
+  if (np) H3D_CUDA(cudaMemcpy(rev.data(), h->rev.p, sizeof(int32_t) * np, cudaMemcpyDeviceToHost));
+  for (int64_t b = 0; b < nbox; ++b)
+    for (int64_t p = h->h_il_ptr[b]; p < h->h_il_ptr[b + 1]; ++p) tgt[p] = (int32_t)b;
+  std::vector<int32_t> vrow_t(std::max<int64_t>(vrows, 1));
+  std::vector<int32_t> vt_upper, ut_upper;
+  std::vector<int32_t> vt_items, ut_items;  // int4 / int2 records
+  int64_t pv = 0, pu = 0;
+  for (int64_t b = 0; b < nbox; ++b) {
+    int j = 0;
+    while (j < h->levels && h3d::level_base(j + 1) <= b) ++j;
+    int64_t a0, a1;
+    box_range(h, j, b - h3d::level_base(j), a0, a1);
+    const int64_t m = a1 - a0, m4 = (m + 3) & ~int64_t(3);
+    // V stack of b as a source box: rows map to T rows of the pairs' targets
+    int64_t v = vrow0[b];
+    for (int64_t q = h->h_il_ptr[b]; q < h->h_il_ptr[b + 1]; ++q) {
+      const int p = rev[q];
+      const int64_t base = tbase[tgt[p]] + h->h_coff[p];
+      for (int l = 0; l < h->h_rank[p]; ++l) vrow_t[v++] = (int32_t)(base + l);
+    }
+    const int rows = h->h_vbox_rows[b];
+    if (rows > 0 && m > 0) {
+      const int nch = (int)((m4 + h3d::kGemvCols - 1) / h3d::kGemvCols);
+      if (nch > 1) {
+        vpofs[b] = pv;
+        pv += (int64_t)rows * nch;
+        vt_upper.push_back((int32_t)b);
+      }
+      for (int ci = 0; ci < nch; ++ci)
+        for (int r0 = 0; r0 < rows; r0 += h3d::kGemvRowChunk) {
+          const int rec[4] = {(int32_t)b, ci, r0, std::min(h3d::kGemvRowChunk, rows - r0)};
+          vt_items.insert(vt_items.end(), rec, rec + 4);
+        }
+    }
+    // U of b as a target box
+    const int R = h->h_rbox[b];
+    if (R > 0 && m > 0) {
+      const int nch = (int)((m + h3d::kGemvRowsT - 1) / h3d::kGemvRowsT);
+      if (nch > 1) {
+        upofs[b] = pu;
+        pu += (int64_t)R * nch;
+        ut_upper.push_back((int32_t)b);
+      }
+      for (int ci = 0; ci < nch; ++ci) {
+        ut_items.push_back((int32_t)b);
+        ut_items.push_back(ci);
+      }
+    }
+  }
+  auto put = [](DevBuf& d, const void* src, size_t bytes) -> cudaError_t {
+    cudaError_t e = d.ensure(std::max<size_t>(bytes, 16));
+    if (e != cudaSuccess || bytes == 0) return e;
+    return cudaMemcpy(d.p, src, bytes, cudaMemcpyHostToDevice);
+  };
+  H3D_CUDA(put(h->gv_ubox_off, h->h_ubox_off.data(), sizeof(int64_t) * nbox));
+  H3D_CUDA(put(h->gv_vbox_off, h->h_vbox_off.data(), sizeof(int64_t) * nbox));
+  H3D_CUDA(put(h->gv_vbox_rows, h->h_vbox_rows.data(), sizeof(int32_t) * nbox));
+  H3D_CUDA(put(h->gv_vrow0, vrow0.data(), sizeof(int64_t) * (nbox + 1)));
+  H3D_CUDA(put(h->gv_vrow_t, vrow_t.data(), sizeof(int32_t) * vrows));
+  H3D_CUDA(put(h->gv_tbase, tbase.data(), sizeof(int64_t) * nbox));
+  H3D_CUDA(put(h->gv_vpofs, vpofs.data(), sizeof(int64_t) * nbox));
+  H3D_CUDA(put(h->gv_upofs, upofs.data(), sizeof(int64_t) * nbox));
+  H3D_CUDA(put(h->gv_vt_items, vt_items.data(), sizeof(int32_t) * vt_items.size()));
+  H3D_CUDA(put(h->gv_vt_upper, vt_upper.data(), sizeof(int32_t) * vt_upper.size()));
+  H3D_CUDA(put(h->gv_ut_items, ut_items.data(), sizeof(int32_t) * ut_items.size()));
+  H3D_CUDA(put(h->gv_ut_upper, ut_upper.data(), sizeof(int32_t) * ut_upper.size()));
+  h->gv_n_vt_items = (int64_t)vt_items.size() / 4;
+  h->gv_n_vt_upper = (int64_t)vt_upper.size();
+  h->gv_n_ut_items = (int64_t)ut_items.size() / 2;
+  h->gv_n_ut_upper = (int64_t)ut_upper.size();
+  H3D_CUDA(h->gv_x.ensure(sizeof(float) * 4 * h->N));
+  H3D_CUDA(h->gv_t.ensure(sizeof(float) * 4 * std::max<int64_t>(trows, 1)));
+  H3D_CUDA(cudaMemsetAsync(h->gv_t.p, 0, sizeof(float) * 4 * std::max<int64_t>(trows, 1), s));
+  H3D_CUDA(h->gv_tt.ensure(sizeof(float) * 4 * std::max<int64_t>(trows, 1)));
+  H3D_CUDA(h->gv_p.ensure(sizeof(float) * 4 * std::max<int64_t>(pv, 1)));
+  H3D_CUDA(h->gv_pt.ensure(sizeof(float) * 4 * std::max<int64_t>(pu, 1)));
+  h->gemv_ok = true;
+  return HODLR3D_OK;
+}
+
+// largest column counts the few-column engine takes in the automatic choice
+// (passes of 4 columns; measured at 64^3: 7.9 ms for 4 columns against 10.4
+// ms for the tensor cores' 32, and 8.7 ms per 4 transposed columns against
+// 28-54 ms for the CUDA-core transpose of 4-32)
+constexpr int kGemvForwardMax = 4;
+constexpr int kGemvTransposeMax = 16;
+
 int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld, int precision,
                   cudaStream_t s, bool trans) {
   if (!h->assembled) return set_error(HODLR3D_ERR_NOT_ASSEMBLED, "hodlr3d_assemble has not run");
@@ -927,13 +1077,69 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
   B.upper_pairs = h->upper.as<int32_t>();
   B.n_upper = h->n_upper;
   B.max_slice = h->max_slice;
-  const int nrp = h3d::padded_nrhs(nrhs);
-  // the tensor-core engine takes the forward mixed product in batches of up to
-  // 32 right-hand sides (fewer are zero padded: streaming the factors costs
-  // the same, and it beats the CUDA-core kernels from one right-hand side on)
-  const bool tc_ok = precision == HODLR3D_MIXED && !trans && h->max_leaf <= 128 &&
-                     h->leaves_aligned && h->tc_entries <= h3d::tc_max_entries();
-  (void)nrp;
+  // Mixed form: the few-column engine streams the FP32 factors once per 4
+  // right-hand sides; the tensor-core engine once per 32 at a higher cost per
+  // factor entry, so it takes the forward product from kGemvForwardMax + 1
+  // columns on.  The transpose has no tensor-core form: past
+  // kGemvTransposeMax columns the CUDA-core kernels (all columns in one pass)
+  // are faster.
+  const bool mixed = precision == HODLR3D_MIXED;
+  bool use_gemv = false;
+  if (mixed && (h->engine == 3 ||
+                (h->engine == 0 && nrhs <= (trans ? kGemvTransposeMax : kGemvForwardMax)))) {
+    H3D_TRY(ensure_near_blocks(h, nr, s));
+    H3D_TRY(ensure_gemv(h, s));
+    use_gemv = h->gemv_ok;
+  }
+  if (h->engine == 3 && !use_gemv)
+    return set_error(HODLR3D_ERR_UNSUPPORTED,
+                     "the few-column engine needs the mixed form, leaves whose near-field inputs "
+                     "fit its shared memory and fewer than 2^31 rows of T");
+  if (use_gemv) {
+    h3d::GemvOp g{};
+    g.levels = h->levels;
+    g.max_leaf4 = (h->max_leaf + 3) & ~3;
+    g.nleaf = h->nleaf;
+    g.N = h->N;
+    g.leaf_off = h->leaf_off.as<int32_t>();
+    g.perm = h->perm.as<int32_t>();
+    g.nbr_leaf = h->nbr_leaf.as<int32_t>();
+    g.u32 = h->u32_pool->as<float>();
+    g.v32 = h->v32_pool->as<float>();
+    g.ubox_off = h->gv_ubox_off.as<int64_t>();
+    g.rbox = h->tc_rbox.as<int32_t>();
+    g.vbox_off = h->gv_vbox_off.as<int64_t>();
+    g.vbox_rows = h->gv_vbox_rows.as<int32_t>();
+    g.vrow0 = h->gv_vrow0.as<int64_t>();
+    g.vrow_t = h->gv_vrow_t.as<int32_t>();
+    g.tbase = h->gv_tbase.as<int64_t>();
+    g.vpofs = h->gv_vpofs.as<int64_t>();
+    g.upofs = h->gv_upofs.as<int64_t>();
+    g.knear = h->knear.as<float>();
+    g.near_off = h->near_off.as<int64_t>();
+    h3d::GemvBuffers gb{};
+    gb.xg = h->gv_x.as<float>();
+    gb.t = h->gv_t.as<float>();
+    gb.tt = h->gv_tt.as<float>();
+    gb.p = h->gv_p.as<float>();
+    gb.pt = h->gv_pt.as<float>();
+    gb.vt_items = h->gv_vt_items.as<int4>();
+    gb.n_vt_items = h->gv_n_vt_items;
+    gb.vt_upper = h->gv_vt_upper.as<int32_t>();
+    gb.n_vt_upper = h->gv_n_vt_upper;
+    gb.ut_items = h->gv_ut_items.as<int2>();
+    gb.n_ut_items = h->gv_n_ut_items;
+    gb.ut_upper = h->gv_ut_upper.as<int32_t>();
+    gb.n_ut_upper = h->gv_n_ut_upper;
+    for (int c0 = 0; c0 < nrhs; c0 += 4)
+      h->launches += h3d::launch_matvec_gemv(s, g, gb, x + c0 * ld, ld, y + c0 * ld, ld,
+                                             std::min(4, nrhs - c0), trans,
+                                             h->profiling ? &h->prof : nullptr);
+    H3D_CUDA(cudaGetLastError());
+    return HODLR3D_OK;
+  }
+  const bool tc_ok = mixed && !trans && h->max_leaf <= 128 && h->leaves_aligned &&
+                     h->tc_entries <= h3d::tc_max_entries();
   if (h->engine == 2 && !tc_ok)
     return set_error(HODLR3D_ERR_UNSUPPORTED,
                      "the tensor-core engine needs A x (not the transpose) in the mixed form, "
@@ -945,35 +1151,8 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
       H3D_CUDA(h->dev_err.ensure(sizeof(int)));
       H3D_CUDA(cudaMemsetAsync(h->dev_err.p, 0, sizeof(int), s));
     }
-    if (!h->near_built) {
-      // FP32 near-field blocks, evaluated once
-      h->h_nbr_leaf.resize(26 * h->nleaf);
-      H3D_CUDA(cudaMemcpy(h->h_nbr_leaf.data(), h->nbr_leaf.p, sizeof(int32_t) * 26 * h->nleaf,
-                          cudaMemcpyDeviceToHost));
-      const std::vector<int32_t>& nbl = h->h_nbr_leaf;
-      std::vector<int64_t> off(27 * h->nleaf, -1);
-      int64_t tot = 0;
-      for (int64_t k = 0; k < h->nleaf; ++k) {
-        const int64_t nk = h->h_leaf_off[k + 1] - h->h_leaf_off[k];
-        for (int sl = 0; sl < 27; ++sl) {
-          const int64_t nn = sl < 26 ? nbl[26 * k + sl] : k;
-          if (nn < 0) continue;
-          const int64_t ne = h->h_leaf_off[nn + 1] - h->h_leaf_off[nn];
-          off[27 * k + sl] = tot;
-          tot += nk * ((ne + 3) & ~int64_t(3));
-        }
-      }
-      H3D_CUDA(h->knear.ensure(sizeof(float) * std::max<int64_t>(tot, 4)));
-      H3D_CUDA(h->near_off.ensure(sizeof(int64_t) * off.size()));
-      H3D_CUDA(cudaMemcpy(h->near_off.p, off.data(), sizeof(int64_t) * off.size(),
-                          cudaMemcpyHostToDevice));
-      h->launches += h3d::launch_near_blocks(s, h->nleaf, h->leaf_off.as<int32_t>(), nr,
-                                             h->near_off.as<int64_t>(), h->knear.as<float>());
-      H3D_CUDA(cudaGetLastError());
-      h->near_floats = tot;
-      h->near_built = true;
-      H3D_TRY(build_tensor_maps(h, off));
-    }
+    H3D_TRY(ensure_near_blocks(h, nr, s));
+    if (!h->maps_built) H3D_TRY(build_tensor_maps(h, h->h_near_off));
     // [X | T], the B operands in the split-exact form
     H3D_CUDA(h->tct.ensure(sizeof(float) * 32 * (h->N + std::max<int64_t>(h->sum_rank4, 1))));
     h3d::TcBuffers T{};
@@ -1592,7 +1771,7 @@ int hodlr3d_get_pair_factors(hodlr3d_t h, int64_t pair, double* U, double* V) {
 int64_t hodlr3d_launch_count(hodlr3d_t h) { return h ? h->launches : 0; }
 
 int hodlr3d_set_engine(hodlr3d_t h, int engine) {
-  if (!h || engine < 0 || engine > 2) return set_error(HODLR3D_ERR_INVALID_ARG, "engine must be 0, 1 or 2");
+  if (!h || engine < 0 || engine > 3) return set_error(HODLR3D_ERR_INVALID_ARG, "engine must be 0, 1, 2 or 3");
   h->engine = engine;
   return HODLR3D_OK;
 }

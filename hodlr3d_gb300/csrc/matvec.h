@@ -132,6 +132,62 @@ int tc_max_entries();
 int launch_near_blocks(cudaStream_t s, int64_t nleaf, const int32_t* leaf_off, const NearOp& near,
                        const int64_t* near_off, float* Knear);
 
+// The few-column form (matvec_gemv.cu): 1, 2 or 4 right-hand sides, A X or
+// A^T X, from the box-grouped FP32 factors and near-field blocks.
+constexpr int kGemvCols = 1024;     // columns of a V-stack chunk (forward)
+constexpr int kGemvRowChunk = 512;  // V-stack rows per forward work item
+constexpr int kGemvRowsT = 256;     // U rows per transposed work item
+
+struct GemvOp {
+  int levels;
+  int max_leaf4;              // round4 of the largest leaf population
+  int64_t nleaf;
+  int64_t N;
+  const int32_t* leaf_off;
+  const int32_t* perm;
+  const int32_t* nbr_leaf;    // nleaf x 26
+  const float* u32;           // grouped FP32 U pool
+  const float* v32;           // grouped FP32 V pool
+  const int64_t* ubox_off;    // per box: U_b at u32 + ubox_off[b], n_b x rbox[b]
+  const int32_t* rbox;
+  const int64_t* vbox_off;    // per box: V stack at v32 + vbox_off[a], vbox_rows[a] x round4(m_a)
+  const int32_t* vbox_rows;
+  const int64_t* vrow0;       // per box: first row of its V stack in the global row numbering
+  const int32_t* vrow_t;      // per global V-stack row: its row of T
+  const int64_t* tbase;       // per box: first row of its T (R_b rows)
+  const int64_t* vpofs;       // per box: chunk partials of its V stack (floats / NR), -1 when one chunk
+  const int64_t* upofs;       // per box: chunk partials of its U^T X (floats / NR), -1 when one chunk
+  const float* knear;         // FP32 near-field blocks (launch_near_blocks)
+  const int64_t* near_off;    // 27 per leaf, -1 for no neighbour
+};
+
+// Work buffers: xg N x 4 floats; t, tt: T rows x 4 floats (t zeroed once:
+// its padding rows are never written); p, pt: chunk partials x 4 floats.
+// Work lists: vt_items (source box, chunk, first row, rows); vt_upper: boxes
+// with chunk partials; ut_items (target box, row chunk); ut_upper likewise.
+struct GemvBuffers {
+  float* xg;
+  float* t;
+  float* tt;
+  float* p;
+  float* pt;
+  const int4* vt_items;
+  int64_t n_vt_items;
+  const int32_t* vt_upper;
+  int64_t n_vt_upper;
+  const int2* ut_items;
+  int64_t n_ut_items;
+  const int32_t* ut_upper;
+  int64_t n_ut_upper;
+};
+
+size_t gemv_uy_smem(int max_leaf4, int nr);
+size_t gemv_vy_smem(int max_leaf4, int nr);
+// nrhs in 1..4.  Returns the number of launches.
+int launch_matvec_gemv(cudaStream_t s, const GemvOp& op, const GemvBuffers& B, const double* X,
+                       int64_t ldx, double* Y, int64_t ldy, int nrhs, bool trans,
+                       MatvecProfiler* prof);
+
 // precision: 0 = FP64, 1 = mixed.  X, Y column-major in the original order.
 // Returns the number of kernel launches.
 int launch_matvec(cudaStream_t s, int64_t N, const int32_t* perm, const FarOp& far,

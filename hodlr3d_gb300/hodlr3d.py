@@ -207,8 +207,9 @@ class HODLR3D:
         return int(self._L.hodlr3d_launch_count(self.handle))
 
     def set_engine(self, engine: str) -> None:
-        """'auto', 'simt' (CUDA cores) or 'tc' (tcgen05 tensor cores, mixed form, 17..32 RHS)."""
-        check(self._L.hodlr3d_set_engine(self.handle, {"auto": 0, "simt": 1, "tc": 2}[engine]))
+        """'auto', 'simt' (CUDA cores, every form), 'tc' (tcgen05 tensor cores,
+        mixed A x) or 'gemv' (few-column FP32 kernels, mixed A x and A^T x)."""
+        check(self._L.hodlr3d_set_engine(self.handle, {"auto": 0, "simt": 1, "tc": 2, "gemv": 3}[engine]))
 
     def device_status(self) -> None:
         """Raises if a bounded device wait gave up in an earlier call."""

@@ -57,7 +57,7 @@ def test_tc_refuses_transpose(case):
     with pytest.raises(RuntimeError, match="tensor-core engine"):
         H.matvec(X, "mixed", transpose=True)
     H.set_engine("auto")
-    y = H.matvec(X, "mixed", transpose=True)  # served by the CUDA-core engine
+    y = H.matvec(X, "mixed", transpose=True)  # served by the CUDA-core engine (32 columns)
     assert torch.isfinite(y).all()
 
 
