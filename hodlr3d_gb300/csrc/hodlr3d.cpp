@@ -242,11 +242,14 @@ struct hodlr3d_handle {
   bool near_built = false;
   std::vector<int32_t> h_nbr_leaf;  // host copy (tensor maps of the near-field blocks)
   std::vector<int64_t> h_near_off;  // 27 per leaf: near-block offsets, -1 for no neighbour
+  std::vector<int64_t> h_near_base;  // per leaf: its near-field matrix (blocks side by side)
+  std::vector<int32_t> h_near_ld;    // per leaf: row length of that matrix
+  DevBuf near_base, near_ld;
   int64_t near_floats = 0;
   // few-column engine (matvec_gemv.cu): tables over the grouped FP32 layouts
   bool gemv_built = false;
   bool gemv_ok = false;          // tree and layouts fit the few-column kernels
-  DevBuf gv_ubox_off, gv_vbox_off, gv_vbox_rows, gv_vrow0, gv_vrow_t, gv_tbase, gv_vpofs,
+  DevBuf gv_ubox_off, gv_vbox_off, gv_vbox_rows, gv_vrow0, gv_vrow_t, gv_trow_v, gv_tbase, gv_vpofs,
       gv_upofs, gv_vt_items, gv_vt_upper, gv_ut_items, gv_ut_upper, gv_x, gv_t, gv_tt, gv_p, gv_pt;
   int64_t gv_n_vt_items = 0, gv_n_vt_upper = 0, gv_n_ut_items = 0, gv_n_ut_upper = 0;
   // GMRES work buffers
@@ -830,10 +833,11 @@ int build_tensor_maps(hodlr3d_t h, const std::vector<int64_t>& near_off) {
   std::atomic<int> bad{0};
   std::mutex bad_mu;
   char bad_msg[160] = {0};
-  auto enc = [&](CUtensorMap* m, const float* base, int64_t inner, int64_t rows, uint32_t box_rows) {
+  auto enc = [&](CUtensorMap* m, const float* base, int64_t inner, int64_t rows, uint32_t box_rows,
+                 int64_t ld) {
     if (!base || inner <= 0 || rows <= 0) return;
     const cuuint64_t dim[2] = {(cuuint64_t)inner, (cuuint64_t)rows};
-    const cuuint64_t stride[1] = {(cuuint64_t)inner * sizeof(float)};
+    const cuuint64_t stride[1] = {(cuuint64_t)ld * sizeof(float)};
     const cuuint32_t box[2] = {32, box_rows}, es[2] = {1, 1};
     const CUresult r = encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dim, stride, box, es,
                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -856,10 +860,11 @@ int build_tensor_maps(hodlr3d_t h, const std::vector<int64_t>& near_off) {
         int64_t b0, b1;
         box_range(h, j, b - h3d::level_base(j), b0, b1);
         if (h->h_rbox[b] > 0)
-          enc(&maps[b], h->u32_pool->as<float>() + h->h_ubox_off[b], h->h_rbox[b], b1 - b0, 128);
+          enc(&maps[b], h->u32_pool->as<float>() + h->h_ubox_off[b], h->h_rbox[b], b1 - b0, 128,
+              h->h_rbox[b]);
         if (h->h_vbox_rows[b] > 0)
           enc(&maps[nbox + b], h->v32_pool->as<float>() + h->h_vbox_off[b],
-              ((b1 - b0) + 3) & ~int64_t(3), h->h_vbox_rows[b], 128);
+              ((b1 - b0) + 3) & ~int64_t(3), h->h_vbox_rows[b], 128, ((b1 - b0) + 3) & ~int64_t(3));
       }
       for (int64_t k = t; k < h->nleaf; k += nthr) {
         const int64_t nk = h->h_leaf_off[k + 1] - h->h_leaf_off[k];
@@ -868,7 +873,8 @@ int build_tensor_maps(hodlr3d_t h, const std::vector<int64_t>& near_off) {
           if (off < 0) continue;
           const int64_t nn = sl < 26 ? h->h_nbr_leaf[26 * k + sl] : k;
           const int64_t ne = h->h_leaf_off[nn + 1] - h->h_leaf_off[nn];
-          enc(&maps[2 * nbox + 27 * k + sl], knear + off, (ne + 3) & ~int64_t(3), nk, 128);
+          enc(&maps[2 * nbox + 27 * k + sl], knear + off, (ne + 3) & ~int64_t(3), nk, 128,
+              h->h_near_ld[k]);
         }
       }
     });
@@ -885,8 +891,10 @@ int build_tensor_maps(hodlr3d_t h, const std::vector<int64_t>& near_off) {
 }
 
 // FP32 near-field blocks of every leaf (both FP32 engines), evaluated once
-// per assembly: leaf k, slot s (0..25 the neighbours, 26 itself) is a
-// row-major nk x round4(ne) block at h_near_off[27 k + s].
+// per assembly.  The blocks of leaf k (slots 0..25 the neighbours, 26
+// itself; absent neighbours skipped) sit side by side in one row-major
+// nk x Rn_k matrix at h_near_base[k] (Rn_k = h_near_ld[k], the sum of their
+// round4(ne)); slot s's block starts at h_near_off[27 k + s] (-1: absent).
 int ensure_near_blocks(hodlr3d_t h, const h3d::NearOp& nr, cudaStream_t s) {
   if (h->near_built) return HODLR3D_OK;
   h->h_nbr_leaf.resize(26 * h->nleaf);
@@ -895,23 +903,36 @@ int ensure_near_blocks(hodlr3d_t h, const h3d::NearOp& nr, cudaStream_t s) {
   const std::vector<int32_t>& nbl = h->h_nbr_leaf;
   std::vector<int64_t>& off = h->h_near_off;
   off.assign(27 * h->nleaf, -1);
+  h->h_near_base.assign(h->nleaf, 0);
+  h->h_near_ld.assign(h->nleaf, 0);
   int64_t tot = 0;
   for (int64_t k = 0; k < h->nleaf; ++k) {
     const int64_t nk = h->h_leaf_off[k + 1] - h->h_leaf_off[k];
+    int64_t col = 0;
     for (int sl = 0; sl < 27; ++sl) {
       const int64_t nn = sl < 26 ? nbl[26 * k + sl] : k;
       if (nn < 0) continue;
       const int64_t ne = h->h_leaf_off[nn + 1] - h->h_leaf_off[nn];
-      off[27 * k + sl] = tot;
-      tot += nk * ((ne + 3) & ~int64_t(3));
+      off[27 * k + sl] = tot + col;
+      col += (ne + 3) & ~int64_t(3);
     }
+    h->h_near_base[k] = tot;
+    h->h_near_ld[k] = (int32_t)col;
+    tot += nk * col;
   }
   H3D_CUDA(h->knear.ensure(sizeof(float) * std::max<int64_t>(tot, 4)));
   H3D_CUDA(h->near_off.ensure(sizeof(int64_t) * off.size()));
   H3D_CUDA(cudaMemcpy(h->near_off.p, off.data(), sizeof(int64_t) * off.size(),
                       cudaMemcpyHostToDevice));
+  H3D_CUDA(h->near_base.ensure(sizeof(int64_t) * h->nleaf));
+  H3D_CUDA(cudaMemcpy(h->near_base.p, h->h_near_base.data(), sizeof(int64_t) * h->nleaf,
+                      cudaMemcpyHostToDevice));
+  H3D_CUDA(h->near_ld.ensure(sizeof(int32_t) * h->nleaf));
+  H3D_CUDA(cudaMemcpy(h->near_ld.p, h->h_near_ld.data(), sizeof(int32_t) * h->nleaf,
+                      cudaMemcpyHostToDevice));
   h->launches += h3d::launch_near_blocks(s, h->nleaf, h->leaf_off.as<int32_t>(), nr,
-                                         h->near_off.as<int64_t>(), h->knear.as<float>());
+                                         h->near_off.as<int64_t>(), h->near_ld.as<int32_t>(),
+                                         h->knear.as<float>());
   H3D_CUDA(cudaGetLastError());
   h->near_floats = tot;
   h->near_built = true;
@@ -942,7 +963,7 @@ int ensure_gemv(hodlr3d_t h, cudaStream_t s) {
   if (np) H3D_CUDA(cudaMemcpy(rev.data(), h->rev.p, sizeof(int32_t) * np, cudaMemcpyDeviceToHost));
   for (int64_t b = 0; b < nbox; ++b)
     for (int64_t p = h->h_il_ptr[b]; p < h->h_il_ptr[b + 1]; ++p) tgt[p] = (int32_t)b;
-  std::vector<int32_t> vrow_t(std::max<int64_t>(vrows, 1));
+  std::vector<int32_t> vrow_t(std::max<int64_t>(vrows, 1)), trow_v(std::max<int64_t>(trows, 1), -1);
   std::vector<int32_t> vt_upper, ut_upper;
   std::vector<int32_t> vt_items, ut_items;  // int4 / int2 records
   int64_t pv = 0, pu = 0;
@@ -957,7 +978,10 @@ int ensure_gemv(hodlr3d_t h, cudaStream_t s) {
     for (int64_t q = h->h_il_ptr[b]; q < h->h_il_ptr[b + 1]; ++q) {
       const int p = rev[q];
       const int64_t base = tbase[tgt[p]] + h->h_coff[p];
-      for (int l = 0; l < h->h_rank[p]; ++l) vrow_t[v++] = (int32_t)(base + l);
+      for (int l = 0; l < h->h_rank[p]; ++l) {
+        trow_v[base + l] = (int32_t)v;
+        vrow_t[v++] = (int32_t)(base + l);
+      }
     }
     const int rows = h->h_vbox_rows[b];
     if (rows > 0 && m > 0) {
@@ -998,6 +1022,7 @@ int ensure_gemv(hodlr3d_t h, cudaStream_t s) {
   H3D_CUDA(put(h->gv_vbox_rows, h->h_vbox_rows.data(), sizeof(int32_t) * nbox));
   H3D_CUDA(put(h->gv_vrow0, vrow0.data(), sizeof(int64_t) * (nbox + 1)));
   H3D_CUDA(put(h->gv_vrow_t, vrow_t.data(), sizeof(int32_t) * vrows));
+  H3D_CUDA(put(h->gv_trow_v, trow_v.data(), sizeof(int32_t) * trows));
   H3D_CUDA(put(h->gv_tbase, tbase.data(), sizeof(int64_t) * nbox));
   H3D_CUDA(put(h->gv_vpofs, vpofs.data(), sizeof(int64_t) * nbox));
   H3D_CUDA(put(h->gv_upofs, upofs.data(), sizeof(int64_t) * nbox));
@@ -1012,7 +1037,7 @@ int ensure_gemv(hodlr3d_t h, cudaStream_t s) {
   H3D_CUDA(h->gv_x.ensure(sizeof(float) * 4 * h->N));
   H3D_CUDA(h->gv_t.ensure(sizeof(float) * 4 * std::max<int64_t>(trows, 1)));
   H3D_CUDA(cudaMemsetAsync(h->gv_t.p, 0, sizeof(float) * 4 * std::max<int64_t>(trows, 1), s));
-  H3D_CUDA(h->gv_tt.ensure(sizeof(float) * 4 * std::max<int64_t>(trows, 1)));
+  H3D_CUDA(h->gv_tt.ensure(sizeof(float) * 4 * std::max<int64_t>(vrows, 1)));
   H3D_CUDA(h->gv_p.ensure(sizeof(float) * 4 * std::max<int64_t>(pv, 1)));
   H3D_CUDA(h->gv_pt.ensure(sizeof(float) * 4 * std::max<int64_t>(pu, 1)));
   h->gemv_ok = true;
@@ -1112,11 +1137,13 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
     g.vbox_rows = h->gv_vbox_rows.as<int32_t>();
     g.vrow0 = h->gv_vrow0.as<int64_t>();
     g.vrow_t = h->gv_vrow_t.as<int32_t>();
+    g.trow_v = h->gv_trow_v.as<int32_t>();
     g.tbase = h->gv_tbase.as<int64_t>();
     g.vpofs = h->gv_vpofs.as<int64_t>();
     g.upofs = h->gv_upofs.as<int64_t>();
     g.knear = h->knear.as<float>();
-    g.near_off = h->near_off.as<int64_t>();
+    g.near_base = h->near_base.as<int64_t>();
+    g.near_ld = h->near_ld.as<int32_t>();
     h3d::GemvBuffers gb{};
     gb.xg = h->gv_x.as<float>();
     gb.t = h->gv_t.as<float>();

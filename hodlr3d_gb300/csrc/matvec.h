@@ -105,7 +105,8 @@ struct TcBuffers {
   int64_t n_upper;
   int max_slice;
   const float* knear;        // FP32 near-field blocks (launch_near_blocks)
-  const int64_t* near_off;   // 27 per leaf: block offsets, -1 for no neighbour
+  const int64_t* near_off;   // 27 per leaf: block offsets, -1 for no neighbour (row
+                             // stride: the leaf's sum of round4(ne))
   // 2D tensor maps (CUtensorMap, 128 bytes each) of the FP32 operands A, box
   // 32 x 128, 128-byte swizzle, zero fill; boxes of all levels numbered
   // together: umaps[b]: the U of the pairs of target box b side by side, as
@@ -127,15 +128,17 @@ int launch_matvec_tc(cudaStream_t s, int64_t N, const int32_t* perm, const FarOp
 // Largest number of table entries (pairs of all levels a block multiplies, or
 // a leaf's pairs plus 27 near-field blocks) one tensor-core block takes.
 int tc_max_entries();
-// Evaluates the FP32 near-field blocks of every leaf (row-major nk x round4(ne)
-// at near_off[27 k + slot], slots 0..25 the neighbours, 26 the leaf itself).
+// Evaluates the FP32 near-field blocks of every leaf: block (k, slot) (slots
+// 0..25 the neighbours, 26 the leaf itself) is nk x round4(ne) at
+// near_off[27 k + slot] with row stride near_ld[k] (the blocks of a leaf side
+// by side in one row-major matrix).
 int launch_near_blocks(cudaStream_t s, int64_t nleaf, const int32_t* leaf_off, const NearOp& near,
-                       const int64_t* near_off, float* Knear);
+                       const int64_t* near_off, const int32_t* near_ld, float* Knear);
 
 // The few-column form (matvec_gemv.cu): 1, 2 or 4 right-hand sides, A X or
 // A^T X, from the box-grouped FP32 factors and near-field blocks.
 constexpr int kGemvCols = 1024;     // columns of a V-stack chunk (forward)
-constexpr int kGemvRowChunk = 512;  // V-stack rows per forward work item
+constexpr int kGemvRowChunk = 2048;  // V-stack rows per forward work item
 constexpr int kGemvRowsT = 256;     // U rows per transposed work item
 
 struct GemvOp {
@@ -154,15 +157,18 @@ struct GemvOp {
   const int32_t* vbox_rows;
   const int64_t* vrow0;       // per box: first row of its V stack in the global row numbering
   const int32_t* vrow_t;      // per global V-stack row: its row of T
+  const int32_t* trow_v;      // per row of T: its global V-stack row, -1 for padding
   const int64_t* tbase;       // per box: first row of its T (R_b rows)
   const int64_t* vpofs;       // per box: chunk partials of its V stack (floats / NR), -1 when one chunk
   const int64_t* upofs;       // per box: chunk partials of its U^T X (floats / NR), -1 when one chunk
   const float* knear;         // FP32 near-field blocks (launch_near_blocks)
-  const int64_t* near_off;    // 27 per leaf, -1 for no neighbour
+  const int64_t* near_base;   // per leaf: its blocks side by side, nk x near_ld[k] row-major
+  const int32_t* near_ld;
 };
 
-// Work buffers: xg N x 4 floats; t, tt: T rows x 4 floats (t zeroed once:
-// its padding rows are never written); p, pt: chunk partials x 4 floats.
+// Work buffers: xg N x 4 floats; t: T rows x 4 floats (zeroed once: its
+// padding rows are never written); tt: V-stack rows x 4 floats (the
+// transposed T in stack order); p, pt: chunk partials x 4 floats.
 // Work lists: vt_items (source box, chunk, first row, rows); vt_upper: boxes
 // with chunk partials; ut_items (target box, row chunk); ut_upper likewise.
 struct GemvBuffers {

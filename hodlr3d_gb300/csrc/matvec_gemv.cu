@@ -19,12 +19,14 @@
 //   V of source box a: row-major (sum of ranks) x round4(m_a) at
 //     v32 + vbox_off[a], one row per column of each V_p, pairs in the order of
 //     a's reverse list (zero columns past m_a);
-//   T (V^T X forward, U^T X transposed): R_b x NR at row tbase[b], the same
-//     grouping as U; vrow_t[v] maps row v of the V stacks (numbered over all
-//     boxes, box a's from vrow0[a]) to its row of T;
+//   T = V^T X (forward): R_b x NR at row tbase[b], the same grouping as U;
+//     vrow_t[v] maps row v of the V stacks (numbered over all boxes, box a's
+//     from vrow0[a]) to its row of T, trow_v the other way (-1: padding);
+//   T = U^T X (transposed): in the row order of the V stacks, so that each
+//     stack meets its T rows contiguously;
 //   X: N x NR FP32 in tree order; near blocks: nk x round4(ne) row-major.
 // Stages:
-//   forward   gather; vt (items: source box, 1024-column chunk, 512 rows):
+//   forward   gather; vt (items: source box, 1024-column chunk, 2048 rows):
 //             T rows or chunk partials; tred (boxes wider than one chunk);
 //             uy (one block per leaf): far field U T of the d levels, near
 //             field, written once in the original order.
@@ -80,14 +82,15 @@ __device__ __forceinline__ void fma_row4(float (&acc)[NR], const float4 v, const
   }
 }
 
-// Dot products of up to ROWS rows (row q at rowp + q ld, q < nrows) of len4
-// 16-byte groups with the vector vec ([4 len4][NR], shared or global memory),
-// LW lanes per row; out(q, acc) is called once per row by its group's first
-// lane.  Every lane of the warp takes part (warp-uniform arguments).
-template <int NR, int LW, class Out>
+// Dot products of up to P (32 / LW) rows (row q at rowp + q ld, q < nrows) of
+// len4 16-byte groups with the vector vec ([4 len4][NR], shared or global
+// memory), LW lanes per row, P rows per lane; out(q, acc) is called once per
+// row by its group's first lane.  Every lane of the warp takes part
+// (warp-uniform arguments).
+template <int NR, int LW, int P = ROWS * LW / 32, class Out>
 __device__ __forceinline__ void seg_rows(const float* __restrict__ rowp, int64_t ld, int nrows,
                                          int len4, const float* vec, Out&& out) {
-  constexpr int G = 32 / LW, P = ROWS / G;
+  constexpr int G = 32 / LW;
   const int lane = threadIdx.x & 31, g = lane / LW, li = lane % LW;
   float acc[P][NR];
 #pragma unroll
@@ -144,6 +147,23 @@ __global__ void k_gather(int64_t N, int nrhs, const double* __restrict__ X, int6
   xg[o] = c < nrhs ? (float)X[c * ldx + perm[t]] : 0.f;
 }
 
+// nr rows of a V stack (row stride m4) times xs, 8 rows per lane and 8 G per
+// warp pass; row R's sums go to dst[map[R] NR + c] (map null: dst[R NR + c]).
+template <int NR, int LW>
+__device__ __forceinline__ void vt_rows(const float* __restrict__ V, int64_t m4, int nr, int len4,
+                                        const float* xs, float* __restrict__ dst,
+                                        const int32_t* __restrict__ map) {
+  constexpr int RB = 8 * (32 / LW);  // rows per warp pass
+  const int w = threadIdx.x >> 5;
+  for (int b0 = w * RB; b0 < nr; b0 += WARPS * RB)
+    seg_rows<NR, LW, 8>(V + b0 * m4, m4, min(RB, nr - b0), len4, xs, [&](int q, const float(&s)[NR]) {
+      const int R = b0 + q;
+      float* o = dst + (int64_t)(map ? map[R] : R) * NR;
+#pragma unroll
+      for (int c = 0; c < NR; ++c) o[c] = s[c];
+    });
+}
+
 // Forward far field, input side: for item (a, ci, r0, nr), rows r0 .. r0+nr of
 // source box a's V stack over columns [ci CW, + CW) times X of those points.
 template <int NR>
@@ -171,21 +191,18 @@ __global__ void __launch_bounds__(THREADS) k_vt(GemvOp op, const int4* __restric
   const int64_t pofs = op.vpofs[a];
   const int32_t* vr = op.vrow_t + op.vrow0[a];
   const float* V = op.v32 + op.vbox_off[a] + (int64_t)r0 * m4 + col0;
-  const int w = threadIdx.x >> 5;
-  for (int b0 = w * ROWS; b0 < nr; b0 += WARPS * ROWS) {
-    seg_rows_any<NR>(V + b0 * m4, m4, min(ROWS, nr - b0), cl / 4, xs, [&](int q, const float(&s)[NR]) {
-      const int R = r0 + b0 + q;
-      if (pofs < 0) {
-        float* dst = T + (int64_t)vr[R] * NR;
-#pragma unroll
-        for (int c = 0; c < NR; ++c) dst[c] = s[c];
-      } else {
-        float* dst = P + (pofs + (int64_t)ci * rows_a + R) * NR;
-#pragma unroll
-        for (int c = 0; c < NR; ++c) dst[c] = s[c];
-      }
-    });
-  }
+  // rows r0 + R of the item go to T row vr[R] or to partial row R of chunk ci
+  float* dst = pofs < 0 ? T : P + (pofs + (int64_t)ci * rows_a + r0) * NR;
+  const int32_t* map = pofs < 0 ? vr + r0 : nullptr;
+  const int len4 = cl / 4;
+  if (len4 > 16)
+    vt_rows<NR, 32>(V, m4, nr, len4, xs, dst, map);
+  else if (len4 > 8)
+    vt_rows<NR, 16>(V, m4, nr, len4, xs, dst, map);
+  else if (len4 > 4)
+    vt_rows<NR, 8>(V, m4, nr, len4, xs, dst, map);
+  else
+    vt_rows<NR, 4>(V, m4, nr, len4, xs, dst, map);
 }
 
 // T rows of a source box wider than one chunk: FP64 sum of its chunk partials
@@ -210,40 +227,36 @@ __global__ void k_tred(GemvOp op, const int32_t* __restrict__ boxes, const float
   }
 }
 
-// The X of leaf k's neighbour leaves (slots 0..25, 26 = itself), zero padded
-// to round4(ne) rows per slot: xn[slot * nep + e][c].  Returns nothing; the
-// caller synchronises.
+// The X of leaf k's neighbour leaves (slots 0..25, 26 = itself; absent ones
+// skipped) in the column order of its near-field matrix: slot by slot, each
+// zero padded to round4(ne) rows, xn[col][c].  The caller synchronises.
 template <int NR>
 __device__ __forceinline__ void stage_near_x(const GemvOp& op, int64_t k, const float* __restrict__ xg,
-                                             float* xn, int nep) {
+                                             float* xn) {
+  int64_t col = 0;
   for (int sl = 0; sl < 27; ++sl) {
     const int64_t nn = sl < 26 ? (int64_t)op.nbr_leaf[k * 26 + sl] : k;
     if (nn < 0) continue;
     const int64_t e0 = op.leaf_off[nn];
     const int ne = (int)(op.leaf_off[nn + 1] - e0), ne4 = (ne + 3) & ~3;
     for (int e = threadIdx.x; e < ne4 * NR; e += THREADS)
-      xn[(int64_t)sl * nep * NR + e] = e < ne * NR ? xg[e0 * NR + e] : 0.f;
+      xn[col * NR + e] = e < ne * NR ? xg[e0 * NR + e] : 0.f;
+    col += ne4;
   }
 }
 
-// Near field of rows [i0, i0 + nrows) of leaf k (leaf-local), added to the
-// warp's FP64 row sums ya[row][c].
+// Near field of rows [i0, i0 + nrows) of leaf k (leaf-local): one segment of
+// its near-field matrix, added to the warp's FP64 row sums ya[row][c].
 template <int NR>
-__device__ __forceinline__ void near_rows(const GemvOp& op, int64_t k, int nk, int i0, int nrows,
-                                          const float* xn, int nep, double* ya) {
-  const int64_t* no = op.near_off + 27 * k;
-  for (int sl = 0; sl < 27; ++sl) {
-    const int64_t off = no[sl];
-    if (off < 0) continue;
-    const int64_t nn = sl < 26 ? (int64_t)op.nbr_leaf[k * 26 + sl] : k;
-    const int ne4 = (int)((op.leaf_off[nn + 1] - op.leaf_off[nn] + 3) & ~int64_t(3));
-    seg_rows_any<NR>(op.knear + off + (int64_t)i0 * ne4, ne4, nrows, ne4 / 4,
-                     xn + (int64_t)sl * nep * NR, [&](int q, const float(&s)[NR]) {
+__device__ __forceinline__ void near_rows(const GemvOp& op, int64_t k, int i0, int nrows,
+                                          const float* xn, double* ya) {
+  const int ld = op.near_ld[k];
+  seg_rows_any<NR>(op.knear + op.near_base[k] + (int64_t)i0 * ld, ld, nrows, ld / 4, xn,
+                   [&](int q, const float(&s)[NR]) {
 #pragma unroll
-                       for (int c = 0; c < NR; ++c) ya[q * NR + c] += (double)s[c];
-                     });
-    __syncwarp();
-  }
+                     for (int c = 0; c < NR; ++c) ya[q * NR + c] += (double)s[c];
+                   });
+  __syncwarp();
 }
 
 // Forward output side, one block per leaf k: y = sum over the levels of
@@ -254,15 +267,14 @@ __global__ void __launch_bounds__(THREADS) k_uy(GemvOp op, const float* __restri
                                                 const float* __restrict__ T, int nrhs,
                                                 double* __restrict__ Y, int64_t ldy) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int nep = op.max_leaf4;
   double* yacc = reinterpret_cast<double*>(smem);                         // WARPS x ROWS x NR
-  float* xn = reinterpret_cast<float*>(smem + sizeof(double) * WARPS * ROWS * NR);
+  float* xn = reinterpret_cast<float*>(smem + sizeof(double) * WARPS * ROWS * NR);  // 27 max_leaf4 x NR
   const int64_t k = blockIdx.x;
   const int d = op.levels;
   const int64_t t0 = op.leaf_off[k];
   const int nk = (int)(op.leaf_off[k + 1] - t0);
   if (nk == 0) return;
-  stage_near_x<NR>(op, k, xg, xn, nep);
+  stage_near_x<NR>(op, k, xg, xn);
   __syncthreads();
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double* ya = yacc + w * ROWS * NR;
@@ -283,7 +295,7 @@ __global__ void __launch_bounds__(THREADS) k_uy(GemvOp op, const float* __restri
       });
       __syncwarp();
     }
-    near_rows<NR>(op, k, nk, i0, nrows, xn, nep, ya);
+    near_rows<NR>(op, k, i0, nrows, xn, ya);
     for (int e = lane; e < nrows * NR; e += 32) {
       const int q = e / NR, c = e - q * NR;
       if (c < nrhs) Y[c * ldy + op.perm[t0 + i0 + q]] = ya[e];
@@ -354,9 +366,18 @@ __global__ void __launch_bounds__(THREADS) k_ut(GemvOp op, const int2* __restric
         acc[3][c] = fmaf(v.w, xv, acc[3][c]);
       }
     }
-    if (live) {
-      float* dst = pofs < 0 ? T + (op.tbase[b] + 4 * (int64_t)k4) * NR
-                            : P + (pofs + (int64_t)ci * R + 4 * (int64_t)k4) * NR;
+    if (live && pofs < 0) {
+      // rows of T in the order of the V stacks (padding rows dropped)
+      const int32_t* tv = op.trow_v + op.tbase[b] + 4 * k4;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int32_t sv = tv[e];
+        if (sv >= 0)
+#pragma unroll
+          for (int c = 0; c < NR; ++c) T[(int64_t)sv * NR + c] = acc[e][c];
+      }
+    } else if (live) {
+      float* dst = P + (pofs + (int64_t)ci * R + 4 * (int64_t)k4) * NR;
 #pragma unroll
       for (int e = 0; e < 4; ++e)
 #pragma unroll
@@ -377,11 +398,14 @@ __global__ void k_tred_t(GemvOp op, const int32_t* __restrict__ boxes, const flo
   const int nch = (int)((n + kGemvRowsT - 1) / kGemvRowsT);
   const int R = op.rbox[b];
   const float* src = P + op.upofs[b] * NR;
-  float* dst = T + op.tbase[b] * NR;
+  const int32_t* tv = op.trow_v + op.tbase[b];
   for (int o = threadIdx.x; o < R * NR; o += blockDim.x) {
+    const int k = o / NR;
+    const int32_t sv = tv[k];
+    if (sv < 0) continue;
     double s = 0.0;
     for (int ci = 0; ci < nch; ++ci) s += (double)src[(int64_t)ci * R * NR + o];
-    dst[o] = (float)s;
+    T[(int64_t)sv * NR + (o - k * NR)] = (float)s;
   }
 }
 
@@ -391,9 +415,9 @@ __global__ void k_tred_t(GemvOp op, const int32_t* __restrict__ boxes, const flo
 // at most 64 rows, FP64 beyond), then the near field; written once.
 template <int NR, int LW>
 __device__ __forceinline__ void stack_cols(const float* __restrict__ V, int64_t m4, int rows,
-                                           const int32_t* __restrict__ vr, const float* __restrict__ T,
-                                           int len4, int shift, int nk, double* fw) {
-  constexpr int G = 32 / LW;
+                                           const float* __restrict__ Tv, int len4, int shift, int nk,
+                                           double* fw) {
+  constexpr int G = 32 / LW, U = 8;
   const int lane = threadIdx.x & 31, g = lane / LW, li = lane % LW, w = threadIdx.x >> 5;
   for (int kw = 0; kw < len4; kw += LW) {
     const int k4 = kw + li;
@@ -412,33 +436,32 @@ __device__ __forceinline__ void stack_cols(const float* __restrict__ V, int64_t 
         for (int c = 0; c < NR; ++c) acc[e][c] = 0.f;
       const int vend = min(rows, v0 + 64 * stride);
       int v = v0;
-      for (; v + 3 * stride < vend; v += 4 * stride) {
-        int tr[4];
-        float4 f[4];
+      for (; v + (U - 1) * stride < vend; v += U * stride) {
+        float4 f[U];
+        float tv[U][NR];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) tr[u] = vr[v + u * stride];
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
+        for (int u = 0; u < U; ++u) {
           f[u] = live ? __ldcs(reinterpret_cast<const float4*>(V + (int64_t)(v + u * stride) * m4) + k4)
                       : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
+          for (int c = 0; c < NR; ++c) tv[u][c] = Tv[(int64_t)(v + u * stride) * NR + c];
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
 #pragma unroll
           for (int c = 0; c < NR; ++c) {
-            const float tv = T[(int64_t)tr[u] * NR + c];
-            acc[0][c] = fmaf(f[u].x, tv, acc[0][c]);
-            acc[1][c] = fmaf(f[u].y, tv, acc[1][c]);
-            acc[2][c] = fmaf(f[u].z, tv, acc[2][c]);
-            acc[3][c] = fmaf(f[u].w, tv, acc[3][c]);
+            acc[0][c] = fmaf(f[u].x, tv[u][c], acc[0][c]);
+            acc[1][c] = fmaf(f[u].y, tv[u][c], acc[1][c]);
+            acc[2][c] = fmaf(f[u].z, tv[u][c], acc[2][c]);
+            acc[3][c] = fmaf(f[u].w, tv[u][c], acc[3][c]);
           }
       }
       for (; v < vend; v += stride) {
-        const int tr = vr[v];
         const float4 f = live ? __ldcs(reinterpret_cast<const float4*>(V + (int64_t)v * m4) + k4)
                               : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
         for (int c = 0; c < NR; ++c) {
-          const float tv = T[(int64_t)tr * NR + c];
+          const float tv = Tv[(int64_t)v * NR + c];
           acc[0][c] = fmaf(f.x, tv, acc[0][c]);
           acc[1][c] = fmaf(f.y, tv, acc[1][c]);
           acc[2][c] = fmaf(f.z, tv, acc[2][c]);
@@ -477,14 +500,14 @@ __global__ void __launch_bounds__(THREADS) k_vy(GemvOp op, const float* __restri
   const int nep = op.max_leaf4;
   double* yacc = reinterpret_cast<double*>(smem);                          // WARPS x ROWS x NR
   double* far = yacc + WARPS * ROWS * NR;                                  // WARPS x nep x NR
-  float* xn = reinterpret_cast<float*>(far + (int64_t)WARPS * nep * NR);   // 27 x nep x NR
+  float* xn = reinterpret_cast<float*>(far + (int64_t)WARPS * nep * NR);   // <= 27 nep x NR
   const int64_t k = blockIdx.x;
   const int d = op.levels;
   const int64_t t0 = op.leaf_off[k];
   const int nk = (int)(op.leaf_off[k + 1] - t0);
   if (nk == 0) return;
   for (int e = threadIdx.x; e < WARPS * nep * NR; e += THREADS) far[e] = 0.0;
-  stage_near_x<NR>(op, k, xg, xn, nep);
+  stage_near_x<NR>(op, k, xg, xn);
   __syncthreads();
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double* fw = far + (int64_t)w * nep * NR;
@@ -498,16 +521,16 @@ __global__ void __launch_bounds__(THREADS) k_vy(GemvOp op, const float* __restri
     const int64_t c0 = t0 - box0, w0 = c0 & ~int64_t(3);
     const int len4 = (int)((((c0 + nk + 3) & ~int64_t(3)) - w0) / 4);
     const float* V = op.v32 + op.vbox_off[a] + w0;
-    const int32_t* vr = op.vrow_t + op.vrow0[a];
+    const float* Tv = T + op.vrow0[a] * NR;
     const int shift = (int)(c0 - w0);
     if (len4 > 16)
-      stack_cols<NR, 32>(V, m4, rows, vr, T, len4, shift, nk, fw);
+      stack_cols<NR, 32>(V, m4, rows, Tv, len4, shift, nk, fw);
     else if (len4 > 8)
-      stack_cols<NR, 16>(V, m4, rows, vr, T, len4, shift, nk, fw);
+      stack_cols<NR, 16>(V, m4, rows, Tv, len4, shift, nk, fw);
     else if (len4 > 4)
-      stack_cols<NR, 8>(V, m4, rows, vr, T, len4, shift, nk, fw);
+      stack_cols<NR, 8>(V, m4, rows, Tv, len4, shift, nk, fw);
     else
-      stack_cols<NR, 4>(V, m4, rows, vr, T, len4, shift, nk, fw);
+      stack_cols<NR, 4>(V, m4, rows, Tv, len4, shift, nk, fw);
     __syncwarp();
   }
   __syncthreads();
@@ -521,7 +544,7 @@ __global__ void __launch_bounds__(THREADS) k_vy(GemvOp op, const float* __restri
       ya[e] = s;
     }
     __syncwarp();
-    near_rows<NR>(op, k, nk, i0, nrows, xn, nep, ya);
+    near_rows<NR>(op, k, i0, nrows, xn, ya);
     for (int e = lane; e < nrows * NR; e += 32) {
       const int q = e / NR, c = e - q * NR;
       if (c < nrhs) Y[c * ldy + op.perm[t0 + i0 + q]] = ya[e];

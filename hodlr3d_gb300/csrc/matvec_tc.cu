@@ -878,10 +878,12 @@ __global__ void k_gather_xt(int64_t N, int nrhs, const double* __restrict__ X, i
 }
 
 // Near-field blocks of every leaf: for neighbour slot s (0..25, 26 = the leaf
-// itself) a row-major nk x round4(ne) FP32 block at near_off[27 k + s], the
-// kernel with the same displacement formula as the on-the-fly near field.
+// itself) an nk x round4(ne) FP32 block at near_off[27 k + s], row stride
+// near_ld[k] (the leaf's blocks side by side), the kernel with the same
+// displacement formula as the on-the-fly near field.
 __global__ void k_near_blocks(const int32_t* __restrict__ leaf_off, NearOp nr,
-                              const int64_t* __restrict__ near_off, float* __restrict__ Knear) {
+                              const int64_t* __restrict__ near_off,
+                              const int32_t* __restrict__ near_ld, float* __restrict__ Knear) {
   const int64_t k = blockIdx.x;
   const int sl = blockIdx.y;
   const int64_t off = near_off[k * 27 + sl];
@@ -903,7 +905,7 @@ __global__ void k_near_blocks(const int32_t* __restrict__ leaf_off, NearOp nr,
                                                 (nr.yl[ti] - nr.yl[ej]) + dcy,
                                                 (nr.zl[ti] - nr.zl[ej]) + dcz);
     }
-    Knear[off + e] = tf32_split_value((double)v);
+    Knear[off + (int64_t)i * near_ld[k] + j] = tf32_split_value((double)v);
   }
 }
 
@@ -912,8 +914,8 @@ __global__ void k_near_blocks(const int32_t* __restrict__ leaf_off, NearOp nr,
 int tc_max_entries() { return kMaxEntries; }
 
 int launch_near_blocks(cudaStream_t s, int64_t nleaf, const int32_t* leaf_off, const NearOp& near,
-                       const int64_t* near_off, float* Knear) {
-  k_near_blocks<<<dim3((unsigned)nleaf, 27), 256, 0, s>>>(leaf_off, near, near_off, Knear);
+                       const int64_t* near_off, const int32_t* near_ld, float* Knear) {
+  k_near_blocks<<<dim3((unsigned)nleaf, 27), 256, 0, s>>>(leaf_off, near, near_off, near_ld, Knear);
   return 1;
 }
 
