@@ -1144,6 +1144,7 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
     g.knear = h->knear.as<float>();
     g.near_base = h->near_base.as<int64_t>();
     g.near_ld = h->near_ld.as<int32_t>();
+    g.near_off = h->near_off.as<int64_t>();
     h3d::GemvBuffers gb{};
     gb.xg = h->gv_x.as<float>();
     gb.t = h->gv_t.as<float>();

@@ -164,6 +164,7 @@ struct GemvOp {
   const float* knear;         // FP32 near-field blocks (launch_near_blocks)
   const int64_t* near_base;   // per leaf: its blocks side by side, nk x near_ld[k] row-major
   const int32_t* near_ld;
+  const int64_t* near_off;    // 27 per leaf: start of each block (column near_off - near_base), -1 absent
 };
 
 // Work buffers: xg N x 4 floats; t: T rows x 4 floats (zeroed once: its

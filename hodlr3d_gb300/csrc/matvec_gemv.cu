@@ -84,9 +84,9 @@ __device__ __forceinline__ void fma_row4(float (&acc)[NR], const float4 v, const
 
 // Dot products of up to P (32 / LW) rows (row q at rowp + q ld, q < nrows) of
 // len4 16-byte groups with the vector vec ([4 len4][NR], shared or global
-// memory), LW lanes per row, P rows per lane; out(q, acc) is called once per
-// row by its group's first lane.  Every lane of the warp takes part
-// (warp-uniform arguments).
+// memory), LW lanes per row, P rows per lane; out(p, q, acc) is called once
+// per row q by its group's first lane (p: the lane's row slot, q = p G + g).
+// Every lane of the warp takes part (warp-uniform arguments).
 template <int NR, int LW, int P = ROWS * LW / 32, class Out>
 __device__ __forceinline__ void seg_rows(const float* __restrict__ rowp, int64_t ld, int nrows,
                                          int len4, const float* vec, Out&& out) {
@@ -119,7 +119,7 @@ __device__ __forceinline__ void seg_rows(const float* __restrict__ rowp, int64_t
   if (li == 0) {
 #pragma unroll
     for (int q = 0; q < P; ++q)
-      if (q * G + g < nrows) out(q * G + g, acc[q]);
+      if (q * G + g < nrows) out(q, q * G + g, acc[q]);
   }
 }
 
@@ -153,15 +153,23 @@ template <int NR, int LW>
 __device__ __forceinline__ void vt_rows(const float* __restrict__ V, int64_t m4, int nr, int len4,
                                         const float* xs, float* __restrict__ dst,
                                         const int32_t* __restrict__ map) {
-  constexpr int RB = 8 * (32 / LW);  // rows per warp pass
-  const int w = threadIdx.x >> 5;
-  for (int b0 = w * RB; b0 < nr; b0 += WARPS * RB)
-    seg_rows<NR, LW, 8>(V + b0 * m4, m4, min(RB, nr - b0), len4, xs, [&](int q, const float(&s)[NR]) {
-      const int R = b0 + q;
-      float* o = dst + (int64_t)(map ? map[R] : R) * NR;
+  constexpr int G = 32 / LW, RB = 8 * G;  // rows per warp pass
+  const int w = threadIdx.x >> 5, g = (threadIdx.x & 31) / LW;
+  for (int b0 = w * RB; b0 < nr; b0 += WARPS * RB) {
+    // output rows of this lane's row slots, loaded ahead of the row data
+    int orow[8];
 #pragma unroll
-      for (int c = 0; c < NR; ++c) o[c] = s[c];
-    });
+    for (int p = 0; p < 8; ++p) {
+      const int R = b0 + p * G + g;
+      orow[p] = map && R < nr ? map[R] : R;
+    }
+    seg_rows<NR, LW, 8>(V + b0 * m4, m4, min(RB, nr - b0), len4, xs,
+                        [&](int p, int, const float(&s)[NR]) {
+                          float* o = dst + (int64_t)orow[p] * NR;
+#pragma unroll
+                          for (int c = 0; c < NR; ++c) o[c] = s[c];
+                        });
+  }
 }
 
 // Forward far field, input side: for item (a, ci, r0, nr), rows r0 .. r0+nr of
@@ -233,15 +241,15 @@ __global__ void k_tred(GemvOp op, const int32_t* __restrict__ boxes, const float
 template <int NR>
 __device__ __forceinline__ void stage_near_x(const GemvOp& op, int64_t k, const float* __restrict__ xg,
                                              float* xn) {
-  int64_t col = 0;
-  for (int sl = 0; sl < 27; ++sl) {
+  const int lane = threadIdx.x & 31;
+  for (int sl = threadIdx.x >> 5; sl < 27; sl += WARPS) {  // one slot per warp
+    const int64_t off = op.near_off[27 * k + sl];
+    if (off < 0) continue;
+    const int64_t col = off - op.near_base[k];
     const int64_t nn = sl < 26 ? (int64_t)op.nbr_leaf[k * 26 + sl] : k;
-    if (nn < 0) continue;
     const int64_t e0 = op.leaf_off[nn];
     const int ne = (int)(op.leaf_off[nn + 1] - e0), ne4 = (ne + 3) & ~3;
-    for (int e = threadIdx.x; e < ne4 * NR; e += THREADS)
-      xn[col * NR + e] = e < ne * NR ? xg[e0 * NR + e] : 0.f;
-    col += ne4;
+    for (int e = lane; e < ne4 * NR; e += 32) xn[col * NR + e] = e < ne * NR ? xg[e0 * NR + e] : 0.f;
   }
 }
 
@@ -252,7 +260,7 @@ __device__ __forceinline__ void near_rows(const GemvOp& op, int64_t k, int i0, i
                                           const float* xn, double* ya) {
   const int ld = op.near_ld[k];
   seg_rows_any<NR>(op.knear + op.near_base[k] + (int64_t)i0 * ld, ld, nrows, ld / 4, xn,
-                   [&](int q, const float(&s)[NR]) {
+                   [&](int, int q, const float(&s)[NR]) {
 #pragma unroll
                      for (int c = 0; c < NR; ++c) ya[q * NR + c] += (double)s[c];
                    });
@@ -274,6 +282,17 @@ __global__ void __launch_bounds__(THREADS) k_uy(GemvOp op, const float* __restri
   const int64_t t0 = op.leaf_off[k];
   const int nk = (int)(op.leaf_off[k + 1] - t0);
   if (nk == 0) return;
+  // per level: the U row of the leaf's first point, R_b, the T rows (times NR)
+  __shared__ int64_t lu[kMaxLevels + 1], lt[kMaxLevels + 1];
+  __shared__ int lr[kMaxLevels + 1];
+  if (threadIdx.x >= 1 && threadIdx.x <= d) {
+    const int j = threadIdx.x, sh = 3 * (d - j);
+    const int64_t kb = k >> sh, b = level_base(j) + kb;
+    const int R = op.rbox[b];
+    lr[j] = R;
+    lu[j] = op.ubox_off[b] + (t0 - op.leaf_off[kb << sh]) * R;
+    lt[j] = op.tbase[b] * NR;
+  }
   stage_near_x<NR>(op, k, xg, xn);
   __syncthreads();
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -283,13 +302,10 @@ __global__ void __launch_bounds__(THREADS) k_uy(GemvOp op, const float* __restri
     for (int e = lane; e < ROWS * NR; e += 32) ya[e] = 0.0;
     __syncwarp();
     for (int j = 1; j <= d; ++j) {
-      const int sh = 3 * (d - j);
-      const int64_t kb = k >> sh, b = level_base(j) + kb;
-      const int R = op.rbox[b];
+      const int R = lr[j];
       if (R == 0) continue;
-      const int64_t box0 = op.leaf_off[kb << sh];
-      const float* U = op.u32 + op.ubox_off[b] + (t0 + i0 - box0) * R;
-      seg_rows_any<NR>(U, R, nrows, R / 4, T + op.tbase[b] * NR, [&](int q, const float(&s)[NR]) {
+      const float* U = op.u32 + lu[j] + (int64_t)i0 * R;
+      seg_rows_any<NR>(U, R, nrows, R / 4, T + lt[j], [&](int, int q, const float(&s)[NR]) {
 #pragma unroll
         for (int c = 0; c < NR; ++c) ya[q * NR + c] += (double)s[c];
       });
@@ -506,23 +522,35 @@ __global__ void __launch_bounds__(THREADS) k_vy(GemvOp op, const float* __restri
   const int64_t t0 = op.leaf_off[k];
   const int nk = (int)(op.leaf_off[k + 1] - t0);
   if (nk == 0) return;
+  // per level: the stack rows, the leaf's first column group of the stack,
+  // its row length, the leaf's column window and the stack's T rows
+  __shared__ int64_t lv[kMaxLevels + 1], lm[kMaxLevels + 1], lt[kMaxLevels + 1];
+  __shared__ int lrows[kMaxLevels + 1], llen[kMaxLevels + 1], lsh[kMaxLevels + 1];
+  if (threadIdx.x >= 1 && threadIdx.x <= d) {
+    const int j = threadIdx.x, sh = 3 * (d - j);
+    const int64_t ka = k >> sh, a = level_base(j) + ka;
+    const int64_t box0 = op.leaf_off[ka << sh];
+    const int64_t c0 = t0 - box0, w0 = c0 & ~int64_t(3);
+    lrows[j] = op.vbox_rows[a];
+    lm[j] = (op.leaf_off[(ka + 1) << sh] - box0 + 3) & ~int64_t(3);
+    llen[j] = (int)((((c0 + nk + 3) & ~int64_t(3)) - w0) / 4);
+    lsh[j] = (int)(c0 - w0);
+    lv[j] = op.vbox_off[a] + w0;
+    lt[j] = op.vrow0[a] * NR;
+  }
   for (int e = threadIdx.x; e < WARPS * nep * NR; e += THREADS) far[e] = 0.0;
   stage_near_x<NR>(op, k, xg, xn);
   __syncthreads();
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double* fw = far + (int64_t)w * nep * NR;
   for (int j = 1; j <= d; ++j) {
-    const int sh = 3 * (d - j);
-    const int64_t ka = k >> sh, a = level_base(j) + ka;
-    const int rows = op.vbox_rows[a];
+    const int rows = lrows[j];
     if (rows == 0) continue;
-    const int64_t box0 = op.leaf_off[ka << sh];
-    const int64_t m4 = (op.leaf_off[(ka + 1) << sh] - box0 + 3) & ~int64_t(3);
-    const int64_t c0 = t0 - box0, w0 = c0 & ~int64_t(3);
-    const int len4 = (int)((((c0 + nk + 3) & ~int64_t(3)) - w0) / 4);
-    const float* V = op.v32 + op.vbox_off[a] + w0;
-    const float* Tv = T + op.vrow0[a] * NR;
-    const int shift = (int)(c0 - w0);
+    const int64_t m4 = lm[j];
+    const int len4 = llen[j];
+    const float* V = op.v32 + lv[j];
+    const float* Tv = T + lt[j];
+    const int shift = lsh[j];
     if (len4 > 16)
       stack_cols<NR, 32>(V, m4, rows, Tv, len4, shift, nk, fw);
     else if (len4 > 8)
