@@ -263,6 +263,12 @@ def level_bytes(H, nr_pad, s):
         "ta_leaf": v_leaf + xb + t_leaf,
         "ut_tc": u_up + t_up + ynl,
         "leaf_tc": u_leaf + near + t_leaf + xb + ynl + y,
+        # few-column engine (A x, then A^T x)
+        "vt": v_up + v_leaf + xb + t_up + t_leaf,
+        "uy": u_up + u_leaf + near + t_up + t_leaf + xb + y,
+        "ut": u_up + u_leaf + xb + t_up + t_leaf,
+        "tred_t": t_up,
+        "vy": v_up + v_leaf + near + t_up + t_leaf + xb + y,
     }
     return b
 
@@ -351,6 +357,31 @@ def run_ours(args):
             "algorithmic_bytes": ran,
             "whole_matvec_GBps": sum(ran.values()) / (ms * 1e-3) / 1e9}
 
+    # ---- one right-hand side in the mixed form (few-column engine) --------
+    def kernel_split(fn):
+        H.set_profiling(True)
+        for _ in range(nprof):
+            fn()
+        torch.cuda.synchronize()
+        r = H.profile_report()
+        H.set_profiling(False)
+        return {k: v[1] / v[0] for k, v in r.items()}
+
+    one = {}
+    for name, tr in (("forward", False), ("transpose", True)):
+        ms1 = timed(lambda: H.matvec(x1, "mixed", transpose=tr), max(3, args.steps // 2), 3)
+        k1 = kernel_split(lambda: H.matvec(x1, "mixed", transpose=tr))
+        a1 = level_bytes(H, 1, 4)
+        t1 = max(k1, key=k1.get)
+        ach = a1[t1] / (k1[t1] * 1e-3) / 1e9
+        one[name] = {"ms": ms1, "rhs_per_s": 1e3 / ms1, "kernel_ms": k1,
+                     "top_kernel": f"k_{t1}", "top_achieved_GBps": ach, "top_frac": ach / hbm,
+                     "whole_GBps": sum(a1[k] for k in k1) / (ms1 * 1e-3) / 1e9}
+    d1 = Yd.reshape(len(rows), -1)[:, 0]
+    y1 = H.matvec(x1, "mixed")[ridx]
+    one["forward"]["error_vs_dense_fp64"] = float((torch.linalg.norm(y1 - d1) / torch.linalg.norm(d1)).item())
+    one["speedup_vs_fp64_1rhs"] = ms64 / one["forward"]["ms"]
+
     # ---- GMRES: b = A x_true, x_true U[0,1) ------------------------------
     xt = torch.tensor(charges_uniform(N, nrhs, seed=21), device=dev).reshape(N, nrhs)
     B = H.matvec(xt, "fp64")
@@ -365,12 +396,19 @@ def run_ours(args):
     x64, info64 = H.gmres(b1, maxit=400, tol=1e-10, restart=0, precision="fp64")
     torch.cuda.synchronize()
     t_fp64 = time.perf_counter() - t
+    t = time.perf_counter()
+    x1m, info1 = H.gmres(b1, maxit=300, tol=1e-10, restart=30, precision="mixed")
+    torch.cuda.synchronize()
+    t_mixed1 = time.perf_counter() - t
     gmres = {"mixed_rhs_per_s": nrhs / t_mixed, "mixed_seconds": t_mixed,
              "mixed_iterations": info["iterations"], "mixed_outer": info["outer"],
              "mixed_rel_residual": info["rel_residual"], "mixed_forward_err": fwd_mixed,
              "fp64_rhs_per_s": 1.0 / t_fp64, "fp64_seconds": t_fp64,
              "fp64_iterations": info64["iterations"], "fp64_rel_residual": info64["rel_residual"],
-             "speedup_mixed_batched_vs_fp64": (nrhs / t_mixed) / (1.0 / t_fp64)}
+             "speedup_mixed_batched_vs_fp64": (nrhs / t_mixed) / (1.0 / t_fp64),
+             "mixed_1rhs_seconds": t_mixed1, "mixed_1rhs_iterations": info1["iterations"],
+             "mixed_1rhs_rel_residual": info1["rel_residual"],
+             "speedup_mixed_1rhs_vs_fp64": t_fp64 / t_mixed1}
 
     # ---- e2e through the C ABI with host buffers -------------------------
     # host arrays of the caller, (N, nrhs) by rows; each step copies them in
@@ -404,6 +442,7 @@ def run_ours(args):
             "config": config(args), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(launches), "clocks": clocks,
             "fp64_1rhs": {"rhs_per_s": 1e3 / ms64, "ms": ms64},
+            "mixed_1rhs": one,
             "speedup_mixed_batched_vs_fp64": value / ws / (1e3 / ms64),
             "error_vs_dense_fp64": {"mixed_max_col_rel": err_mixed, "fp64_max_col_rel": err_fp64,
                                     "rows_sampled": len(rows)},

@@ -25,6 +25,7 @@ ERR_NO_DEVICE = 9
 
 FP64 = 0
 MIXED = 1
+FP64X = 2  # FP64-accurate products in FP32-pair arithmetic
 
 
 class Options(ctypes.Structure):

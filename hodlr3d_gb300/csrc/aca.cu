@@ -279,10 +279,11 @@ __global__ void k_aca_compact(const AcaTask* __restrict__ tasks, const int32_t* 
 // FP32 U of every pair (split-exact form) from its FP64 U (n x r,
 // column-major): row-major with row stride us[p] (the sum of the padded ranks
 // of the pairs of its target box, whose U share the rows), its r columns
-// followed by zeros up to round4(r), at u32[p]; one block per pair.
+// followed by zeros up to round4(r), at u32[p]; one block per pair.  lo != 0:
+// the remainders instead, FP64 value minus the split-exact value, rounded.
 __global__ void k_u32(const double* const* __restrict__ u64, float* const* __restrict__ u32,
                       const int32_t* __restrict__ nsize, const int32_t* __restrict__ us,
-                      const int32_t* __restrict__ rank) {
+                      const int32_t* __restrict__ rank, int lo) {
   const int64_t p = blockIdx.x;
   const int r = rank[p];
   if (r <= 0) return;
@@ -293,15 +294,21 @@ __global__ void k_u32(const double* const* __restrict__ u64, float* const* __res
   for (int64_t e = threadIdx.x; e < n * rp; e += blockDim.x) {
     const int64_t i = e / rp;
     const int l = (int)(e - i * rp);
-    dst[i * st + l] = l < r ? tf32_split_value(src[(int64_t)l * n + i]) : 0.f;
+    float v = 0.f;
+    if (l < r) {
+      const double a = src[(int64_t)l * n + i];
+      v = lo ? (float)(a - (double)tf32_split_value(a)) : tf32_split_value(a);
+    }
+    dst[i * st + l] = v;
   }
 }
 
 // FP32 V of every pair (split-exact form) from its FP64 V (m x r,
 // column-major): column-major with the leading dimension padded to
-// mp = round4(m), padding zero, at v32[p]; one block per pair.
+// mp = round4(m), padding zero, at v32[p]; one block per pair.  lo != 0: the
+// remainders, as k_u32.
 __global__ void k_v32(const double* const* __restrict__ v64, float* const* __restrict__ v32,
-                      const int32_t* __restrict__ msize, const int32_t* __restrict__ rank) {
+                      const int32_t* __restrict__ msize, const int32_t* __restrict__ rank, int lo) {
   const int64_t p = blockIdx.x;
   const int r = rank[p];
   if (r <= 0) return;
@@ -310,7 +317,12 @@ __global__ void k_v32(const double* const* __restrict__ v64, float* const* __res
   float* dst = v32[p];
   for (int64_t e = threadIdx.x; e < mp * r; e += blockDim.x) {
     const int64_t l = e / mp, i = e - l * mp;
-    dst[e] = i < m ? tf32_split_value(src[l * m + i]) : 0.f;
+    float v = 0.f;
+    if (i < m) {
+      const double a = src[l * m + i];
+      v = lo ? (float)(a - (double)tf32_split_value(a)) : tf32_split_value(a);
+    }
+    dst[e] = v;
   }
 }
 
@@ -344,16 +356,16 @@ cudaError_t launch_aca_compact(cudaStream_t s, int ntasks, const AcaTask* tasks,
 }
 
 cudaError_t launch_u32(cudaStream_t s, int64_t npairs, const double* const* u64, float* const* u32,
-                       const int32_t* nsize, const int32_t* us, const int32_t* rank) {
+                       const int32_t* nsize, const int32_t* us, const int32_t* rank, int lo) {
   if (npairs <= 0) return cudaSuccess;
-  k_u32<<<(unsigned)npairs, 256, 0, s>>>(u64, u32, nsize, us, rank);
+  k_u32<<<(unsigned)npairs, 256, 0, s>>>(u64, u32, nsize, us, rank, lo);
   return cudaGetLastError();
 }
 
 cudaError_t launch_v32(cudaStream_t s, int64_t npairs, const double* const* v64, float* const* v32,
-                       const int32_t* msize, const int32_t* rank) {
+                       const int32_t* msize, const int32_t* rank, int lo) {
   if (npairs <= 0) return cudaSuccess;
-  k_v32<<<(unsigned)npairs, 256, 0, s>>>(v64, v32, msize, rank);
+  k_v32<<<(unsigned)npairs, 256, 0, s>>>(v64, v32, msize, rank, lo);
   return cudaGetLastError();
 }
 

@@ -34,11 +34,12 @@ cudaError_t launch_aca(cudaStream_t s, int block, int grid, const AcaTask* tasks
 cudaError_t launch_aca_compact(cudaStream_t s, int ntasks, const AcaTask* tasks,
                                const int32_t* rank, const int64_t* dst_off, const double* ws,
                                double* out64);
-// FP32 U of every pair from its FP64 U (see k_u32 in aca.cu)
+// FP32 U of every pair from its FP64 U, or (lo) the remainders (see k_u32
+// in aca.cu)
 cudaError_t launch_u32(cudaStream_t s, int64_t npairs, const double* const* u64, float* const* u32,
-                       const int32_t* nsize, const int32_t* us, const int32_t* rank);
-// FP32 V of every pair from its FP64 V (see k_v32 in aca.cu)
+                       const int32_t* nsize, const int32_t* us, const int32_t* rank, int lo);
+// FP32 V of every pair from its FP64 V, or (lo) the remainders (see k_v32)
 cudaError_t launch_v32(cudaStream_t s, int64_t npairs, const double* const* v64, float* const* v32,
-                       const int32_t* msize, const int32_t* rank);
+                       const int32_t* msize, const int32_t* rank, int lo);
 
 }  // namespace h3d

@@ -188,6 +188,11 @@ struct hodlr3d_handle {
   // h_ustride[p] = R_b.  The tensor-core T uses the same grouping: T of box b
   // is 32 x R_b at 32-wide offset h_tbox_off[b].
   DevBuf* u32_pool = nullptr;
+  // FP64-accurate form: lo parts of the FP32 copies (FP64 value minus the
+  // FP32 value, rounded), same layouts; built on first use
+  DevBuf u32lo_pool, v32lo_pool, knearlo;
+  bool lo_built = false;
+  std::vector<int32_t> h_pair_m, h_pair_n;  // per pair: source and target box sizes
   std::vector<int64_t> h_ubox_off, h_tbox_off;
   std::vector<int32_t> h_rbox, h_ustride, h_coff;
   DevBuf ustride, tc_toff, tc_tld, tc_tbox, tc_rbox;
@@ -250,7 +255,8 @@ struct hodlr3d_handle {
   bool gemv_built = false;
   bool gemv_ok = false;          // tree and layouts fit the few-column kernels
   DevBuf gv_ubox_off, gv_vbox_off, gv_vbox_rows, gv_vrow0, gv_vrow_t, gv_trow_v, gv_tbase, gv_vpofs,
-      gv_upofs, gv_vt_items, gv_vt_upper, gv_ut_items, gv_ut_upper, gv_x, gv_t, gv_tt, gv_p, gv_pt;
+      gv_upofs, gv_vt_items, gv_vt_upper, gv_ut_items, gv_ut_upper, gv_x, gv_t, gv_tt, gv_p, gv_pt,
+      gv_xl, gv_tl, gv_ttl, gv_pd, gv_ptd;
   int64_t gv_n_vt_items = 0, gv_n_vt_upper = 0, gv_n_ut_items = 0, gv_n_ut_upper = 0;
   // GMRES work buffers
   DevBuf g_Q, g_w, g_r, g_x, g_b, g_H, g_cs, g_sn, g_beta, g_hk, g_bnorm, g_err, g_part, g_y,
@@ -471,6 +477,9 @@ int group_fp32(hodlr3d_t h) {
   h->h_vbox_off[nbox] = vcur;
   h->h_ubox_off[nbox] = ucur;
   h->h_tbox_off[nbox] = tcur;
+  h->h_pair_m = msize;
+  h->h_pair_n = nsize;
+  h->lo_built = false;
   h->v32_pool = new DevBuf();
   h->pools.push_back(h->v32_pool);
   H3D_CUDA(h->v32_pool->ensure(sizeof(float) * std::max<int64_t>(vcur, 4)));
@@ -502,9 +511,9 @@ int group_fp32(hodlr3d_t h) {
     H3D_CUDA(cudaMemcpy(dn.p, nsize.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice));
     H3D_CUDA(cudaMemcpy(dus.p, h->h_ustride.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice));
     H3D_CUDA(h3d::launch_v32(s, np, d64.as<const double* const>(), d32.as<float* const>(),
-                             dm.as<int32_t>(), dr.as<int32_t>()));
+                             dm.as<int32_t>(), dr.as<int32_t>(), 0));
     H3D_CUDA(h3d::launch_u32(s, np, du64.as<const double* const>(), du32.as<float* const>(),
-                             dn.as<int32_t>(), dus.as<int32_t>(), dr.as<int32_t>()));
+                             dn.as<int32_t>(), dus.as<int32_t>(), dr.as<int32_t>(), 0));
     h->launches += 2;
     H3D_CUDA(cudaStreamSynchronize(s));
   }
@@ -948,7 +957,7 @@ int ensure_gemv(hodlr3d_t h, cudaStream_t s) {
   h->gemv_built = true;
   h->gemv_ok = false;
   const int ml4 = (h->max_leaf + 3) & ~3;
-  if (h3d::gemv_vy_smem(ml4, 4) > 200 * 1024) return HODLR3D_OK;
+  if (h3d::gemv_smem_bytes(ml4, 4, true) > 200 * 1024) return HODLR3D_OK;
   const int64_t np = h->npairs;
   const int64_t nbox = (int64_t)h->h_vbox_rows.size();
   const int64_t trows = h->h_tbox_off[nbox] / 32;
@@ -1044,6 +1053,63 @@ int ensure_gemv(hodlr3d_t h, cudaStream_t s) {
   return HODLR3D_OK;
 }
 
+// The FP64-accurate form's lo parts (U, V, near field) and its work buffers,
+// built on first use after each assembly.
+int ensure_lo(hodlr3d_t h, const h3d::NearOp& nr, cudaStream_t s) {
+  if (h->lo_built) return HODLR3D_OK;
+  const int64_t np = h->npairs;
+  const float* ubase = h->u32_pool->as<float>();
+  const float* vbase = h->v32_pool->as<float>();
+  H3D_CUDA(h->u32lo_pool.ensure(h->u32_pool->bytes));
+  H3D_CUDA(h->v32lo_pool.ensure(h->v32_pool->bytes));
+  if (np) {
+    std::vector<float*> ulo(np), vlo(np);
+    for (int64_t p = 0; p < np; ++p) {
+      ulo[p] = h->u32lo_pool.as<float>() + (h->h_u32[p] - ubase);
+      vlo[p] = h->v32lo_pool.as<float>() + (h->h_v32[p] - vbase);
+    }
+    DevBuf d64, dlo, dsz, dr, dus;
+    H3D_CUDA(d64.ensure(sizeof(void*) * np));
+    H3D_CUDA(dlo.ensure(sizeof(void*) * np));
+    H3D_CUDA(dsz.ensure(sizeof(int32_t) * np));
+    H3D_CUDA(dr.ensure(sizeof(int32_t) * np));
+    H3D_CUDA(dus.ensure(sizeof(int32_t) * np));
+    H3D_CUDA(cudaMemcpy(dr.p, h->h_rank.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(cudaMemcpy(dus.p, h->h_ustride.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice));
+    // V
+    H3D_CUDA(cudaMemcpy(d64.p, h->h_v64.data(), sizeof(void*) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(cudaMemcpy(dlo.p, vlo.data(), sizeof(void*) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(cudaMemcpy(dsz.p, h->h_pair_m.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(h3d::launch_v32(s, np, d64.as<const double* const>(), dlo.as<float* const>(),
+                             dsz.as<int32_t>(), dr.as<int32_t>(), 1));
+    H3D_CUDA(cudaStreamSynchronize(s));
+    // U
+    H3D_CUDA(cudaMemcpy(d64.p, h->h_u64.data(), sizeof(void*) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(cudaMemcpy(dlo.p, ulo.data(), sizeof(void*) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(cudaMemcpy(dsz.p, h->h_pair_n.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(h3d::launch_u32(s, np, d64.as<const double* const>(), dlo.as<float* const>(),
+                             dsz.as<int32_t>(), dus.as<int32_t>(), dr.as<int32_t>(), 1));
+    H3D_CUDA(cudaStreamSynchronize(s));
+    h->launches += 2;
+  }
+  H3D_CUDA(h->knearlo.ensure(sizeof(float) * std::max<int64_t>(h->near_floats, 4)));
+  h->launches += h3d::launch_near_lo(s, h->nleaf, h->leaf_off.as<int32_t>(), nr,
+                                     h->near_off.as<int64_t>(), h->near_ld.as<int32_t>(),
+                                     h->knear.as<float>(), h->knearlo.as<float>());
+  H3D_CUDA(cudaGetLastError());
+  const int64_t nbox = (int64_t)h->h_vbox_rows.size();
+  const int64_t trows = std::max<int64_t>(h->h_tbox_off[nbox] / 32, 1);
+  const size_t gp = h->gv_p.bytes / sizeof(float), gpt = h->gv_pt.bytes / sizeof(float);
+  H3D_CUDA(h->gv_xl.ensure(sizeof(float) * 4 * h->N));
+  H3D_CUDA(h->gv_tl.ensure(sizeof(float) * 4 * trows));
+  H3D_CUDA(cudaMemsetAsync(h->gv_tl.p, 0, sizeof(float) * 4 * trows, s));
+  H3D_CUDA(h->gv_ttl.ensure(h->gv_tt.bytes));
+  H3D_CUDA(h->gv_pd.ensure(sizeof(double) * gp));
+  H3D_CUDA(h->gv_ptd.ensure(sizeof(double) * gpt));
+  h->lo_built = true;
+  return HODLR3D_OK;
+}
+
 // largest column counts the few-column engine takes in the automatic choice
 // (passes of 4 columns; measured at 64^3: 7.9 ms for 4 columns against 10.4
 // ms for the tensor cores' 32, and 8.7 ms per 4 transposed columns against
@@ -1057,10 +1123,13 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
   if (!x || !y) return set_error(HODLR3D_ERR_INVALID_ARG, "null vector");
   if (nrhs < 1 || nrhs > 64) return set_error(HODLR3D_ERR_INVALID_ARG, "nrhs must be in 1..64");
   if (ld < h->N) return set_error(HODLR3D_ERR_INVALID_ARG, "ld < n");
-  if (precision != HODLR3D_FP64 && precision != HODLR3D_MIXED)
+  if (precision != HODLR3D_FP64 && precision != HODLR3D_MIXED && precision != HODLR3D_FP64X)
     return set_error(HODLR3D_ERR_INVALID_ARG, "unknown precision %d", precision);
   if (precision == HODLR3D_MIXED && !h->opt.keep_fp32)
     return set_error(HODLR3D_ERR_INVALID_ARG, "mixed precision needs keep_fp32");
+  // the FP64-accurate form builds on the FP32 copies; without them, or on a
+  // tree the few-column kernels do not take, it is the FP64 form
+  if (precision == HODLR3D_FP64X && !h->opt.keep_fp32) precision = HODLR3D_FP64;
   H3D_TRY(ensure_matvec_buffers(h, nrhs));
   const bool f32 = precision == HODLR3D_MIXED;
   h3d::FarOp far{};
@@ -1109,14 +1178,21 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
   // kGemvTransposeMax columns the CUDA-core kernels (all columns in one pass)
   // are faster.
   const bool mixed = precision == HODLR3D_MIXED;
+  const bool fp64x = precision == HODLR3D_FP64X;
   bool use_gemv = false;
-  if (mixed && (h->engine == 3 ||
-                (h->engine == 0 && nrhs <= (trans ? kGemvTransposeMax : kGemvForwardMax)))) {
+  if (fp64x || (mixed && (h->engine == 3 || (h->engine == 0 &&
+                                             nrhs <= (trans ? kGemvTransposeMax : kGemvForwardMax))))) {
     H3D_TRY(ensure_near_blocks(h, nr, s));
     H3D_TRY(ensure_gemv(h, s));
     use_gemv = h->gemv_ok;
+    if (use_gemv && fp64x) H3D_TRY(ensure_lo(h, nr, s));
   }
-  if (h->engine == 3 && !use_gemv)
+  if (fp64x && !use_gemv) {
+    precision = HODLR3D_FP64;
+    far.ufac = h->u64.as<const void*>();
+    far.vfac = h->v64.as<const void*>();
+  }
+  if (h->engine == 3 && !use_gemv && !fp64x)
     return set_error(HODLR3D_ERR_UNSUPPORTED,
                      "the few-column engine needs the mixed form, leaves whose near-field inputs "
                      "fit its shared memory and fewer than 2^31 rows of T");
@@ -1142,6 +1218,9 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
     g.vpofs = h->gv_vpofs.as<int64_t>();
     g.upofs = h->gv_upofs.as<int64_t>();
     g.knear = h->knear.as<float>();
+    g.u32lo = fp64x ? h->u32lo_pool.as<float>() : nullptr;
+    g.v32lo = fp64x ? h->v32lo_pool.as<float>() : nullptr;
+    g.knearlo = fp64x ? h->knearlo.as<float>() : nullptr;
     g.near_base = h->near_base.as<int64_t>();
     g.near_ld = h->near_ld.as<int32_t>();
     g.near_off = h->near_off.as<int64_t>();
@@ -1151,6 +1230,11 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
     gb.tt = h->gv_tt.as<float>();
     gb.p = h->gv_p.as<float>();
     gb.pt = h->gv_pt.as<float>();
+    gb.xl = h->gv_xl.as<float>();
+    gb.tl = h->gv_tl.as<float>();
+    gb.ttl = h->gv_ttl.as<float>();
+    gb.pd = h->gv_pd.as<double>();
+    gb.ptd = h->gv_ptd.as<double>();
     gb.vt_items = h->gv_vt_items.as<int4>();
     gb.n_vt_items = h->gv_n_vt_items;
     gb.vt_upper = h->gv_vt_upper.as<int32_t>();
@@ -1161,7 +1245,7 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
     gb.n_ut_upper = h->gv_n_ut_upper;
     for (int c0 = 0; c0 < nrhs; c0 += 4)
       h->launches += h3d::launch_matvec_gemv(s, g, gb, x + c0 * ld, ld, y + c0 * ld, ld,
-                                             std::min(4, nrhs - c0), trans,
+                                             std::min(4, nrhs - c0), trans, fp64x,
                                              h->profiling ? &h->prof : nullptr);
     H3D_CUDA(cudaGetLastError());
     return HODLR3D_OK;
@@ -1438,10 +1522,11 @@ int hodlr3d_matvec_noalloc(hodlr3d_t h, const double* x, double* y, int nrhs, in
   if (!x || !y) return set_error(HODLR3D_ERR_INVALID_ARG, "null vector");
   if (nrhs < 1 || nrhs > 64) return set_error(HODLR3D_ERR_INVALID_ARG, "nrhs must be in 1..64");
   if (ld < h->N) return set_error(HODLR3D_ERR_INVALID_ARG, "ld < n");
-  if (precision != HODLR3D_FP64 && precision != HODLR3D_MIXED)
+  if (precision != HODLR3D_FP64 && precision != HODLR3D_MIXED && precision != HODLR3D_FP64X)
     return set_error(HODLR3D_ERR_INVALID_ARG, "unknown precision %d", precision);
   if (precision == HODLR3D_MIXED && !h->opt.keep_fp32)
     return set_error(HODLR3D_ERR_INVALID_ARG, "mixed precision needs keep_fp32");
+  if (precision == HODLR3D_FP64X) precision = HODLR3D_FP64;  // the CUDA-core kernels only
   // the work buffers of the product, carved from the fixed scratch array
   const int nr = h3d::padded_nrhs(nrhs);
   const size_t s_real = precision == HODLR3D_MIXED ? sizeof(float) : sizeof(double);
@@ -1588,13 +1673,13 @@ int hodlr3d_gmres(hodlr3d_t h, const double* b, double* x, int nrhs, int64_t ld,
   int total_it = 0, outer = 0;
   bool brk = false, converged = false;
   double final_err = 0.0;
-  if (prm->precision == HODLR3D_FP64) {
+  if (prm->precision == HODLR3D_FP64 || prm->precision == HODLR3D_FP64X) {
     const int m = prm->restart > 0 ? prm->restart : prm->maxit;
     bool first = true;
     while (total_it < prm->maxit) {
       int it = 0;
       const int mm = std::min(m, prm->maxit - total_it);
-      H3D_TRY(gmres_cycle(h, h->g_b.as<double>(), h->g_x.as<double>(), nrhs, mm, prm->tol, HODLR3D_FP64,
+      H3D_TRY(gmres_cycle(h, h->g_b.as<double>(), h->g_x.as<double>(), nrhs, mm, prm->tol, prm->precision,
                           trans, first, bnorm, &it, err, hp, &brk));
       first = false;
       total_it += it;
@@ -1642,8 +1727,9 @@ int hodlr3d_gmres(hodlr3d_t h, const double* b, double* x, int nrhs, int64_t ld,
       }
       total_it += inner_total;
       h->launches += h3d::gmres_add(s, vec, dx.as<double>(), h->g_x.as<double>());
-      // r = b - A x in FP64
-      H3D_TRY(matvec_device(h, h->g_x.as<double>(), wtmp.as<double>(), nrhs, N, HODLR3D_FP64, s, trans));
+      // r = b - A x, the product FP64-accurate (FP32-pair arithmetic where the
+      // few-column kernels take the tree, else FP64), the difference in FP64
+      H3D_TRY(matvec_device(h, h->g_x.as<double>(), wtmp.as<double>(), nrhs, N, HODLR3D_FP64X, s, trans));
       h->launches += h3d::gmres_sub(s, vec, h->g_b.as<double>(), wtmp.as<double>(), r);
     }
     if (!converged) {

@@ -162,6 +162,9 @@ struct GemvOp {
   const int64_t* vpofs;       // per box: chunk partials of its V stack (floats / NR), -1 when one chunk
   const int64_t* upofs;       // per box: chunk partials of its U^T X (floats / NR), -1 when one chunk
   const float* knear;         // FP32 near-field blocks (launch_near_blocks)
+  const float* u32lo;         // fp64x: lo parts (FP64 value - FP32 copy), same layouts
+  const float* v32lo;
+  const float* knearlo;
   const int64_t* near_base;   // per leaf: its blocks side by side, nk x near_ld[k] row-major
   const int32_t* near_ld;
   const int64_t* near_off;    // 27 per leaf: start of each block (column near_off - near_base), -1 absent
@@ -169,7 +172,8 @@ struct GemvOp {
 
 // Work buffers: xg N x 4 floats; t: T rows x 4 floats (zeroed once: its
 // padding rows are never written); tt: V-stack rows x 4 floats (the
-// transposed T in stack order); p, pt: chunk partials x 4 floats.
+// transposed T in stack order); p, pt: chunk partials x 4 floats.  The fp64x
+// form adds the lo parts xl, tl (zeroed once), ttl and FP64 partials pd, ptd.
 // Work lists: vt_items (source box, chunk, first row, rows); vt_upper: boxes
 // with chunk partials; ut_items (target box, row chunk); ut_upper likewise.
 struct GemvBuffers {
@@ -178,6 +182,11 @@ struct GemvBuffers {
   float* tt;
   float* p;
   float* pt;
+  float* xl;
+  float* tl;
+  float* ttl;
+  double* pd;
+  double* ptd;
   const int4* vt_items;
   int64_t n_vt_items;
   const int32_t* vt_upper;
@@ -188,12 +197,18 @@ struct GemvBuffers {
   int64_t n_ut_upper;
 };
 
-size_t gemv_uy_smem(int max_leaf4, int nr);
-size_t gemv_vy_smem(int max_leaf4, int nr);
-// nrhs in 1..4.  Returns the number of launches.
+// Largest dynamic shared memory a few-column launch asks for.
+size_t gemv_smem_bytes(int max_leaf4, int nr, bool fp64x);
+// nrhs in 1..4; fp64x: the FP64-accurate form from the FP32 pairs.  Returns
+// the number of launches.
 int launch_matvec_gemv(cudaStream_t s, const GemvOp& op, const GemvBuffers& B, const double* X,
-                       int64_t ldx, double* Y, int64_t ldy, int nrhs, bool trans,
+                       int64_t ldx, double* Y, int64_t ldy, int nrhs, bool trans, bool fp64x,
                        MatvecProfiler* prof);
+// fp64x: lo parts of the near-field blocks, knearlo = K (FP64, as the FP64
+// near field evaluates it) - Knear, same layout.
+int launch_near_lo(cudaStream_t s, int64_t nleaf, const int32_t* leaf_off, const NearOp& near,
+                   const int64_t* near_off, const int32_t* near_ld, const float* Knear,
+                   float* Knearlo);
 
 // precision: 0 = FP64, 1 = mixed.  X, Y column-major in the original order.
 // Returns the number of kernel launches.

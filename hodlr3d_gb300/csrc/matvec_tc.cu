@@ -909,7 +909,44 @@ __global__ void k_near_blocks(const int32_t* __restrict__ leaf_off, NearOp nr,
   }
 }
 
+// lo parts of the near-field blocks for the FP64-accurate few-column form:
+// the FP64 entry (the FP64 near field's formula, from the tree-ordered FP64
+// points) minus the stored FP32 block entry, rounded to FP32
+__global__ void k_near_lo(const int32_t* __restrict__ leaf_off, NearOp nr,
+                          const int64_t* __restrict__ near_off, const int32_t* __restrict__ near_ld,
+                          const float* __restrict__ Knear, float* __restrict__ Knearlo) {
+  const int64_t k = blockIdx.x;
+  const int sl = blockIdx.y;
+  const int64_t off = near_off[k * 27 + sl];
+  if (off < 0) return;
+  const int64_t nn = sl < 26 ? (int64_t)nr.nbr_leaf[k * 26 + sl] : k;
+  const int64_t t0 = leaf_off[k], e0 = leaf_off[nn];
+  const int nk = (int)(leaf_off[k + 1] - t0), ne = (int)(leaf_off[nn + 1] - e0);
+  const int nep = (ne + 3) & ~3;
+  const int64_t ld = near_ld[k];
+  for (int e = threadIdx.x; e < nk * nep; e += blockDim.x) {
+    const int i = e / nep, j = e - i * nep;
+    const int64_t o = off + (int64_t)i * ld + j;
+    double v = 0.0;
+    if (j < ne) {
+      const int64_t ti = t0 + i, ej = e0 + j;
+      v = (nn == k && i == j) ? nr.kd.diag
+                              : entry64_offdiag(nr.kd, __dsub_rn(nr.xs[ti], nr.xs[ej]),
+                                                __dsub_rn(nr.ys[ti], nr.ys[ej]),
+                                                __dsub_rn(nr.zs[ti], nr.zs[ej]));
+    }
+    Knearlo[o] = (float)(v - (double)Knear[o]);
+  }
+}
+
 }  // namespace
+
+int launch_near_lo(cudaStream_t s, int64_t nleaf, const int32_t* leaf_off, const NearOp& near,
+                   const int64_t* near_off, const int32_t* near_ld, const float* Knear,
+                   float* Knearlo) {
+  k_near_lo<<<dim3((unsigned)nleaf, 27), 256, 0, s>>>(leaf_off, near, near_off, near_ld, Knear, Knearlo);
+  return 1;
+}
 
 int tc_max_entries() { return kMaxEntries; }
 

@@ -16,16 +16,16 @@ from typing import Optional
 import numpy as np
 
 from . import _lib
-from ._lib import FP64, MIXED, HODLR3DError, check
+from ._lib import FP64, FP64X, MIXED, HODLR3DError, check
 
-_PREC = {"fp64": FP64, "mixed": MIXED, FP64: FP64, MIXED: MIXED}
+_PREC = {"fp64": FP64, "mixed": MIXED, "fp64x": FP64X, FP64: FP64, MIXED: MIXED, FP64X: FP64X}
 
 
 def _prec(p) -> int:
     try:
         return _PREC[p]
     except KeyError:
-        raise ValueError(f"precision must be 'fp64' or 'mixed', got {p!r}") from None
+        raise ValueError(f"precision must be 'fp64', 'mixed' or 'fp64x', got {p!r}") from None
 
 
 class HODLR3D:

@@ -36,8 +36,13 @@ enum hodlr3d_status {
 };
 
 enum hodlr3d_precision {
-  HODLR3D_FP64 = 0, /* FP64 end to end (matches the reference's FP64 matvec) */
-  HODLR3D_MIXED = 1 /* FP32 factors and near field, FP64 accumulation across tiles */
+  HODLR3D_FP64 = 0,  /* FP64 end to end (matches the reference's FP64 matvec) */
+  HODLR3D_MIXED = 1, /* FP32 factors and near field, FP64 accumulation across tiles */
+  HODLR3D_FP64X = 2  /* FP64-accurate products in FP32-pair arithmetic: every FP64 entry
+                        as hi + lo FP32 values (relative error 2^-46), exact FP32 products
+                        and compensated sums, FP64 across tiles; needs keep_fp32 (without
+                        it, or on a tree the few-column kernels do not take: HODLR3D_FP64).
+                        Agrees with the FP64 form to ~1e-13 relative. */
 };
 
 /* Options of hodlr3d_create; fill with hodlr3d_default_options first. */
@@ -72,8 +77,9 @@ typedef struct hodlr3d_gmres_params {
   int maxit;        /* Krylov iterations (unrestarted) or per cycle when restart > 0 */
   int restart;      /* 0: unrestarted as the reference; m > 0: GMRES(m) */
   double tol;       /* relative residual |r| / |b| to reach */
-  int precision;    /* HODLR3D_FP64: plain GMRES; HODLR3D_MIXED: FP32 inner GMRES(restart)
-                       with FP64 outer residual (iterative refinement) */
+  int precision;    /* HODLR3D_FP64 (or HODLR3D_FP64X): plain GMRES with products of that
+                       form; HODLR3D_MIXED: FP32 inner GMRES(restart) with an FP64-accurate
+                       outer residual (HODLR3D_FP64X products; iterative refinement) */
   int max_outer;    /* HODLR3D_MIXED: refinement steps (0: 20) */
   double inner_tol; /* HODLR3D_MIXED: inner relative tolerance (0: 1e-5) */
   int transpose;    /* solve A^T x = b (adjoint) instead of A x = b */
