@@ -382,6 +382,15 @@ def run_ours(args):
     one["forward"]["error_vs_dense_fp64"] = float((torch.linalg.norm(y1 - d1) / torch.linalg.norm(d1)).item())
     one["speedup_vs_fp64_1rhs"] = ms64 / one["forward"]["ms"]
 
+    # ---- FP64-accurate products in FP32-pair arithmetic (fp64x) ----------
+    msx = timed(lambda: H.matvec(x1, "fp64x"), max(3, args.steps // 2), 3)
+    kx = kernel_split(lambda: H.matvec(x1, "fp64x"))
+    y64, yx = H.matvec(x1, "fp64"), H.matvec(x1, "fp64x")
+    fp64x = {"ms": msx, "rhs_per_s": 1e3 / msx, "kernel_ms": kx,
+             "whole_GBps": 2 * sum(level_bytes(H, 1, 4)[k] for k in kx) / (msx * 1e-3) / 1e9,
+             "rel_diff_vs_fp64": float((torch.linalg.norm(yx - y64) / torch.linalg.norm(y64)).item()),
+             "speedup_vs_fp64_1rhs": ms64 / msx}
+
     # ---- GMRES: b = A x_true, x_true U[0,1) ------------------------------
     xt = torch.tensor(charges_uniform(N, nrhs, seed=21), device=dev).reshape(N, nrhs)
     B = H.matvec(xt, "fp64")
@@ -443,6 +452,7 @@ def run_ours(args):
             "gpu_launches": int(launches), "clocks": clocks,
             "fp64_1rhs": {"rhs_per_s": 1e3 / ms64, "ms": ms64},
             "mixed_1rhs": one,
+            "fp64x_1rhs": fp64x,
             "speedup_mixed_batched_vs_fp64": value / ws / (1e3 / ms64),
             "error_vs_dense_fp64": {"mixed_max_col_rel": err_mixed, "fp64_max_col_rel": err_fp64,
                                     "rows_sampled": len(rows)},
