@@ -22,6 +22,7 @@ ERR_BREAKDOWN = 6
 ERR_NO_CONVERGENCE = 7
 ERR_UNSUPPORTED = 8
 ERR_NO_DEVICE = 9
+ERR_IO = 10
 
 FP64 = 0
 MIXED = 1
@@ -90,6 +91,8 @@ def lib() -> ctypes.CDLL:
                             ctypes.POINTER(vp)], i32),
         "hodlr3d_destroy": ([vp], None),
         "hodlr3d_assemble": ([vp], i32),
+        "hodlr3d_save": ([vp, ctypes.c_char_p], i32),
+        "hodlr3d_load": ([ctypes.c_char_p, ctypes.POINTER(Options), ctypes.POINTER(vp)], i32),
         "hodlr3d_matvec": ([vp, vp, vp, i32, i64, i32, vp], i32),
         "hodlr3d_matvec_host": ([vp, vp, vp, i32, i64, i32], i32),
         "hodlr3d_matvec_host_rows": ([vp, vp, vp, i32, i32], i32),
@@ -135,3 +138,18 @@ def default_options(device: int = 0, diag_override: float = math.nan, keep_fp32:
     o.aca_workspace_bytes = aca_workspace_bytes
     o.rank_cap = rank_cap
     return o
+
+
+def read_factor_header(path) -> dict:
+    """The parameters stored in a factor file (include/hodlr3d.h, hodlr3d_save):
+    magic, then {version, header bytes, n, nP1D, tol_pow, L, kernel, levels,
+    diag, npairs, npools, reserved, lists hash}."""
+    import struct
+    with open(path, "rb") as f:
+        head = f.read(8 + 72)
+    if len(head) < 80 or head[:8] != b"H3DFACT1":
+        raise HODLR3DError(ERR_IO, f"{path}: not a hodlr3d factor file")
+    v = struct.unpack("<IIqiidiidqiiQ", head[8:80])
+    keys = ("version", "header_bytes", "n", "nP1D", "tol_pow", "L", "kernel", "levels", "diag",
+            "npairs", "npools", "reserved", "lists_hash")
+    return dict(zip(keys, v))

@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import ctypes
 import math
+import os
 from typing import Optional
 
 import numpy as np
@@ -78,6 +79,36 @@ class HODLR3D:
         """ACA of every interaction-list pair (HODLR3D::assemble)."""
         check(self._L.hodlr3d_assemble(self.handle))
         self.assembled = True
+
+    # ---- factor persistence (no reference counterpart) ----------------------
+    def save(self, path) -> None:
+        """Writes the assembled operator (parameters, points, ranks, pivots,
+        FP64 factors) to a versioned binary file (hodlr3d_save)."""
+        check(self._L.hodlr3d_save(self.handle, os.fsencode(path)))
+
+    @classmethod
+    def load(cls, path, *, device: int = 0, keep_fp32: bool = True) -> "HODLR3D":
+        """An assembled operator from a file written by save(): the tree is
+        rebuilt from the saved points and checked against the saved lists; no
+        ACA runs (hodlr3d_load)."""
+        L_ = _lib.lib()
+        opt = _lib.default_options(device, math.nan, keep_fp32, 0, 0)
+        h = ctypes.c_void_p()
+        check(L_.hodlr3d_load(os.fsencode(path), ctypes.byref(opt), ctypes.byref(h)))
+        self = cls.__new__(cls)
+        self._h = h
+        self._L = L_
+        self.device = int(device)
+        st = _lib.Stats()
+        check(L_.hodlr3d_get_stats(h, ctypes.byref(st)))
+        self.N = int(st.n_points)
+        hdr = _lib.read_factor_header(path)
+        self.nParticlesInLeafAlong1D = hdr["nP1D"]
+        self.L = hdr["L"]
+        self.TOL_POW = hdr["tol_pow"]
+        self.Qchoice = hdr["kernel"]
+        self.assembled = True
+        return self
 
     def MatVecProduct(self, b, precision="fp64", out=None) -> np.ndarray:
         """Ab = A b for host arrays b of shape (N,) or (N, nrhs) (HODLR3D::MatVecProduct).

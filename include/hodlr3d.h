@@ -32,7 +32,8 @@ enum hodlr3d_status {
   HODLR3D_ERR_BREAKDOWN = 6,     /* GMRES Arnoldi breakdown (h(k+1,k) == 0) */
   HODLR3D_ERR_NO_CONVERGENCE = 7,/* GMRES stopped at maxit above the tolerance */
   HODLR3D_ERR_UNSUPPORTED = 8,   /* kernel or feature not available on the device */
-  HODLR3D_ERR_NO_DEVICE = 9      /* no usable CUDA device */
+  HODLR3D_ERR_NO_DEVICE = 9,     /* no usable CUDA device */
+  HODLR3D_ERR_IO = 10            /* factor file missing, unreadable, corrupt or not matching */
 };
 
 enum hodlr3d_precision {
@@ -113,6 +114,17 @@ void hodlr3d_destroy(hodlr3d_t h);
  * HODLR3D::assemble -> HODLR3DTree::getUVtTree (src/HODLR3D.cpp:17-19,
  * src/HODLR3DTree.cpp:1621-1645, src/ACA.cpp:127-238). */
 int hodlr3d_assemble(hodlr3d_t h);
+
+/* Factor persistence (no reference counterpart: the reference re-assembles
+ * every run).  hodlr3d_save writes an assembled operator -- parameters,
+ * points, ranks, pivots and FP64 factors -- to a versioned binary file with a
+ * checksum; hodlr3d_load rebuilds the tree from the saved points, checks that
+ * its interaction lists are the saved ones and returns an assembled handle
+ * (FP32 copies re-derived) without running ACA.  opt as hodlr3d_create (its
+ * diag_override is replaced by the saved diagonal).  HODLR3D_ERR_IO on a
+ * missing, truncated, corrupt or mismatching file. */
+int hodlr3d_save(hodlr3d_t h, const char* path);
+int hodlr3d_load(const char* path, const hodlr3d_options* opt, hodlr3d_t* out);
 
 /* ---- products -------------------------------------------------------- */
 /* y = A x for nrhs columns (column-major, leading dimension ld >= n), device
