@@ -54,7 +54,11 @@ __device__ __forceinline__ double entry64_offdiag(const KernelDesc& kd, double d
     case 8: return __ddiv_rn(1.0, __dmul_rn(R2, R2));
     case 9: return log(R);
     case 10: return __dmul_rn(__dmul_rn(R, R), log(R));
+    case 11: return j0(R);  // J_0(kappa R), kappa = 1
+    case 12: return y0(R);  // Y_0(kappa R), kappa = 1
     case 13: return __ddiv_rn(cos(R), R);
+    // K_{1/2}(R) / sqrt(R) = sqrt(pi / (2 R)) e^{-R} / sqrt(R) = sqrt(pi / 2) e^{-R} / R
+    case 14: return __ddiv_rn(__dmul_rn(1.2533141373155002512, exp(-R)), R);
     case 15: return __ddiv_rn(exp(__dmul_rn(-50.0, R)), R);
     case 16: return __dmul_rn(kd.h3, __ddiv_rn(1.0, R));
   }
@@ -82,7 +86,10 @@ __device__ __forceinline__ float entry32_offdiag(const KernelDesc& kd, float dx,
     case 0: return log1pf(R);
     case 9: return logf(R);
     case 10: return R2 * logf(R);
+    case 11: return j0f(R);
+    case 12: return y0f(R);
     case 13: return cosf(R) / R;
+    case 14: return 1.25331414f * __expf(-R) / R;
     case 15: return expf(-50.0f * R) / R;
   }
   return 0.0f;

@@ -278,7 +278,8 @@ int check_handle(hodlr3d_t h) {
   return HODLR3D_OK;
 }
 
-bool kernel_supported(int k) { return (k >= 0 && k <= 10) || k == 13 || k == 15 || k == 16; }
+// every Qchoice of the reference (src/kernel.cpp:65-227) has a device form
+bool kernel_supported(int k) { return k >= 0 && k <= 16; }
 
 // ---------------------------------------------------------------------------
 // tree
@@ -1685,9 +1686,7 @@ int hodlr3d_create(const double* xyz, int64_t n, int nP1D, double L, int tol_pow
   if (nP1D < 1) return set_error(HODLR3D_ERR_INVALID_ARG, "nParticlesInLeafAlong1D must be >= 1");
   if (!(L > 0.0)) return set_error(HODLR3D_ERR_INVALID_ARG, "L must be positive");
   if (tol_pow < 0 || tol_pow > 30) return set_error(HODLR3D_ERR_INVALID_ARG, "TOL_POW out of range");
-  if (kernel_id < 0 || kernel_id > 16) return set_error(HODLR3D_ERR_INVALID_ARG, "unknown Qchoice %d", kernel_id);
-  if (!kernel_supported(kernel_id))
-    return set_error(HODLR3D_ERR_UNSUPPORTED, "Qchoice %d (Bessel function kernel) is not available on the device", kernel_id);
+  if (!kernel_supported(kernel_id)) return set_error(HODLR3D_ERR_INVALID_ARG, "unknown Qchoice %d", kernel_id);
   for (int64_t i = 0; i < 3 * n; ++i)
     if (!std::isfinite(xyz[i])) return set_error(HODLR3D_ERR_NONFINITE, "non-finite coordinate");
   // depth as the reference computes it (src/HODLR3D.cpp:6-7)

@@ -102,8 +102,9 @@ const char* hodlr3d_last_error(void);
  * interaction lists on the device.  Replaces HODLR3D::HODLR3D(nParticlesInLeafAlong1D,
  * L, TOL_POW, Qchoice, particles) (include/HODLR3D.hpp:18, src/HODLR3D.cpp:3-15).
  * xyz: host array of n points, x y z interleaved (the reference's pts3D).
- * kernel_id: the reference's Qchoice (src/kernel.cpp:65-227); 0-10, 13, 15, 16
- * run on the device, 11, 12, 14 (Bessel) return HODLR3D_ERR_UNSUPPORTED. */
+ * kernel_id: the reference's Qchoice 0-16 (src/kernel.cpp:65-227), all evaluated on
+ * the device (11, 12: J0, Y0 of CUDA's math library; 14: K_{1/2}(r)/sqrt(r) in
+ * its closed form sqrt(pi/2) e^{-r} / r). */
 int hodlr3d_create(const double* xyz, int64_t n, int nP1D, double L, int tol_pow, int kernel_id,
                    const hodlr3d_options* opt, hodlr3d_t* out);
 

@@ -42,6 +42,10 @@ CASES = {
     "grid32_q16_tol10": ("grid_cell_centres", (32,), 4, 1.0, 10, 16, "nan", 0, False),
     # depth 4 with one point per leaf, domain half-width 2
     "grid16_leaf1_q4_tol8": ("grid_cell_centres", (16, 2.0), 1, 2.0, 8, 4, "nan", 0, False),
+    # the Bessel-function kernels: J0(r), Y0(r), K_{1/2}(r)/sqrt(r)
+    "grid16_q11_tol8": ("grid_cell_centres", (16,), 4, 1.0, 8, 11, "nan", 0, True),
+    "grid16_q12_tol8": ("grid_cell_centres", (16,), 4, 1.0, 8, 12, "nan", 0, True),
+    "grid16_q14_tol8": ("grid_cell_centres", (16,), 4, 1.0, 8, 14, "nan", 0, True),
 }
 
 

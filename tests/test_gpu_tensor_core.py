@@ -46,7 +46,13 @@ def test_tc_matches_simt_engine(case, nrhs):
     ya = H.matvec(X, "mixed")
     H.device_status()
     err = (torch.linalg.norm(yt - ys, dim=0) / torch.linalg.norm(ys, dim=0)).max().item()
-    assert err <= 2e-6, err
+    # J0 / Y0 (Qchoice 11, 12): smooth oscillatory blocks whose ACA factors
+    # cancel (|U||V^T| >> |K|), so the engines' per-entry FP32 / 3xTF32
+    # roundings differ by more relative to K x with N(0,1) charges (measured
+    # 3.8e-6 at 16^3); both stay within 2e-6 of the reference's FP64 product
+    # on its own charges (test_tc_matches_reference_fp64)
+    tol = 1e-5 if int(g["kernel"]) in (11, 12) else 2e-6
+    assert err <= tol, err
     assert torch.equal(ya, yt)  # the automatic choice is the tensor-core engine here
 
 

@@ -52,12 +52,15 @@ def test_invalid_arguments_fail_cleanly():
     # bad kernel id
     code = L.hodlr3d_create(pts.ctypes.data, 10, 4, 1.0, 10, 42, None, ctypes.byref(h))
     assert code == _lib.ERR_INVALID_ARG and not h.value
-    # Bessel kernels are not offered on the device
-    code = L.hodlr3d_create(pts.ctypes.data, 10, 4, 1.0, 10, 11, None, ctypes.byref(h))
-    assert code == _lib.ERR_UNSUPPORTED
-    assert b"Bessel" in L.hodlr3d_last_error()
+    code = L.hodlr3d_create(pts.ctypes.data, 10, 4, 1.0, 10, -1, None, ctypes.byref(h))
+    assert code == _lib.ERR_INVALID_ARG and not h.value
     # null handle
     assert L.hodlr3d_assemble(None) == _lib.ERR_INVALID_ARG
+    # factor files: bad arguments and a missing file fail before any device work
+    assert L.hodlr3d_save(None, b"x.h3d") == _lib.ERR_INVALID_ARG
+    assert L.hodlr3d_load(None, None, ctypes.byref(h)) == _lib.ERR_INVALID_ARG
+    assert L.hodlr3d_load(b"/nonexistent/op.h3d", None, ctypes.byref(h)) == _lib.ERR_IO
+    assert not h.value and b"cannot open" in L.hodlr3d_last_error()
 
 
 def test_no_device_or_tree_error_is_reported():
