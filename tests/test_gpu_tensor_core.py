@@ -1,10 +1,12 @@
 """The tensor-core engine (tcgen05 kind::tf32, 3xTF32) of the mixed-precision
 matvec against the CUDA-core engine and the reference's FP64 matvec.
 
-The engine takes A x with 17..32 right-hand sides on trees whose leaf
-populations are multiples of 4 (16-byte aligned FP32 operand rows); other
-cases are refused with HODLR3D_ERR_UNSUPPORTED when it is forced, and the
-automatic choice routes them to the CUDA-core engine."""
+The engine takes A x in batches of up to 32 right-hand sides on trees whose
+leaf populations are multiples of 4 (16-byte aligned FP32 operand rows); the
+automatic choice gives it A x with more than 4 columns (fewer go to the
+few-column kernels).  Other cases are refused with HODLR3D_ERR_UNSUPPORTED
+when it is forced, and the automatic choice routes them to the CUDA-core
+engine."""
 import numpy as np
 import pytest
 import torch
