@@ -51,11 +51,11 @@ namespace {
 constexpr int THREADS = 256;
 constexpr int WARPS = THREADS / 32;
 
-// rows per warp in the output kernels (fewer for the fp64x form with 4
-// columns, whose accumulators are twice as many)
+// rows per warp in the output kernels (fewer for the fp64x form, whose
+// accumulators and loads are twice as many)
 template <int NR, bool DF>
 __host__ __device__ constexpr int rows_per_warp() {
-  return DF && NR == 4 ? 4 : 8;
+  return DF ? 4 : 8;
 }
 
 __device__ __forceinline__ int level_of(int64_t box, int levels) {
