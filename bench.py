@@ -333,6 +333,24 @@ def run_ours(args):
     ms_max = max_over_ranks(ws, ms)
     value = ws * nrhs / (ms_max * 1e-3)
 
+    # ---- the same product replayed from a CUDA graph (captured once) -------
+    graph = None
+    try:
+        side = torch.cuda.Stream()
+        side.wait_stream(stream)
+        with torch.cuda.stream(side):
+            H.matvec(X, "mixed")
+        stream.wait_stream(side)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            Yg = H.matvec(X, "mixed")
+        msg = timed(g.replay, args.steps, args.warmup)
+        graph = {"ms": msg, "rhs_per_s": nrhs / (msg * 1e-3),
+                 "matches_eager": bool(torch.equal(Yg, H.matvec(X, "mixed")))}
+        del g
+    except RuntimeError as e:  # capture refused by the runtime: report, keep going
+        graph = {"error": str(e)[:200]}
+
     # ---- FP64 form, one right-hand side ----------------------------------
     ms64 = timed(lambda: H.matvec(x1, "fp64"), max(3, args.steps // 2), 2)
 
@@ -451,6 +469,7 @@ def run_ours(args):
             "config": config(args), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(launches), "clocks": clocks,
             "fp64_1rhs": {"rhs_per_s": 1e3 / ms64, "ms": ms64},
+            "cuda_graph": graph,
             "mixed_1rhs": one,
             "fp64x_1rhs": fp64x,
             "speedup_mixed_batched_vs_fp64": value / ws / (1e3 / ms64),
