@@ -99,7 +99,8 @@ def dist_init():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if ws > 1:
         import torch.distributed as dist
-        dist.init_process_group("nccl" if os.environ.get("H3D_BACKEND") != "gloo" else "gloo")
+        if not dist.is_initialized():
+            dist.init_process_group("nccl" if os.environ.get("H3D_BACKEND") != "gloo" else "gloo")
     return ws, rank, local
 
 
@@ -114,7 +115,8 @@ def max_over_ranks(ws, v: float) -> float:
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"  # gloo reduces host tensors
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
