@@ -12,6 +12,7 @@
 
 #include <cmath>
 #include <stdexcept>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -62,7 +63,9 @@ class HODLR3D {
   hodlr3d_gb300::TreeView tree;  // stands in for the reference's A (HODLR3DTree*)
   hodlr3d_gb300::TreeView* A;
   int N;
-  int precision = HODLR3D_FP64;  // HODLR3D_MIXED selects the FP32 factors
+  // HODLR3D_MIXED selects the FP32 factors; HODLR3D_FP64X FP64-accurate
+  // products in FP32-pair arithmetic
+  int precision = HODLR3D_FP64;
 
   HODLR3D(int nParticlesInLeafAlong1D, double L, int TOL_POW, int Qchoice,
           std::vector<pts3D>& particles, double diag_override = NAN) {
@@ -82,6 +85,15 @@ class HODLR3D {
 
   void assemble() { hodlr3d_gb300::check(hodlr3d_assemble(tree.h)); }
 
+  // Factor files (no reference counterpart): save an assembled operator,
+  // or build one from a file without running ACA.
+  void save(const std::string& path) const { hodlr3d_gb300::check(hodlr3d_save(tree.h, path.c_str())); }
+  static std::unique_ptr<HODLR3D> load(const std::string& path) {
+    hodlr3d_t h = nullptr;
+    hodlr3d_gb300::check(hodlr3d_load(path.c_str(), nullptr, &h));
+    return std::unique_ptr<HODLR3D>(new HODLR3D(h));
+  }
+
   // Ab = A b (host vectors); Ab is resized like the reference's (src/HODLR3DTree.cpp:1782).
   template <class Vec>
   void MatVecProduct(Vec& b, Vec& AFMM_Ab) {
@@ -90,6 +102,15 @@ class HODLR3D {
   }
 
   hodlr3d_t handle() const { return tree.h; }
+
+ private:
+  explicit HODLR3D(hodlr3d_t h) {
+    hodlr3d_stats st;
+    hodlr3d_gb300::check(hodlr3d_get_stats(h, &st));
+    N = (int)st.n_points;
+    tree.h = h;
+    A = &tree;
+  }
 };
 
 #endif

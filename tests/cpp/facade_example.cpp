@@ -73,7 +73,27 @@ int main(int argc, char** argv) {
   }
   printf("N=%d matvec_rel_err=%.3e max_rank=%d memory_entries=%.0f gmres_it=%d gmres_res=%.3e fwd_err=%.3e\n",
          N, err, H->A->getMaxRank(), mem, nit, gerr, std::sqrt(fe / fn));
-  const bool ok = err < 1e-8 && gerr <= 1e-10 && std::sqrt(fe / fn) < 1e-8;
+  // factor file round trip: the loaded operator gives the same product
+  const std::string path = std::string(argc > 2 ? argv[2] : "/tmp") + "/facade_example.h3d";
+  H->save(path);
+  std::unique_ptr<HODLR3D> G2 = HODLR3D::load(path);
+  std::vector<double> Hb2;
+  G2->MatVecProduct(b, Hb2);
+  bool same = Hb2.size() == Hb.size();
+  for (int t = 0; same && t < N; ++t) same = Hb2[t] == Hb[t];
+  // the FP64-accurate FP32-pair form against the FP64 form
+  G2->precision = HODLR3D_FP64X;
+  std::vector<double> Hbx;
+  G2->MatVecProduct(b, Hbx);
+  double dx = 0.0, dn = 0.0;
+  for (int t = 0; t < N; ++t) {
+    dx += (Hbx[t] - Hb[t]) * (Hbx[t] - Hb[t]);
+    dn += Hb[t] * Hb[t];
+  }
+  std::remove(path.c_str());
+  printf("loaded_same=%d fp64x_rel_diff=%.3e\n", (int)same, std::sqrt(dx / dn));
+  const bool ok = err < 1e-8 && gerr <= 1e-10 && std::sqrt(fe / fn) < 1e-8 && same &&
+                  std::sqrt(dx / dn) < 1e-12;
   delete H;
   return ok ? 0 : 1;
 }
