@@ -1361,6 +1361,10 @@ int ensure_lo(hodlr3d_t h, const h3d::NearOp& nr, cudaStream_t s) {
 // 28-54 ms for the CUDA-core transpose of 4-32)
 constexpr int kGemvForwardMax = 4;
 constexpr int kGemvTransposeMax = 16;
+// on trees the tensor-core engine does not take, passes of 4 columns beat the
+// CUDA-core kernels' single pass up to 32 columns (64^3: ~6 ms per pass
+// against 54 ms for 32 columns)
+constexpr int kGemvForwardNoTcMax = 32;
 
 int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld, int precision,
                   cudaStream_t s, bool trans) {
@@ -1424,9 +1428,11 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
   // are faster.
   const bool mixed = precision == HODLR3D_MIXED;
   const bool fp64x = precision == HODLR3D_FP64X;
+  // trees the tensor-core engine takes (16-byte aligned leaf rows, bounded tables)
+  const bool tc_tree = h->max_leaf <= 128 && h->leaves_aligned && h->tc_entries <= h3d::tc_max_entries();
+  const int gemv_max = trans ? kGemvTransposeMax : (tc_tree ? kGemvForwardMax : kGemvForwardNoTcMax);
   bool use_gemv = false;
-  if (fp64x || (mixed && (h->engine == 3 || (h->engine == 0 &&
-                                             nrhs <= (trans ? kGemvTransposeMax : kGemvForwardMax))))) {
+  if (fp64x || (mixed && (h->engine == 3 || (h->engine == 0 && nrhs <= gemv_max)))) {
     H3D_TRY(ensure_near_blocks(h, nr, s));
     H3D_TRY(ensure_gemv(h, s));
     use_gemv = h->gemv_ok;
@@ -1495,8 +1501,7 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
     H3D_CUDA(cudaGetLastError());
     return HODLR3D_OK;
   }
-  const bool tc_ok = mixed && !trans && h->max_leaf <= 128 && h->leaves_aligned &&
-                     h->tc_entries <= h3d::tc_max_entries();
+  const bool tc_ok = mixed && !trans && tc_tree;
   if (h->engine == 2 && !tc_ok)
     return set_error(HODLR3D_ERR_UNSUPPORTED,
                      "the tensor-core engine needs A x (not the transpose) in the mixed form, "

@@ -41,8 +41,11 @@ def test_gemv_matches_simt_engine(case, nrhs, transpose):
     ya = H.matvec(X, "mixed", transpose=transpose)
     H.device_status()
     assert colerr(yg, ys) <= 2e-6
-    if transpose or nrhs <= 4:
-        assert torch.equal(ya, yg)  # the automatic choice: A x up to 4 columns, A^T x up to 16
+    tc_tree = bool((np.diff(H.leaf_offsets()) % 4 == 0).all()) and int(np.diff(H.leaf_offsets()).max()) <= 128
+    if transpose or nrhs <= 4 or not tc_tree:
+        # the automatic choice: A^T x up to 16 columns, A x up to 4 (up to 32
+        # on trees the tensor-core engine does not take)
+        assert torch.equal(ya, yg)
     # columns are independent: the product of one column alone is the same
     H.set_engine("gemv")
     y1 = H.matvec(X[:, :1].contiguous(), "mixed", transpose=transpose)
