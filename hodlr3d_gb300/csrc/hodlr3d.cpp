@@ -255,6 +255,7 @@ struct hodlr3d_handle {
   // few-column engine (matvec_gemv.cu): tables over the grouped FP32 layouts
   bool gemv_built = false;
   bool gemv_ok = false;          // tree and layouts fit the few-column kernels
+  bool gemv8_ok = false;         // ... in passes of 8 columns (mixed form)
   DevBuf gv_ubox_off, gv_vbox_off, gv_vbox_rows, gv_vrow0, gv_vrow_t, gv_trow_v, gv_tbase, gv_vpofs,
       gv_upofs, gv_vt_items, gv_vt_upper, gv_ut_items, gv_ut_upper, gv_x, gv_t, gv_tt, gv_p, gv_pt,
       gv_xl, gv_tl, gv_ttl, gv_pd, gv_ptd;
@@ -1288,12 +1289,14 @@ int ensure_gemv(hodlr3d_t h, cudaStream_t s) {
   h->gv_n_vt_upper = (int64_t)vt_upper.size();
   h->gv_n_ut_items = (int64_t)ut_items.size() / 2;
   h->gv_n_ut_upper = (int64_t)ut_upper.size();
-  H3D_CUDA(h->gv_x.ensure(sizeof(float) * 4 * h->N));
-  H3D_CUDA(h->gv_t.ensure(sizeof(float) * 4 * std::max<int64_t>(trows, 1)));
-  H3D_CUDA(cudaMemsetAsync(h->gv_t.p, 0, sizeof(float) * 4 * std::max<int64_t>(trows, 1), s));
-  H3D_CUDA(h->gv_tt.ensure(sizeof(float) * 4 * std::max<int64_t>(vrows, 1)));
-  H3D_CUDA(h->gv_p.ensure(sizeof(float) * 4 * std::max<int64_t>(pv, 1)));
-  H3D_CUDA(h->gv_pt.ensure(sizeof(float) * 4 * std::max<int64_t>(pu, 1)));
+  // 8 columns (mixed); the fp64x form's 4 columns of FP32 pairs fit too
+  H3D_CUDA(h->gv_x.ensure(sizeof(float) * 8 * h->N));
+  H3D_CUDA(h->gv_t.ensure(sizeof(float) * 8 * std::max<int64_t>(trows, 1)));
+  H3D_CUDA(cudaMemsetAsync(h->gv_t.p, 0, sizeof(float) * 8 * std::max<int64_t>(trows, 1), s));
+  H3D_CUDA(h->gv_tt.ensure(sizeof(float) * 8 * std::max<int64_t>(vrows, 1)));
+  H3D_CUDA(h->gv_p.ensure(sizeof(float) * 8 * std::max<int64_t>(pv, 1)));
+  H3D_CUDA(h->gv_pt.ensure(sizeof(float) * 8 * std::max<int64_t>(pu, 1)));
+  h->gemv8_ok = h3d::gemv_smem_bytes(ml4, 8, false) <= 200 * 1024;
   h->gemv_ok = true;
   return HODLR3D_OK;
 }
@@ -1356,11 +1359,11 @@ int ensure_lo(hodlr3d_t h, const h3d::NearOp& nr, cudaStream_t s) {
 }
 
 // largest column counts the few-column engine takes in the automatic choice
-// (passes of 4 columns; measured at 64^3: 7.9 ms for 4 columns against 10.4
-// ms for the tensor cores' 32, and 8.7 ms per 4 transposed columns against
-// 28-54 ms for the CUDA-core transpose of 4-32)
+// (measured at 64^3: 5.7 ms for 4 columns against 10.4 ms for the tensor
+// cores' 32; transposed, 7.0 ms for 4 and 46 ms for 32 columns against 28
+// and 53 ms for the CUDA-core transpose)
 constexpr int kGemvForwardMax = 4;
-constexpr int kGemvTransposeMax = 16;
+constexpr int kGemvTransposeMax = 32;
 // on trees the tensor-core engine does not take, passes of 4 columns beat the
 // CUDA-core kernels' single pass up to 32 columns (64^3: ~6 ms per pass
 // against 54 ms for 32 columns)
@@ -1494,9 +1497,15 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
     gb.n_ut_items = h->gv_n_ut_items;
     gb.ut_upper = h->gv_ut_upper.as<int32_t>();
     gb.n_ut_upper = h->gv_n_ut_upper;
-    for (int c0 = 0; c0 < nrhs; c0 += 4)
+    // passes of 8 columns for the mixed transpose (when the leaves'
+    // near-field inputs fit the shared memory: 8 columns 11.6 ms against two
+    // passes of 4, 14.1 ms, at 64^3), else of 4 (the forward kernels read the
+    // vector with a lane stride of 4 NR floats, which 8 columns turn into
+    // serialised shared-memory and L1 accesses: 16.8 ms against 11.4)
+    const int width = (!fp64x && trans && nrhs > 4 && h->gemv8_ok) ? 8 : 4;
+    for (int c0 = 0; c0 < nrhs; c0 += width)
       h->launches += h3d::launch_matvec_gemv(s, g, gb, x + c0 * ld, ld, y + c0 * ld, ld,
-                                             std::min(4, nrhs - c0), trans, fp64x,
+                                             std::min(width, nrhs - c0), trans, fp64x,
                                              h->profiling ? &h->prof : nullptr);
     H3D_CUDA(cudaGetLastError());
     return HODLR3D_OK;

@@ -135,8 +135,8 @@ int tc_max_entries();
 int launch_near_blocks(cudaStream_t s, int64_t nleaf, const int32_t* leaf_off, const NearOp& near,
                        const int64_t* near_off, const int32_t* near_ld, float* Knear);
 
-// The few-column form (matvec_gemv.cu): 1, 2 or 4 right-hand sides, A X or
-// A^T X, from the box-grouped FP32 factors and near-field blocks.
+// The few-column form (matvec_gemv.cu): 1, 2, 4 or 8 right-hand sides, A X
+// or A^T X, from the box-grouped FP32 factors and near-field blocks.
 constexpr int kGemvCols = 1024;     // columns of a V-stack chunk (forward)
 constexpr int kGemvRowChunk = 2048;  // V-stack rows per forward work item
 constexpr int kGemvRowsT = 256;     // U rows per transposed work item
@@ -170,10 +170,11 @@ struct GemvOp {
   const int64_t* near_off;    // 27 per leaf: start of each block (column near_off - near_base), -1 absent
 };
 
-// Work buffers: xg N x 4 floats; t: T rows x 4 floats (zeroed once: its
-// padding rows are never written); tt: V-stack rows x 4 floats (the
-// transposed T in stack order); p, pt: chunk partials x 4 floats.  The fp64x
-// form adds the lo parts xl, tl (zeroed once), ttl and FP64 partials pd, ptd.
+// Work buffers: xg N x 8 floats; t: T rows x 8 floats (zeroed once: its
+// padding rows are never written); tt: V-stack rows x 8 floats (the
+// transposed T in stack order); p, pt: chunk partials x 8 floats.  The fp64x
+// form (4 columns) adds the lo parts xl, tl (zeroed once), ttl and the chunk
+// partials as FP32 pairs pd, ptd.
 // Work lists: vt_items (source box, chunk, first row, rows); vt_upper: boxes
 // with chunk partials; ut_items (target box, row chunk); ut_upper likewise.
 struct GemvBuffers {
@@ -197,10 +198,11 @@ struct GemvBuffers {
   int64_t n_ut_upper;
 };
 
-// Largest dynamic shared memory a few-column launch asks for.
+// Largest dynamic shared memory a few-column launch of nr (<= 4 or <= 8)
+// columns asks for.
 size_t gemv_smem_bytes(int max_leaf4, int nr, bool fp64x);
-// nrhs in 1..4; fp64x: the FP64-accurate form from the FP32 pairs.  Returns
-// the number of launches.
+// nrhs in 1..8 (fp64x: 1..4, the FP64-accurate form from the FP32 pairs).
+// Returns the number of launches (0: nrhs out of range).
 int launch_matvec_gemv(cudaStream_t s, const GemvOp& op, const GemvBuffers& B, const double* X,
                        int64_t ldx, double* Y, int64_t ldy, int nrhs, bool trans, bool fp64x,
                        MatvecProfiler* prof);

@@ -1,4 +1,4 @@
-// Few-column products (1, 2 or 4 right-hand sides) on the CUDA cores, A X and
+// Few-column products (1, 2, 4 or 8 right-hand sides; fp64x up to 4) on the CUDA cores, A X and
 // A^T X streamed from the box-grouped FP32 factors, in two arithmetics:
 //   mixed  FP32 factors and near field, FP32 FMAs (DF = false);
 //   fp64x  FP64-accurate: every FP64 entry a as the pair hi + lo of FP32
@@ -52,10 +52,10 @@ constexpr int THREADS = 256;
 constexpr int WARPS = THREADS / 32;
 
 // rows per warp in the output kernels (fewer for the fp64x form, whose
-// accumulators and loads are twice as many)
+// accumulators and loads are twice as many, and for 8 columns)
 template <int NR, bool DF>
 __host__ __device__ constexpr int rows_per_warp() {
-  return DF ? 4 : 8;
+  return DF || NR == 8 ? 4 : 8;
 }
 
 __device__ __forceinline__ int level_of(int64_t box, int levels) {
@@ -127,11 +127,18 @@ __device__ __forceinline__ void load_rows4(const float* p, float (&x)[4][NR]) {
     const float4 a = q[0], b = q[1];
     x[0][0] = a.x; x[0][1] = a.y; x[1][0] = a.z; x[1][1] = a.w;
     x[2][0] = b.x; x[2][1] = b.y; x[3][0] = b.z; x[3][1] = b.w;
-  } else {
+  } else if constexpr (NR == 4) {
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
       const float4 a = q[e];
       x[e][0] = a.x; x[e][1] = a.y; x[e][2] = a.z; x[e][3] = a.w;
+    }
+  } else {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const float4 a = q[2 * e], b = q[2 * e + 1];
+      x[e][0] = a.x; x[e][1] = a.y; x[e][2] = a.z; x[e][3] = a.w;
+      x[e][4] = b.x; x[e][5] = b.y; x[e][6] = b.z; x[e][7] = b.w;
     }
   }
 }
@@ -151,52 +158,103 @@ __device__ __forceinline__ float4 ld4(const float* p, int64_t i) {
 // group's first lane (p: the lane's row slot, q = p G + g).  fp64x: rowl, vecl
 // hold the lo parts.  Every lane of the warp takes part (warp-uniform
 // arguments).
-template <int NR, bool DF, int LW, int P, class Out>
+template <int NR, bool DF, int LW, int P, bool COL_OUTER = false, class Out>
 __device__ __forceinline__ void seg_rows(const float* __restrict__ rowp, const float* __restrict__ rowl,
                                          int64_t ld, int nrows, int len4, const float* vec,
                                          const float* vecl, Out&& out) {
   constexpr int G = 32 / LW;
   const int lane = threadIdx.x & 31, g = lane / LW, li = lane % LW;
-  float s[P][NR], c[P][NR];
+  if constexpr (!DF) {
+    // mixed form: one FP32 sum per row and column
+    float acc[P][NR];
 #pragma unroll
-  for (int q = 0; q < P; ++q)
+    for (int q = 0; q < P; ++q)
 #pragma unroll
-    for (int k = 0; k < NR; ++k) s[q][k] = c[q][k] = 0.f;
-  for (int k4 = li; k4 < len4; k4 += LW) {
-    float x[4][NR], xl[4][NR];
-    load_rows4<NR>(vec + (int64_t)k4 * 4 * NR, x);
-    if constexpr (DF) load_rows4<NR>(vecl + (int64_t)k4 * 4 * NR, xl);
-    float4 v[P], vl[P];
+      for (int k = 0; k < NR; ++k) acc[q][k] = 0.f;
+    for (int k4 = li; k4 < len4; k4 += LW) {
+      float x[4][NR];
+      load_rows4<NR>(vec + (int64_t)k4 * 4 * NR, x);
+      float4 v[P];
 #pragma unroll
-    for (int q = 0; q < P; ++q) {
-      const int row = q * G + g;
-      const bool ok = row < nrows;
-      v[q] = ok ? ld4(rowp + row * ld, k4) : make_float4(0.f, 0.f, 0.f, 0.f);
-      if constexpr (DF) vl[q] = ok ? ld4(rowl + row * ld, k4) : make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int q = 0; q < P; ++q) {
+        const int row = q * G + g;
+        v[q] = row < nrows ? ld4(rowp + row * ld, k4) : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      // the same FMA sequence per row and column in either loop order (so the
+      // results are identical); the order only steers the compiler's
+      // scheduling, measured per kernel
+      if constexpr (COL_OUTER) {
+#pragma unroll
+        for (int q = 0; q < P; ++q)
+#pragma unroll
+          for (int k = 0; k < NR; ++k) {
+            acc[q][k] = fmaf(v[q].x, x[0][k], acc[q][k]);
+            acc[q][k] = fmaf(v[q].y, x[1][k], acc[q][k]);
+            acc[q][k] = fmaf(v[q].z, x[2][k], acc[q][k]);
+            acc[q][k] = fmaf(v[q].w, x[3][k], acc[q][k]);
+          }
+      } else {
+#pragma unroll
+        for (int q = 0; q < P; ++q)
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+#pragma unroll
+            for (int k = 0; k < NR; ++k) acc[q][k] = fmaf(comp(v[q], e), x[e][k], acc[q][k]);
+      }
     }
 #pragma unroll
+    for (int o = LW / 2; o > 0; o >>= 1)
+#pragma unroll
+      for (int q = 0; q < P; ++q)
+#pragma unroll
+        for (int k = 0; k < NR; ++k) acc[q][k] += __shfl_xor_sync(0xffffffffu, acc[q][k], o);
+    if (li == 0) {
+#pragma unroll
+      for (int q = 0; q < P; ++q)
+        if (q * G + g < nrows) out(q, q * G + g, acc[q], acc[q]);  // (the second sum is unused)
+    }
+  } else {
+    // fp64x: the pair sums (s, c) of every row and column
+    float s[P][NR], c[P][NR];
+#pragma unroll
     for (int q = 0; q < P; ++q)
 #pragma unroll
-      for (int e = 0; e < 4; ++e)
+      for (int k = 0; k < NR; ++k) s[q][k] = c[q][k] = 0.f;
+    for (int k4 = li; k4 < len4; k4 += LW) {
+      float x[4][NR], xl[4][NR];
+      load_rows4<NR>(vec + (int64_t)k4 * 4 * NR, x);
+      load_rows4<NR>(vecl + (int64_t)k4 * 4 * NR, xl);
+      float4 v[P], vl[P];
 #pragma unroll
-        for (int k = 0; k < NR; ++k)
-          mac<DF>(s[q][k], c[q][k], comp(v[q], e), DF ? comp(vl[q], e) : 0.f, x[e][k],
-                  DF ? xl[e][k] : 0.f);
-  }
-#pragma unroll
-  for (int o = LW / 2; o > 0; o >>= 1)
-#pragma unroll
-    for (int q = 0; q < P; ++q)
-#pragma unroll
-      for (int k = 0; k < NR; ++k) {
-        const float s2 = __shfl_xor_sync(0xffffffffu, s[q][k], o);
-        const float c2 = DF ? __shfl_xor_sync(0xffffffffu, c[q][k], o) : 0.f;
-        merge<DF>(s[q][k], c[q][k], s2, c2);
+      for (int q = 0; q < P; ++q) {
+        const int row = q * G + g;
+        const bool ok = row < nrows;
+        v[q] = ok ? ld4(rowp + row * ld, k4) : make_float4(0.f, 0.f, 0.f, 0.f);
+        vl[q] = ok ? ld4(rowl + row * ld, k4) : make_float4(0.f, 0.f, 0.f, 0.f);
       }
-  if (li == 0) {
 #pragma unroll
-    for (int q = 0; q < P; ++q)
-      if (q * G + g < nrows) out(q, q * G + g, s[q], c[q]);
+      for (int q = 0; q < P; ++q)
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+#pragma unroll
+          for (int k = 0; k < NR; ++k)
+            mac<true>(s[q][k], c[q][k], comp(v[q], e), comp(vl[q], e), x[e][k], xl[e][k]);
+    }
+#pragma unroll
+    for (int o = LW / 2; o > 0; o >>= 1)
+#pragma unroll
+      for (int q = 0; q < P; ++q)
+#pragma unroll
+        for (int k = 0; k < NR; ++k) {
+          const float s2 = __shfl_xor_sync(0xffffffffu, s[q][k], o);
+          const float c2 = __shfl_xor_sync(0xffffffffu, c[q][k], o);
+          merge<true>(s[q][k], c[q][k], s2, c2);
+        }
+    if (li == 0) {
+#pragma unroll
+      for (int q = 0; q < P; ++q)
+        if (q * G + g < nrows) out(q, q * G + g, s[q], c[q]);
+    }
   }
 }
 
@@ -257,13 +315,14 @@ struct Bufs {
 };
 
 // nr rows of a V stack (row stride m4) times xs, P rows per lane and P G per
-// warp pass; row R's sums go to T row map[R], or to partial row R (map null).
+// warp pass; row R's sums go to T row map[R] of dst (fp64x: hi in dst, lo in
+// dstl), or (map null) to partial row R of dst (fp64x: as FP32 pairs).
 template <int NR, bool DF, int LW>
 __device__ __forceinline__ void vt_rows(const float* __restrict__ V, const float* __restrict__ Vl,
                                         int64_t m4, int nr, int len4, const float* xs,
-                                        const float* xsl, const Bufs& B, int64_t pbase,
-                                        const int32_t* __restrict__ map) {
-  constexpr int P = DF ? 4 : 8;
+                                        const float* xsl, float* __restrict__ dst,
+                                        float* __restrict__ dstl, const int32_t* __restrict__ map) {
+  constexpr int P = DF || NR == 8 ? 4 : 8;
   constexpr int G = 32 / LW, RB = P * G;  // rows per warp pass
   const int w = threadIdx.x >> 5, g = (threadIdx.x & 31) / LW;
   for (int b0 = w * RB; b0 < nr; b0 += WARPS * RB) {
@@ -274,28 +333,22 @@ __device__ __forceinline__ void vt_rows(const float* __restrict__ V, const float
       const int R = b0 + p * G + g;
       orow[p] = map && R < nr ? map[R] : R;
     }
-    seg_rows<NR, DF, LW, P>(V + b0 * m4, DF ? Vl + b0 * m4 : nullptr, m4, min(RB, nr - b0), len4, xs,
+    seg_rows<NR, DF, LW, P, true>(V + b0 * m4, DF ? Vl + b0 * m4 : nullptr, m4, min(RB, nr - b0), len4, xs,
                             xsl, [&](int p, int, const float(&sv)[NR], const float(&cv)[NR]) {
-                              if (map) {
+                              if constexpr (!DF) {
+                                float* o = dst + (int64_t)orow[p] * NR;
+#pragma unroll
+                                for (int k = 0; k < NR; ++k) o[k] = sv[k];
+                              } else if (map) {
                                 const int64_t o = (int64_t)orow[p] * NR;
 #pragma unroll
-                                for (int k = 0; k < NR; ++k) {
-                                  if constexpr (DF)
-                                    renorm(sv[k], cv[k], B.t[o + k], B.tl[o + k]);
-                                  else
-                                    B.t[o + k] = sv[k];
-                                }
+                                for (int k = 0; k < NR; ++k) renorm(sv[k], cv[k], dst[o + k], dstl[o + k]);
                               } else {
-                                // partials: FP32 (mixed) or FP32 pairs (fp64x)
-                                float* o = static_cast<float*>(B.p) + (pbase + orow[p]) * NR * (DF ? 2 : 1);
+                                float* o = dst + (int64_t)orow[p] * 2 * NR;  // FP32 pairs
 #pragma unroll
                                 for (int k = 0; k < NR; ++k) {
-                                  if constexpr (DF) {
-                                    o[2 * k] = sv[k];
-                                    o[2 * k + 1] = cv[k];
-                                  } else {
-                                    o[k] = sv[k];
-                                  }
+                                  o[2 * k] = sv[k];
+                                  o[2 * k + 1] = cv[k];
                                 }
                               }
                             });
@@ -332,17 +385,19 @@ __global__ void __launch_bounds__(THREADS) k_vt(GemvOp op, const int4* __restric
   const float* V = op.v32 + vofs;
   const float* Vl = DF ? op.v32lo + vofs : nullptr;
   // rows r0 + R of the item go to T row vr[R] or to partial row R of chunk ci
-  const int64_t pbase = pofs < 0 ? 0 : pofs + (int64_t)ci * rows_a + r0;
   const int32_t* map = pofs < 0 ? vr + r0 : nullptr;
+  float* dst = map ? B.t
+                   : static_cast<float*>(B.p) + (pofs + (int64_t)ci * rows_a + r0) * NR * (DF ? 2 : 1);
+  float* dstl = map ? B.tl : nullptr;
   const int len4 = cl / 4;
   if (len4 > 16)
-    vt_rows<NR, DF, 32>(V, Vl, m4, nr, len4, xs, xsl, B, pbase, map);
+    vt_rows<NR, DF, 32>(V, Vl, m4, nr, len4, xs, xsl, dst, dstl, map);
   else if (len4 > 8)
-    vt_rows<NR, DF, 16>(V, Vl, m4, nr, len4, xs, xsl, B, pbase, map);
+    vt_rows<NR, DF, 16>(V, Vl, m4, nr, len4, xs, xsl, dst, dstl, map);
   else if (len4 > 4)
-    vt_rows<NR, DF, 8>(V, Vl, m4, nr, len4, xs, xsl, B, pbase, map);
+    vt_rows<NR, DF, 8>(V, Vl, m4, nr, len4, xs, xsl, dst, dstl, map);
   else
-    vt_rows<NR, DF, 4>(V, Vl, m4, nr, len4, xs, xsl, B, pbase, map);
+    vt_rows<NR, DF, 4>(V, Vl, m4, nr, len4, xs, xsl, dst, dstl, map);
 }
 
 // partial i (FP32, or in the fp64x form an FP32 pair) as FP64
@@ -606,24 +661,25 @@ __device__ __forceinline__ void stack_cols(const float* __restrict__ V, const fl
                                            double* fw) {
   // rows per lane summed in the arithmetic before an FP64 add: 64 (mixed),
   // 256 (fp64x, compensated)
-  constexpr int G = 32 / LW, U = DF ? 4 : 8, BLK = DF ? 256 : 64;
+  constexpr int G = 32 / LW, U = DF || NR == 8 ? 4 : 8, BLK = DF ? 256 : 64;
   const int lane = threadIdx.x & 31, g = lane / LW, li = lane % LW, w = threadIdx.x >> 5;
   for (int kw = 0; kw < len4; kw += LW) {
     const int k4 = kw + li;
     const bool live = k4 < len4;
-    double a64[4][NR];
-#pragma unroll
-    for (int e = 0; e < 4; ++e)
-#pragma unroll
-      for (int k = 0; k < NR; ++k) a64[e][k] = 0.0;
     const int stride = WARPS * G;
-    for (int v0 = w * G + g; v0 < rows; v0 += BLK * stride) {
+    // every row block: the lane groups (which hold the same columns) are
+    // merged, and the first group adds the block's sums to the warp's FP64
+    // column sums; one summation order for every column count.  The groups
+    // share the warp's row block starts, so every lane runs the same number
+    // of blocks (the shuffles stay convergent).
+    for (int vb = w * G; vb < rows; vb += BLK * stride) {
+      const int v0 = vb + g;
       float s[4][NR], c[4][NR];
 #pragma unroll
       for (int e = 0; e < 4; ++e)
 #pragma unroll
         for (int k = 0; k < NR; ++k) s[e][k] = c[e][k] = 0.f;
-      const int vend = min(rows, v0 + BLK * stride);
+      const int vend = min(rows, vb + BLK * stride);
       int v = v0;
       for (; v + (U - 1) * stride < vend; v += U * stride) {
         float4 f[U], fl[U];
@@ -659,24 +715,23 @@ __device__ __forceinline__ void stack_cols(const float* __restrict__ V, const fl
         }
       }
 #pragma unroll
-      for (int e = 0; e < 4; ++e)
+      for (int o = 16; o >= LW; o >>= 1)
 #pragma unroll
-        for (int k = 0; k < NR; ++k) a64[e][k] += value<DF>(s[e][k], c[e][k]);
-    }
-    // the lane groups of the warp hold the same columns
+        for (int e = 0; e < 4; ++e)
 #pragma unroll
-    for (int o = 16; o >= LW; o >>= 1)
+          for (int k = 0; k < NR; ++k) {
+            const float s2 = __shfl_xor_sync(0xffffffffu, s[e][k], o);
+            const float c2 = DF ? __shfl_xor_sync(0xffffffffu, c[e][k], o) : 0.f;
+            merge<DF>(s[e][k], c[e][k], s2, c2);
+          }
+      if (g == 0 && live) {
 #pragma unroll
-      for (int e = 0; e < 4; ++e)
+        for (int e = 0; e < 4; ++e) {
+          const int i = 4 * k4 + e - shift;  // leaf-local point
+          if (i >= 0 && i < nk)
 #pragma unroll
-        for (int k = 0; k < NR; ++k) a64[e][k] += __shfl_xor_sync(0xffffffffu, a64[e][k], o);
-    if (g == 0 && live) {
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const int i = 4 * k4 + e - shift;  // leaf-local point
-        if (i >= 0 && i < nk)
-#pragma unroll
-          for (int k = 0; k < NR; ++k) fw[i * NR + k] += a64[e][k];
+            for (int k = 0; k < NR; ++k) fw[i * NR + k] += value<DF>(s[e][k], c[e][k]);
+        }
       }
     }
   }
@@ -835,20 +890,22 @@ int dispatch(cudaStream_t s, const GemvOp& op, const GemvBuffers& G, const doubl
              double* Y, int64_t ldy, int nrhs, bool trans, MatvecProfiler* prof) {
   if (nrhs <= 1) return run<1, DF>(s, op, G, X, ldx, Y, ldy, nrhs, trans, prof);
   if (nrhs <= 2) return run<2, DF>(s, op, G, X, ldx, Y, ldy, nrhs, trans, prof);
-  return run<4, DF>(s, op, G, X, ldx, Y, ldy, nrhs, trans, prof);
+  if (DF || nrhs <= 4) return run<4, DF>(s, op, G, X, ldx, Y, ldy, nrhs, trans, prof);
+  return run<8, false>(s, op, G, X, ldx, Y, ldy, nrhs, trans, prof);
 }
 
 }  // namespace
 
 size_t gemv_smem_bytes(int max_leaf4, int nr, bool fp64x) {
-  // the transposed output kernel takes the most; 4 columns the most per form
-  (void)nr;
-  return fp64x ? vy_smem<4, true>(max_leaf4) : vy_smem<4, false>(max_leaf4);
+  // the transposed output kernel takes the most
+  if (fp64x) return vy_smem<4, true>(max_leaf4);
+  return nr > 4 ? vy_smem<8, false>(max_leaf4) : vy_smem<4, false>(max_leaf4);
 }
 
 int launch_matvec_gemv(cudaStream_t s, const GemvOp& op, const GemvBuffers& B, const double* X,
                        int64_t ldx, double* Y, int64_t ldy, int nrhs, bool trans, bool fp64x,
                        MatvecProfiler* prof) {
+  if (nrhs < 1 || nrhs > (fp64x ? 4 : 8)) return 0;
   return fp64x ? dispatch<true>(s, op, B, X, ldx, Y, ldy, nrhs, trans, prof)
                : dispatch<false>(s, op, B, X, ldx, Y, ldy, nrhs, trans, prof);
 }

@@ -43,7 +43,7 @@ def test_gemv_matches_simt_engine(case, nrhs, transpose):
     assert colerr(yg, ys) <= 2e-6
     tc_tree = bool((np.diff(H.leaf_offsets()) % 4 == 0).all()) and int(np.diff(H.leaf_offsets()).max()) <= 128
     if transpose or nrhs <= 4 or not tc_tree:
-        # the automatic choice: A^T x up to 16 columns, A x up to 4 (up to 32
+        # the automatic choice: A^T x up to 32 columns, A x up to 4 (up to 32
         # on trees the tensor-core engine does not take)
         assert torch.equal(ya, yg)
     # columns are independent: the product of one column alone is the same
