@@ -1,5 +1,6 @@
-// Few-column products (1, 2, 4 or 8 right-hand sides; fp64x up to 4) on the CUDA cores, A X and
-// A^T X streamed from the box-grouped FP32 factors, in two arithmetics:
+// Few-column products on the CUDA cores (passes of 1, 2, 4 or, for the mixed
+// transpose, 8 right-hand sides), A X and A^T X streamed from the
+// box-grouped FP32 factors, in two arithmetics:
 //   mixed  FP32 factors and near field, FP32 FMAs (DF = false);
 //   fp64x  FP64-accurate: every FP64 entry a as the pair hi + lo of FP32
 //          values (hi the mixed form's copy, lo = a - hi rounded, relative
@@ -13,8 +14,8 @@
 // src/HODLR3DTree.cpp:1647-1805 (far field V^T q then U T per interaction-list
 // pair, near field over the leaf's neighbours and itself).
 //
-// Every factor entry is used 1..4 times, so the factors and near-field blocks
-// are read once, with 16-byte streaming loads.  Sums: within a row segment of
+// Every factor entry is used once per column of the pass, so the factors and
+// near-field blocks are read once per pass, with 16-byte streaming loads.  Sums: within a row segment of
 // at most 1024 columns (or a chunk of 256 rows, or 64 rows of a stack) in the
 // arithmetic above, FP64 across segments, chunks, levels and near blocks.
 //
@@ -151,10 +152,10 @@ __device__ __forceinline__ float4 ld4(const float* p, int64_t i) {
   return __ldcs(reinterpret_cast<const float4*>(p) + i);
 }
 
-// Dot products of up to P (32 / LW) rows (row q at rowp + q ld, q < nrows) of
+// Dot products of up to P G (G = 32 / LW) rows (row q at rowp + q ld, q < nrows) of
 // len4 16-byte groups with the vector vec ([4 len4][NR], shared or global
 // memory), LW lanes per row, P rows per lane; out(p, q, s, c) is called once
-// per row q with its sums s[NR] + c[NR] (c zero in the mixed form) by its
+// per row q with its sums s[NR] + c[NR] (c: the mixed form passes s again, unused) by its
 // group's first lane (p: the lane's row slot, q = p G + g).  fp64x: rowl, vecl
 // hold the lo parts.  Every lane of the warp takes part (warp-uniform
 // arguments).
