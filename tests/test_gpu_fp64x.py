@@ -68,3 +68,27 @@ def test_fp64x_gmres_matches_fp64(case):
     assert abs(ix["iterations"] - i64["iterations"]) <= 1
     res = (torch.linalg.norm(b - H.matvec(xx, "fp64")) / torch.linalg.norm(b)).item()
     assert res <= 2 * tol, res
+
+
+def test_fp64x_without_fp32_copies_is_the_fp64_form(tmp_path):
+    """keep_fp32 = 0: no FP32 copies to pair with, so fp64x products are the
+    FP64 form's, bit for bit; a factor file saved from such a handle loads
+    into one with the copies (the file holds the FP64 factors)."""
+    from hodlr3d_gb300 import HODLR3D
+    from hodlr3d_gb300.workloads import grid_cell_centres
+    H = HODLR3D(4, 1.0, 10, 16, grid_cell_centres(16), keep_fp32=False)
+    H.assemble()
+    X = torch.tensor(np.random.default_rng(9).standard_normal((H.N, 3)), device="cuda")
+    y64 = H.matvec(X, "fp64")
+    assert torch.equal(H.matvec(X, "fp64x"), y64)
+    with pytest.raises(RuntimeError, match="keep_fp32"):
+        H.matvec(X, "mixed")
+    path = tmp_path / "op.h3d"
+    H.save(path)
+    G = HODLR3D.load(path)
+    try:
+        assert torch.equal(G.matvec(X, "fp64"), y64)
+        assert colerr(G.matvec(X, "fp64x"), y64) <= 1e-12
+    finally:
+        G.close()
+        H.close()
