@@ -233,13 +233,23 @@ __device__ __forceinline__ void seg_rows(const float* __restrict__ rowp, const f
         v[q] = ok ? ld4(rowp + row * ld, k4) : make_float4(0.f, 0.f, 0.f, 0.f);
         vl[q] = ok ? ld4(rowl + row * ld, k4) : make_float4(0.f, 0.f, 0.f, 0.f);
       }
+      if constexpr (COL_OUTER) {
 #pragma unroll
-      for (int q = 0; q < P; ++q)
-#pragma unroll
-        for (int e = 0; e < 4; ++e)
+        for (int q = 0; q < P; ++q)
 #pragma unroll
           for (int k = 0; k < NR; ++k)
-            mac<true>(s[q][k], c[q][k], comp(v[q], e), comp(vl[q], e), x[e][k], xl[e][k]);
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+              mac<true>(s[q][k], c[q][k], comp(v[q], e), comp(vl[q], e), x[e][k], xl[e][k]);
+      } else {
+#pragma unroll
+        for (int q = 0; q < P; ++q)
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+#pragma unroll
+            for (int k = 0; k < NR; ++k)
+              mac<true>(s[q][k], c[q][k], comp(v[q], e), comp(vl[q], e), x[e][k], xl[e][k]);
+      }
     }
 #pragma unroll
     for (int o = LW / 2; o > 0; o >>= 1)
