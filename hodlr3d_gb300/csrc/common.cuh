@@ -23,6 +23,15 @@ __host__ __device__ inline int digit_of(int bx, int by, int bz) {
 // index of the first box of level j in the all-levels box numbering
 __host__ __device__ inline int64_t level_base(int j) { return ((int64_t(1) << (3 * j)) - 1) / 7; }
 
+// One-time settings that apply per device (kernel attributes such as the
+// dynamic shared-memory limit) are tracked per device ordinal.
+constexpr int kMaxDevices = 64;
+inline int current_device() {
+  int d = 0;
+  if (cudaGetDevice(&d) != cudaSuccess || d < 0 || d >= kMaxDevices) d = 0;
+  return d;
+}
+
 // ---------------------------------------------------------------------------
 // Kernel entries.  `kind` is the reference's Qchoice (src/kernel.cpp:65-227);
 // the diagonal is Kii for kind 16 and 0 otherwise (the dispatch of

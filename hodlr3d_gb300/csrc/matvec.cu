@@ -373,11 +373,12 @@ static int run(cudaStream_t s, int64_t N, const int32_t* perm, const FarOp& far,
   const int threads = 64 * C::G;
   const size_t shm_vtx = sizeof(FT) * (64 * 65 + 64 * NR);
   const size_t shm_leaf = sizeof(FT) * (64 * 65 + 128 * NR) + sizeof(NearPt<FT>) * 64;
-  static bool attr_set = false;  // per instantiation
-  if (!attr_set) {
+  static bool attr_set[kMaxDevices] = {};  // per instantiation and device
+  const int dev = current_device();
+  if (!attr_set[dev]) {
     cudaFuncSetAttribute(k_vtx<FT, NR, TRANS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm_vtx);
     cudaFuncSetAttribute(k_leaf<FT, NR, TRANS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm_leaf);
-    attr_set = true;
+    attr_set[dev] = true;
   }
   if (far.levels >= 2) {
     if (B.n_items > 0) {

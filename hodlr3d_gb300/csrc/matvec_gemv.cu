@@ -837,12 +837,14 @@ size_t vy_smem(int max_leaf4) {
 template <int NR, bool DF>
 int run(cudaStream_t s, const GemvOp& op, const GemvBuffers& G, const double* X, int64_t ldx,
         double* Y, int64_t ldy, int nrhs, bool trans, MatvecProfiler* prof) {
-  static int attr_done = 0;  // largest shared-memory request set so far, per instantiation
+  // largest shared-memory request set so far, per instantiation and device
+  static int attr_done[kMaxDevices] = {};
+  const int dev = current_device();
   const size_t shu = uy_smem<NR, DF>(op.max_leaf4), shv = vy_smem<NR, DF>(op.max_leaf4);
-  if ((int)shv > attr_done) {
+  if ((int)shv > attr_done[dev]) {
     cudaFuncSetAttribute(k_uy<NR, DF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shu);
     cudaFuncSetAttribute(k_vy<NR, DF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shv);
-    attr_done = (int)shv;
+    attr_done[dev] = (int)shv;
   }
   Bufs B{};
   B.xg = G.xg;

@@ -959,13 +959,14 @@ int launch_near_blocks(cudaStream_t s, int64_t nleaf, const int32_t* leaf_off, c
 int launch_matvec_tc(cudaStream_t s, int64_t N, const int32_t* perm, const FarOp& far,
                      const NearOp& near, const TcBuffers& B, const double* X, int64_t ldx,
                      double* Y, int64_t ldy, int nrhs, MatvecProfiler* prof) {
-  static bool attr = false;
-  if (!attr) {
+  static bool attr[kMaxDevices] = {};  // kernel attributes are per device
+  const int dev = current_device();
+  if (!attr[dev]) {
     cudaFuncSetAttribute(k_ta_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     cudaFuncSetAttribute(k_ta_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     cudaFuncSetAttribute(k_ut_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     cudaFuncSetAttribute(k_leaf_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-    attr = true;
+    attr[dev] = true;
   }
   const CUtensorMap* umaps = static_cast<const CUtensorMap*>(B.umaps);
   const CUtensorMap* vmaps = static_cast<const CUtensorMap*>(B.vmaps);
