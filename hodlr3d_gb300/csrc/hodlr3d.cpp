@@ -1435,7 +1435,14 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
   const bool tc_tree = h->max_leaf <= 128 && h->leaves_aligned && h->tc_entries <= h3d::tc_max_entries();
   const int gemv_max = trans ? kGemvTransposeMax : (tc_tree ? kGemvForwardMax : kGemvForwardNoTcMax);
   bool use_gemv = false;
-  if (fp64x || (mixed && (h->engine == 3 || (h->engine == 0 && nrhs <= gemv_max)))) {
+  // fp64x: the few-column kernels (automatic or forced); forcing the CUDA-core
+  // kernels gives the FP64 form; the tensor cores have no FP64-accurate form
+  if (fp64x && h->engine == 2)
+    return set_error(HODLR3D_ERR_UNSUPPORTED,
+                     "the tensor-core engine has no FP64-accurate form (use HODLR3D_MIXED or "
+                     "another engine)");
+  if ((fp64x && h->engine != 1) ||
+      (mixed && (h->engine == 3 || (h->engine == 0 && nrhs <= gemv_max)))) {
     H3D_TRY(ensure_near_blocks(h, nr, s));
     H3D_TRY(ensure_gemv(h, s));
     use_gemv = h->gemv_ok;

@@ -92,3 +92,17 @@ def test_fp64x_without_fp32_copies_is_the_fp64_form(tmp_path):
     finally:
         G.close()
         H.close()
+
+
+def test_fp64x_under_forced_engines(case):
+    """Forcing the CUDA-core engine gives the FP64 form; the tensor cores have
+    no FP64-accurate form and refuse it."""
+    g, H = case
+    X = torch.tensor(np.random.default_rng(2).standard_normal((H.N, 2)), device="cuda")
+    H.set_engine("simt")
+    ys = H.matvec(X, "fp64x")
+    H.set_engine("tc")
+    with pytest.raises(RuntimeError, match="FP64-accurate"):
+        H.matvec(X, "fp64x")
+    H.set_engine("auto")
+    assert torch.equal(ys, H.matvec(X, "fp64"))
