@@ -201,9 +201,10 @@ int64_t hodlr3d_launch_count(hodlr3d_t h);
 /* Matvec engine: 0 = automatic (mixed form: the few-column FP32 kernels for
  * A x with 1..4 right-hand sides (1..32 on trees the tensor cores do not
  * take) and A^T x with 1..32, the tensor cores, tcgen05 3xTF32, for A x with
- * more; otherwise CUDA-core kernels), 1 = CUDA-core kernels only, 2 = tensor cores only, 3 = few-column
- * kernels only (HODLR3D_ERR_UNSUPPORTED where the chosen engine does not
- * apply). */
+ * more; HODLR3D_FP64X: the few-column kernels; otherwise CUDA-core kernels),
+ * 1 = CUDA-core kernels only (HODLR3D_FP64X becomes HODLR3D_FP64), 2 = tensor
+ * cores only, 3 = few-column kernels only (HODLR3D_ERR_UNSUPPORTED where the
+ * chosen engine does not apply). */
 int hodlr3d_set_engine(hodlr3d_t h, int engine);
 /* Synchronises the device and reports HODLR3D_ERR_CUDA if a bounded
  * tensor-core wait gave up in an earlier call on this handle. */
