@@ -193,6 +193,7 @@ struct hodlr3d_handle {
   // FP32 value, rounded), same layouts; built on first use
   DevBuf u32lo_pool, v32lo_pool, knearlo;
   bool lo_built = false;
+  bool lo_unavailable = false;  // the lo parts did not fit: fp64x is the FP64 form
   std::vector<int32_t> h_pair_m, h_pair_n;  // per pair: source and target box sizes
   std::vector<int64_t> h_ubox_off, h_tbox_off;
   std::vector<int32_t> h_rbox, h_ustride, h_coff;
@@ -483,6 +484,7 @@ int group_fp32(hodlr3d_t h) {
   h->h_pair_m = msize;
   h->h_pair_n = nsize;
   h->lo_built = false;
+  h->lo_unavailable = false;
   h->v32_pool = new DevBuf();
   h->pools.push_back(h->v32_pool);
   H3D_CUDA(h->v32_pool->ensure(sizeof(float) * std::max<int64_t>(vcur, 4)));
@@ -1446,7 +1448,21 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
     H3D_TRY(ensure_near_blocks(h, nr, s));
     H3D_TRY(ensure_gemv(h, s));
     use_gemv = h->gemv_ok;
-    if (use_gemv && fp64x) H3D_TRY(ensure_lo(h, nr, s));
+    if (use_gemv && fp64x && !h->lo_unavailable) {
+      const int st = ensure_lo(h, nr, s);
+      if (st == HODLR3D_ERR_OUT_OF_MEMORY) {
+        // the lo parts (as large as the FP32 copies) do not fit: the FP64 form
+        // serves instead, now and for the rest of this assembly
+        cudaGetLastError();
+        h->u32lo_pool.release();
+        h->v32lo_pool.release();
+        h->knearlo.release();
+        h->lo_unavailable = true;
+      } else if (st != HODLR3D_OK) {
+        return st;
+      }
+    }
+    if (fp64x && h->lo_unavailable) use_gemv = false;
   }
   if (fp64x && !use_gemv) {
     precision = HODLR3D_FP64;

@@ -41,8 +41,10 @@ enum hodlr3d_precision {
   HODLR3D_MIXED = 1, /* FP32 factors and near field, FP64 accumulation across tiles */
   HODLR3D_FP64X = 2  /* FP64-accurate products in FP32-pair arithmetic: every FP64 entry
                         as hi + lo FP32 values (relative error 2^-46), exact FP32 products
-                        and compensated sums, FP64 across tiles; needs keep_fp32 (without
-                        it, or on a tree the few-column kernels do not take: HODLR3D_FP64).
+                        and compensated sums, FP64 across tiles; needs keep_fp32 and device
+                        memory for the lo parts (as much as the FP32 copies), built on first
+                        use; without them, or on a tree the few-column kernels do not take:
+                        HODLR3D_FP64.
                         Agrees with the FP64 form to ~1e-13 relative. */
 };
 
