@@ -72,3 +72,36 @@ def test_no_device_or_tree_error_is_reported():
     code = L.hodlr3d_create(pts.ctypes.data, 64, 4, 1.0, 10, 16, None, ctypes.byref(h))
     assert code in (_lib.ERR_NO_DEVICE, _lib.ERR_INVALID_ARG)
     assert not h.value
+
+
+def _factor_header(version=1, n=64, npairs=0, npools=0):
+    import struct
+    # FileHeader (hodlr3d.cpp): version, header bytes, n, nP1D, tol_pow, L, kernel, levels,
+    # diag, npairs, npools, reserved, lists hash
+    return b"H3DFACT1" + struct.pack("<IIqiidiidqiiQ", version, 72, n, 4, 10, 1.0, 16, 1, 0.5,
+                                     npairs, npools, 0, 0x1234)
+
+
+def test_factor_header_reader(tmp_path):
+    p = tmp_path / "h.h3d"
+    p.write_bytes(_factor_header(n=4096, npairs=2808) + b"\0" * 64)
+    h = _lib.read_factor_header(p)
+    assert (h["version"], h["header_bytes"], h["n"], h["nP1D"], h["tol_pow"], h["kernel"]) == (1, 72, 4096, 4, 10, 16)
+    assert h["L"] == 1.0 and h["diag"] == 0.5 and h["npairs"] == 2808 and h["lists_hash"] == 0x1234
+
+
+def test_factor_file_validation_before_any_device_work(tmp_path):
+    """Wrong magic, wrong version and truncated points are refused with
+    HODLR3D_ERR_IO while reading, before the tree is rebuilt on a device."""
+    L = _lib.lib()
+    h = ctypes.c_void_p()
+    cases = {
+        "magic.h3d": b"H3DFACT9" + _factor_header()[8:],
+        "version.h3d": _factor_header(version=2),
+        "truncated.h3d": _factor_header(n=64) + b"\0" * 100,  # 64 points need 1536 bytes
+    }
+    for name, data in cases.items():
+        p = tmp_path / name
+        p.write_bytes(data)
+        assert L.hodlr3d_load(str(p).encode(), None, ctypes.byref(h)) == _lib.ERR_IO, name
+        assert not h.value
