@@ -244,6 +244,11 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
   m.offB = A_BYTES + tc::kmajor_off(m.cb, 4 * m.qb, KC);
   const int R = tid & 127;
   const uint32_t lane_base = ((uint32_t)((tid >> 5) & 3) * 32u) << 16;
+  // a warp whose 32 rows all lie at or past the tile's live rows (a 64-point
+  // leaf in a 128-row tile) skips splitting A: the tensor core still
+  // multiplies its lanes of tensor memory (stale values) into accumulator
+  // rows that no epilogue reads.  Warp-uniform, as tcgen05.st requires.
+  const bool warp_live = 32 * ((tid >> 5) & 3) < src.live_rows();
 
   float sum[NCOL], comp[NCOL], cross[NCOL];
 #pragma unroll
@@ -296,24 +301,26 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
     unsigned char* slot = smem + s * SLOT_BYTES;
     {
       // the row this thread owns, from the 128-byte swizzled A box of its K half
-      const unsigned char* sa = slot + (kq >> 1) * A_HALF + (uint32_t)R * 128u;
-      float hi[16], lo[16];
+      if (warp_live) {
+        const unsigned char* sa = slot + (kq >> 1) * A_HALF + (uint32_t)R * 128u;
+        float hi[16], lo[16];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int qq = 4 * (kq & 1) + j;
-        const float4 x = *reinterpret_cast<const float4*>(sa + ((uint32_t)(qq ^ (R & 7)) << 4));
-        hi[4 * j] = tf32_rz(x.x);
-        hi[4 * j + 1] = tf32_rz(x.y);
-        hi[4 * j + 2] = tf32_rz(x.z);
-        hi[4 * j + 3] = tf32_rz(x.w);
-        lo[4 * j] = x.x - hi[4 * j];
-        lo[4 * j + 1] = x.y - hi[4 * j + 1];
-        lo[4 * j + 2] = x.z - hi[4 * j + 2];
-        lo[4 * j + 3] = x.w - hi[4 * j + 3];
+        for (int j = 0; j < 4; ++j) {
+          const int qq = 4 * (kq & 1) + j;
+          const float4 x = *reinterpret_cast<const float4*>(sa + ((uint32_t)(qq ^ (R & 7)) << 4));
+          hi[4 * j] = tf32_rz(x.x);
+          hi[4 * j + 1] = tf32_rz(x.y);
+          hi[4 * j + 2] = tf32_rz(x.z);
+          hi[4 * j + 3] = tf32_rz(x.w);
+          lo[4 * j] = x.x - hi[4 * j];
+          lo[4 * j + 1] = x.y - hi[4 * j + 1];
+          lo[4 * j + 2] = x.z - hi[4 * j + 2];
+          lo[4 * j + 3] = x.w - hi[4 * j + 3];
+        }
+        const uint32_t ta = tmem + TM_A + TM_ASTRIDE * (uint32_t)(c % kABuf) + 16u * kq + lane_base;
+        tc::tmem_st16(ta, hi);
+        tc::tmem_st16(ta + (uint32_t)KC, lo);
       }
-      const uint32_t ta = tmem + TM_A + TM_ASTRIDE * (uint32_t)(c % kABuf) + 16u * kq + lane_base;
-      tc::tmem_st16(ta, hi);
-      tc::tmem_st16(ta + (uint32_t)KC, lo);
       if (copies_b && src.fresh_b(c)) {
         // the B segment this thread copied: low part next to it
         unsigned char* sb = slot + m.offB;
@@ -459,6 +466,8 @@ struct SrcTa {
   // holds K range s % cpt, so B is copied and split in the first kSlots chunks
   // only and read from the slot afterwards
   __device__ bool fresh_b(int c) const { return c < kSlots || kSlots % cpt != 0; }
+  // tiles of V-stack rows: every row of a tile can be live
+  __device__ int live_rows() const { return 128; }
   __device__ int level_of(int tg) const {
     int j = 0;
     while (j + 1 < nlev && lv[1][j + 1] <= tg) ++j;
@@ -663,6 +672,8 @@ struct SrcItems {
   const float* wb = nullptr;
 
   __device__ bool fresh_b(int) const { return true; }
+  // rows of the block's tile that the epilogue writes (all items share them)
+  __device__ int live_rows() const { return nrows; }
   // next item with K after item i
   __device__ int next_item(int i) const {
     ++i;
