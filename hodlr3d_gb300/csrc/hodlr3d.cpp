@@ -1360,6 +1360,107 @@ int ensure_lo(hodlr3d_t h, const h3d::NearOp& nr, cudaStream_t s) {
   return HODLR3D_OK;
 }
 
+// The few-column engine (matvec_gemv.cu) over this handle's tables, in passes
+// of 4 (or 8) columns; its tables and, for fp64x, the lo parts exist.
+int run_gemv(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld, cudaStream_t s,
+             bool trans, bool fp64x) {
+  h3d::GemvOp g{};
+  g.levels = h->levels;
+  g.max_leaf4 = (h->max_leaf + 3) & ~3;
+  g.nleaf = h->nleaf;
+  g.N = h->N;
+  g.leaf_off = h->leaf_off.as<int32_t>();
+  g.perm = h->perm.as<int32_t>();
+  g.nbr_leaf = h->nbr_leaf.as<int32_t>();
+  g.u32 = h->u32_pool->as<float>();
+  g.v32 = h->v32_pool->as<float>();
+  g.ubox_off = h->gv_ubox_off.as<int64_t>();
+  g.rbox = h->tc_rbox.as<int32_t>();
+  g.vbox_off = h->gv_vbox_off.as<int64_t>();
+  g.vbox_rows = h->gv_vbox_rows.as<int32_t>();
+  g.vrow0 = h->gv_vrow0.as<int64_t>();
+  g.vrow_t = h->gv_vrow_t.as<int32_t>();
+  g.trow_v = h->gv_trow_v.as<int32_t>();
+  g.tbase = h->gv_tbase.as<int64_t>();
+  g.vpofs = h->gv_vpofs.as<int64_t>();
+  g.upofs = h->gv_upofs.as<int64_t>();
+  g.knear = h->knear.as<float>();
+  g.u32lo = fp64x ? h->u32lo_pool.as<float>() : nullptr;
+  g.v32lo = fp64x ? h->v32lo_pool.as<float>() : nullptr;
+  g.knearlo = fp64x ? h->knearlo.as<float>() : nullptr;
+  g.near_base = h->near_base.as<int64_t>();
+  g.near_ld = h->near_ld.as<int32_t>();
+  g.near_off = h->near_off.as<int64_t>();
+  h3d::GemvBuffers gb{};
+  gb.xg = h->gv_x.as<float>();
+  gb.t = h->gv_t.as<float>();
+  gb.tt = h->gv_tt.as<float>();
+  gb.p = h->gv_p.as<float>();
+  gb.pt = h->gv_pt.as<float>();
+  gb.xl = h->gv_xl.as<float>();
+  gb.tl = h->gv_tl.as<float>();
+  gb.ttl = h->gv_ttl.as<float>();
+  gb.pd = h->gv_pd.as<double>();
+  gb.ptd = h->gv_ptd.as<double>();
+  gb.vt_items = h->gv_vt_items.as<int4>();
+  gb.n_vt_items = h->gv_n_vt_items;
+  gb.vt_upper = h->gv_vt_upper.as<int32_t>();
+  gb.n_vt_upper = h->gv_n_vt_upper;
+  gb.ut_items = h->gv_ut_items.as<int2>();
+  gb.n_ut_items = h->gv_n_ut_items;
+  gb.ut_upper = h->gv_ut_upper.as<int32_t>();
+  gb.n_ut_upper = h->gv_n_ut_upper;
+  // passes of 8 columns for the mixed transpose (when the leaves'
+  // near-field inputs fit the shared memory: 8 columns 11.6 ms against two
+  // passes of 4, 14.1 ms, at 64^3), else of 4 (the forward kernels read the
+  // vector with a lane stride of 4 NR floats, which 8 columns turn into
+  // serialised shared-memory and L1 accesses: 16.8 ms against 11.4)
+  const int width = (!fp64x && trans && nrhs > 4 && h->gemv8_ok) ? 8 : 4;
+  for (int c0 = 0; c0 < nrhs; c0 += width)
+    h->launches += h3d::launch_matvec_gemv(s, g, gb, x + c0 * ld, ld, y + c0 * ld, ld,
+                                           std::min(width, nrhs - c0), trans, fp64x,
+                                           h->profiling ? &h->prof : nullptr);
+  H3D_CUDA(cudaGetLastError());
+  return HODLR3D_OK;
+}
+
+// The tensor-core engine (matvec_tc.cu) in batches of 32 columns; builds its
+// near-field blocks and tensor maps on first use.
+int run_tc(hodlr3d_t h, const h3d::FarOp& far, const h3d::NearOp& nr, const double* x, double* y,
+           int nrhs, int64_t ld, cudaStream_t s) {
+  H3D_TRY(ensure_matvec_buffers(h, 32));  // slice partials and level sums of 32 columns
+  if (!h->dev_err.p) {
+    H3D_CUDA(h->dev_err.ensure(sizeof(int)));
+    H3D_CUDA(cudaMemsetAsync(h->dev_err.p, 0, sizeof(int), s));
+  }
+  H3D_TRY(ensure_near_blocks(h, nr, s));
+  if (!h->maps_built) H3D_TRY(build_tensor_maps(h, h->h_near_off));
+  // [X | T], the B operands in the split-exact form
+  H3D_CUDA(h->tct.ensure(sizeof(float) * 32 * (h->N + std::max<int64_t>(h->sum_rank4, 1))));
+  h3d::TcBuffers T{};
+  T.xt = h->tct.as<float>();
+  T.t = T.xt + 32 * h->N;
+  T.p = reinterpret_cast<float*>(h->pbuf.p);
+  T.ynl = h->ynl.as<double>();
+  T.err = h->dev_err.as<int>();
+  T.upper_pairs = h->upper.as<int32_t>();
+  T.n_upper = h->n_upper;
+  T.max_slice = h->max_slice;
+  T.knear = h->knear.as<float>();
+  T.near_off = h->near_off.as<int64_t>();
+  const CUtensorMap* tm = h->tmaps.as<CUtensorMap>();
+  const int64_t nbox = (int64_t)h->h_vbox_rows.size();
+  T.umaps = tm;
+  T.vmaps = tm + nbox;
+  T.nmaps = tm + 2 * nbox;
+  for (int c0 = 0; c0 < nrhs; c0 += 32)
+    h->launches += h3d::launch_matvec_tc(s, h->N, h->perm.as<int32_t>(), far, nr, T, x + c0 * ld,
+                                         ld, y + c0 * ld, ld, std::min(32, nrhs - c0),
+                                         h->profiling ? &h->prof : nullptr);
+  H3D_CUDA(cudaGetLastError());
+  return HODLR3D_OK;
+}
+
 // largest column counts the few-column engine takes in the automatic choice
 // (measured at 64^3: 5.7 ms for 4 columns against 10.4 ms for the tensor
 // cores' 32; transposed, 7.0 ms for 4 and 46 ms for 32 columns against 28
@@ -1473,106 +1574,17 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
     return set_error(HODLR3D_ERR_UNSUPPORTED,
                      "the few-column engine needs the mixed form, leaves whose near-field inputs "
                      "fit its shared memory and fewer than 2^31 rows of T");
-  if (use_gemv) {
-    h3d::GemvOp g{};
-    g.levels = h->levels;
-    g.max_leaf4 = (h->max_leaf + 3) & ~3;
-    g.nleaf = h->nleaf;
-    g.N = h->N;
-    g.leaf_off = h->leaf_off.as<int32_t>();
-    g.perm = h->perm.as<int32_t>();
-    g.nbr_leaf = h->nbr_leaf.as<int32_t>();
-    g.u32 = h->u32_pool->as<float>();
-    g.v32 = h->v32_pool->as<float>();
-    g.ubox_off = h->gv_ubox_off.as<int64_t>();
-    g.rbox = h->tc_rbox.as<int32_t>();
-    g.vbox_off = h->gv_vbox_off.as<int64_t>();
-    g.vbox_rows = h->gv_vbox_rows.as<int32_t>();
-    g.vrow0 = h->gv_vrow0.as<int64_t>();
-    g.vrow_t = h->gv_vrow_t.as<int32_t>();
-    g.trow_v = h->gv_trow_v.as<int32_t>();
-    g.tbase = h->gv_tbase.as<int64_t>();
-    g.vpofs = h->gv_vpofs.as<int64_t>();
-    g.upofs = h->gv_upofs.as<int64_t>();
-    g.knear = h->knear.as<float>();
-    g.u32lo = fp64x ? h->u32lo_pool.as<float>() : nullptr;
-    g.v32lo = fp64x ? h->v32lo_pool.as<float>() : nullptr;
-    g.knearlo = fp64x ? h->knearlo.as<float>() : nullptr;
-    g.near_base = h->near_base.as<int64_t>();
-    g.near_ld = h->near_ld.as<int32_t>();
-    g.near_off = h->near_off.as<int64_t>();
-    h3d::GemvBuffers gb{};
-    gb.xg = h->gv_x.as<float>();
-    gb.t = h->gv_t.as<float>();
-    gb.tt = h->gv_tt.as<float>();
-    gb.p = h->gv_p.as<float>();
-    gb.pt = h->gv_pt.as<float>();
-    gb.xl = h->gv_xl.as<float>();
-    gb.tl = h->gv_tl.as<float>();
-    gb.ttl = h->gv_ttl.as<float>();
-    gb.pd = h->gv_pd.as<double>();
-    gb.ptd = h->gv_ptd.as<double>();
-    gb.vt_items = h->gv_vt_items.as<int4>();
-    gb.n_vt_items = h->gv_n_vt_items;
-    gb.vt_upper = h->gv_vt_upper.as<int32_t>();
-    gb.n_vt_upper = h->gv_n_vt_upper;
-    gb.ut_items = h->gv_ut_items.as<int2>();
-    gb.n_ut_items = h->gv_n_ut_items;
-    gb.ut_upper = h->gv_ut_upper.as<int32_t>();
-    gb.n_ut_upper = h->gv_n_ut_upper;
-    // passes of 8 columns for the mixed transpose (when the leaves'
-    // near-field inputs fit the shared memory: 8 columns 11.6 ms against two
-    // passes of 4, 14.1 ms, at 64^3), else of 4 (the forward kernels read the
-    // vector with a lane stride of 4 NR floats, which 8 columns turn into
-    // serialised shared-memory and L1 accesses: 16.8 ms against 11.4)
-    const int width = (!fp64x && trans && nrhs > 4 && h->gemv8_ok) ? 8 : 4;
-    for (int c0 = 0; c0 < nrhs; c0 += width)
-      h->launches += h3d::launch_matvec_gemv(s, g, gb, x + c0 * ld, ld, y + c0 * ld, ld,
-                                             std::min(width, nrhs - c0), trans, fp64x,
-                                             h->profiling ? &h->prof : nullptr);
-    H3D_CUDA(cudaGetLastError());
-    return HODLR3D_OK;
-  }
+  if (use_gemv) return run_gemv(h, x, y, nrhs, ld, s, trans, fp64x);
   const bool tc_ok = mixed && !trans && tc_tree;
   if (h->engine == 2 && !tc_ok)
     return set_error(HODLR3D_ERR_UNSUPPORTED,
                      "the tensor-core engine needs A x (not the transpose) in the mixed form, "
                      "leaves of at most 128 points, each a multiple of 4, and at most %d pairs per "
                      "block (this tree: %d)", h3d::tc_max_entries(), h->tc_entries);
-  if (tc_ok && h->engine != 1) {
-    H3D_TRY(ensure_matvec_buffers(h, 32));  // slice partials and level sums of 32 columns
-    if (!h->dev_err.p) {
-      H3D_CUDA(h->dev_err.ensure(sizeof(int)));
-      H3D_CUDA(cudaMemsetAsync(h->dev_err.p, 0, sizeof(int), s));
-    }
-    H3D_TRY(ensure_near_blocks(h, nr, s));
-    if (!h->maps_built) H3D_TRY(build_tensor_maps(h, h->h_near_off));
-    // [X | T], the B operands in the split-exact form
-    H3D_CUDA(h->tct.ensure(sizeof(float) * 32 * (h->N + std::max<int64_t>(h->sum_rank4, 1))));
-    h3d::TcBuffers T{};
-    T.xt = h->tct.as<float>();
-    T.t = T.xt + 32 * h->N;
-    T.p = reinterpret_cast<float*>(h->pbuf.p);
-    T.ynl = h->ynl.as<double>();
-    T.err = h->dev_err.as<int>();
-    T.upper_pairs = h->upper.as<int32_t>();
-    T.n_upper = h->n_upper;
-    T.max_slice = h->max_slice;
-    T.knear = h->knear.as<float>();
-    T.near_off = h->near_off.as<int64_t>();
-    const CUtensorMap* tm = h->tmaps.as<CUtensorMap>();
-    const int64_t nbox = (int64_t)h->h_vbox_rows.size();
-    T.umaps = tm;
-    T.vmaps = tm + nbox;
-    T.nmaps = tm + 2 * nbox;
-    for (int c0 = 0; c0 < nrhs; c0 += 32)
-      h->launches += h3d::launch_matvec_tc(s, h->N, h->perm.as<int32_t>(), far, nr, T, x + c0 * ld,
-                                           ld, y + c0 * ld, ld, std::min(32, nrhs - c0),
-                                           h->profiling ? &h->prof : nullptr);
-  } else {
-    h->launches += h3d::launch_matvec(s, h->N, h->perm.as<int32_t>(), far, nr, B, x, ld, y, ld, nrhs,
-                                      precision, trans ? 1 : 0, h->profiling ? &h->prof : nullptr);
-  }
+  if (tc_ok && h->engine != 1) return run_tc(h, far, nr, x, y, nrhs, ld, s);
+  // the CUDA-core engine (matvec.cu)
+  h->launches += h3d::launch_matvec(s, h->N, h->perm.as<int32_t>(), far, nr, B, x, ld, y, ld, nrhs,
+                                    precision, trans ? 1 : 0, h->profiling ? &h->prof : nullptr);
   H3D_CUDA(cudaGetLastError());
   return HODLR3D_OK;
 }
