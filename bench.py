@@ -9,8 +9,8 @@ HBM.  `e2e` is the same product through the C-ABI host entry point
 (hodlr3d_matvec_host: host buffers, copies inside the timed region).  The
 FP64 form at one right-hand side and the GMRES solves are reported beside it.
 `--impl reference` times the reference algorithm on the host cores (the CPU
-oracle port of it, since the reference itself cannot be built on the GPU
-host) on a bounded sample of the same workload.  For N > 1 (torchrun) every
+oracle port of it: the reference's sources do not travel with this package)
+on a bounded sample of the same workload.  For N > 1 (torchrun) every
 rank runs an independent replica; value = all ranks' right-hand sides / max time.
 """
 from __future__ import annotations
@@ -20,6 +20,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -50,7 +51,8 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        self.path = os.path.join(os.environ.get("HODLR3D_CLOCKS_DIR", tempfile.gettempdir()),
+                                 f"hodlr3d_clocks_{os.getpid()}.csv")
 
     def start(self):
         try:

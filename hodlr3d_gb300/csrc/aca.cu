@@ -11,7 +11,7 @@
 // Bit-exactness: kernel entries and residual rows/columns are evaluated with
 // the reference's operation order and no fused multiply-adds; norms and dot
 // products use the canonical reduction order; pivots are first maxima.  The
-// CPU checker reproduces the same ranks and pivots.
+// CPU oracle reproduces the same ranks and pivots.
 #include "aca.h"
 #include "common.cuh"
 

@@ -133,7 +133,7 @@ __device__ __forceinline__ float tf32_split_value(double x) {
 // ---------------------------------------------------------------------------
 // The canonical reduction: each lane holds the sequential sum of its strided
 // elements; the butterfly p[L] + p[L ^ o], o = 16..1, leaves the same value in
-// every lane.  Its CPU restatement is the checker's canonical_sum.
+// every lane.  Its CPU restatement is the oracle's canonical_sum.
 __device__ __forceinline__ double warp_butterfly_sum(double v) {
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1) v = __dadd_rn(v, __shfl_xor_sync(0xffffffffu, v, o));

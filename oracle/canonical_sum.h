@@ -1,6 +1,6 @@
 /* TEST INFRASTRUCTURE.  The canonical FP64 reduction order of the CUDA
  * kernels (hodlr3d_gb300/csrc/common.cuh, warp_canonical_sum), restated for
- * the CPU checker and the Eigen API shim so that norms and dot products --
+ * the CPU oracle and the Eigen API shim so that norms and dot products --
  * and with them the stopping test of the ACA -- agree bit for bit.
  *
  * canonical_sum(f, n): the index range is cut into chunks of 8192; in a chunk,

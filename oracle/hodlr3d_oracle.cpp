@@ -2,8 +2,8 @@
 //
 // This file is the oracle: a plain C++/OpenMP restatement of the reference
 // path (tree, interaction lists, ACA, matvec, GMRES) that the parity tests,
-// the smoke check and the CPU-baseline leg of the benchmark use as the checker
-// of the CUDA product.  The product never links it.  Every function cites the
+// the smoke check and the CPU-baseline leg of the benchmark compare the CUDA
+// product with.  The product never links it.  Every function cites the
 // reference file:line it follows.  It is pinned against the reference's own
 // sources compiled in this repository's test environment (oracle/Makefile.ref,
 // tests/golden/make_golden.py): identical leaf order, neighbour slots,

@@ -2,8 +2,8 @@
  * lists, partially pivoted ACA, matvec, GMRES, dense direct sum).
  *
  * TEST INFRASTRUCTURE ONLY.  This is the oracle: the parity tests, the smoke
- * check and the CPU-baseline leg of the benchmark call it as the checker of
- * the CUDA path.  The product (hodlr3d_gb300) never links or calls it.
+ * check and the CPU-baseline leg of the benchmark check the CUDA path
+ * against it.  The product (hodlr3d_gb300) never links or calls it.
  *
  * It is pinned against the reference's own sources compiled here (see
  * oracle/Makefile.ref and tests/golden/make_golden.py).

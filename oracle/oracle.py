@@ -1,7 +1,7 @@
 """ctypes wrapper of the CPU oracle (oracle/hodlr3d_oracle.cpp).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()``
-and by the CPU-baseline leg of ``bench.py`` as the checker of the CUDA path.
+and by the CPU-baseline leg of ``bench.py``, to check the CUDA path against.
 The product package never imports it.
 """
 from __future__ import annotations
