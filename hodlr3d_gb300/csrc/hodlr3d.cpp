@@ -1472,21 +1472,9 @@ constexpr int kGemvTransposeMax = 32;
 // against 54 ms for 32 columns)
 constexpr int kGemvForwardNoTcMax = 32;
 
-int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld, int precision,
-                  cudaStream_t s, bool trans) {
-  if (!h->assembled) return set_error(HODLR3D_ERR_NOT_ASSEMBLED, "hodlr3d_assemble has not run");
-  if (!x || !y) return set_error(HODLR3D_ERR_INVALID_ARG, "null vector");
-  if (nrhs < 1 || nrhs > 64) return set_error(HODLR3D_ERR_INVALID_ARG, "nrhs must be in 1..64");
-  if (ld < h->N) return set_error(HODLR3D_ERR_INVALID_ARG, "ld < n");
-  if (precision != HODLR3D_FP64 && precision != HODLR3D_MIXED && precision != HODLR3D_FP64X)
-    return set_error(HODLR3D_ERR_INVALID_ARG, "unknown precision %d", precision);
-  if (precision == HODLR3D_MIXED && !h->opt.keep_fp32)
-    return set_error(HODLR3D_ERR_INVALID_ARG, "mixed precision needs keep_fp32");
-  // the FP64-accurate form builds on the FP32 copies; without them, or on a
-  // tree the few-column kernels do not take, it is the FP64 form
-  if (precision == HODLR3D_FP64X && !h->opt.keep_fp32) precision = HODLR3D_FP64;
-  H3D_TRY(ensure_matvec_buffers(h, nrhs));
-  const bool f32 = precision == HODLR3D_MIXED;
+// The operator as the matvec kernels see it: pair tables and factors (FP32
+// copies when f32, else the FP64 factors), and the near field.
+h3d::FarOp far_op(hodlr3d_t h, bool f32) {
   h3d::FarOp far{};
   far.levels = h->levels;
   far.nleaf = h->nleaf;
@@ -1506,6 +1494,10 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
   far.part_off = h->part_off.as<int64_t>();
   far.ufac = f32 ? h->u32.as<const void*>() : h->u64.as<const void*>();
   far.vfac = f32 ? h->v32.as<const void*>() : h->v64.as<const void*>();
+  return far;
+}
+
+h3d::NearOp near_op(hodlr3d_t h) {
   h3d::NearOp nr{};
   nr.nbr_leaf = h->nbr_leaf.as<int32_t>();
   nr.xs = h->xs.as<double>();
@@ -1516,6 +1508,26 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
   nr.zl = h->zl.as<float>();
   nr.centre = h->centre.as<double>();
   nr.kd = h->kd;
+  return nr;
+}
+
+int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld, int precision,
+                  cudaStream_t s, bool trans) {
+  if (!h->assembled) return set_error(HODLR3D_ERR_NOT_ASSEMBLED, "hodlr3d_assemble has not run");
+  if (!x || !y) return set_error(HODLR3D_ERR_INVALID_ARG, "null vector");
+  if (nrhs < 1 || nrhs > 64) return set_error(HODLR3D_ERR_INVALID_ARG, "nrhs must be in 1..64");
+  if (ld < h->N) return set_error(HODLR3D_ERR_INVALID_ARG, "ld < n");
+  if (precision != HODLR3D_FP64 && precision != HODLR3D_MIXED && precision != HODLR3D_FP64X)
+    return set_error(HODLR3D_ERR_INVALID_ARG, "unknown precision %d", precision);
+  if (precision == HODLR3D_MIXED && !h->opt.keep_fp32)
+    return set_error(HODLR3D_ERR_INVALID_ARG, "mixed precision needs keep_fp32");
+  // the FP64-accurate form builds on the FP32 copies; without them, or on a
+  // tree the few-column kernels do not take, it is the FP64 form
+  if (precision == HODLR3D_FP64X && !h->opt.keep_fp32) precision = HODLR3D_FP64;
+  H3D_TRY(ensure_matvec_buffers(h, nrhs));
+  const bool f32 = precision == HODLR3D_MIXED;
+  h3d::FarOp far = far_op(h, f32);
+  const h3d::NearOp nr = near_op(h);
   h3d::MatvecBuffers B{};
   B.xsorted = h->xsorted.p;
   B.tbuf = h->tbuf.p;
@@ -1567,8 +1579,7 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
   }
   if (fp64x && !use_gemv) {
     precision = HODLR3D_FP64;
-    far.ufac = h->u64.as<const void*>();
-    far.vfac = h->v64.as<const void*>();
+    far = far_op(h, false);
   }
   if (h->engine == 3 && !use_gemv && !fp64x)
     return set_error(HODLR3D_ERR_UNSUPPORTED,
@@ -1850,35 +1861,8 @@ int hodlr3d_matvec_noalloc(hodlr3d_t h, const double* x, double* y, int nrhs, in
   H3D_CUDA(h3d::noalloc_scratch(h->device, &base));
   unsigned char* b8 = static_cast<unsigned char*>(base);
   const bool f32 = precision == HODLR3D_MIXED;
-  h3d::FarOp far{};
-  far.levels = h->levels;
-  far.nleaf = h->nleaf;
-  far.leaf_off = h->leaf_off.as<int32_t>();
-  far.il_ptr = h->il_ptr.as<int64_t>();
-  far.rev = h->rev.as<int32_t>();
-  far.rank = h->rank.as<int32_t>();
-  far.pair_level = h->pair_level.as<int32_t>();
-  far.pair_tgt = h->pair_tgt.as<int32_t>();
-  far.pair_src = h->pair_src.as<int32_t>();
-  far.tr_off = h->tr_off.as<int64_t>();
-  far.ustride = h->ustride.as<int32_t>();
-  far.tc_toff = h->tc_toff.as<int64_t>();
-  far.tc_tld = h->tc_tld.as<int32_t>();
-  far.tc_tbox = h->tc_tbox.as<int64_t>();
-  far.tc_rbox = h->tc_rbox.as<int32_t>();
-  far.part_off = h->part_off.as<int64_t>();
-  far.ufac = f32 ? h->u32.as<const void*>() : h->u64.as<const void*>();
-  far.vfac = f32 ? h->v32.as<const void*>() : h->v64.as<const void*>();
-  h3d::NearOp nrop{};
-  nrop.nbr_leaf = h->nbr_leaf.as<int32_t>();
-  nrop.xs = h->xs.as<double>();
-  nrop.ys = h->ys.as<double>();
-  nrop.zs = h->zs.as<double>();
-  nrop.xl = h->xl.as<float>();
-  nrop.yl = h->yl.as<float>();
-  nrop.zl = h->zl.as<float>();
-  nrop.centre = h->centre.as<double>();
-  nrop.kd = h->kd;
+  const h3d::FarOp far = far_op(h, f32);
+  const h3d::NearOp nrop = near_op(h);
   h3d::MatvecBuffers B{};
   B.xsorted = b8;
   B.tbuf = b8 + b_x;
@@ -1938,6 +1922,9 @@ int hodlr3d_dense_rows(hodlr3d_t h, const int64_t* rows, int64_t nrows, const do
   H3D_TRY(check_handle(h));
   if (!rows || !x || !y || nrows < 0 || nrhs < 1 || ldx < h->N)
     return set_error(HODLR3D_ERR_INVALID_ARG, "bad arguments");
+  // one block per (row, column): the grid's limits
+  if (nrows > INT32_MAX || nrhs > 65535)
+    return set_error(HODLR3D_ERR_INVALID_ARG, "nrows must be <= 2^31 - 1 and nrhs <= 65535");
   h3d::launch_dense_rows((cudaStream_t)stream, h->N, h->xyz.as<double>(), h->kd,
                          rows, nrows, x, ldx, y, nrhs);
   ++h->launches;
@@ -2200,6 +2187,8 @@ int hodlr3d_device_status(hodlr3d_t h) {
   H3D_CUDA(cudaDeviceSynchronize());
   int v = 0;
   if (h->dev_err.p) H3D_CUDA(cudaMemcpy(&v, h->dev_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (v == 2)
+    return set_error(HODLR3D_ERR_CUDA, "a tensor-core block's operand table overflowed (results of that call are invalid)");
   if (v) return set_error(HODLR3D_ERR_CUDA, "a tensor-core wait gave up (results of that call are invalid)");
   return HODLR3D_OK;
 }

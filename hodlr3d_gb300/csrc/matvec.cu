@@ -446,6 +446,10 @@ __global__ void k_dense_rows(int64_t N, const double* __restrict__ xyz, KernelDe
   const int64_t r = blockIdx.x;
   const int c = blockIdx.y;
   const int64_t i = rows[r];
+  if (i < 0 || i >= N) {  // a row id outside the point set: NaN, nothing read
+    if (threadIdx.x == 0) Y[c * nrows + r] = __longlong_as_double(0x7ff8000000000000LL);
+    return;
+  }
   const double xi = xyz[3 * i], yi = xyz[3 * i + 1], zi = xyz[3 * i + 2];
   double acc = 0.0;
   for (int64_t j = threadIdx.x; j < N; j += blockDim.x) {

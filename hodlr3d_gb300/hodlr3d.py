@@ -177,7 +177,10 @@ class HODLR3D:
         """FP64 direct sum of sampled rows: y[r] = sum_j K(rows[r], j) x[j]."""
         import torch
         xc, nrhs, shape = self._dev_cols(x)
-        rows_t = torch.as_tensor(np.asarray(rows, np.int64), device=xc.device)
+        rows_np = np.asarray(rows, np.int64).reshape(-1)
+        if rows_np.size and (rows_np.min() < 0 or rows_np.max() >= self.N):
+            raise ValueError(f"row ids must lie in [0, {self.N})")
+        rows_t = torch.as_tensor(rows_np, device=xc.device)
         y = torch.empty((nrhs, len(rows_t)), dtype=torch.float64, device=xc.device)
         check(self._L.hodlr3d_dense_rows(self.handle, rows_t.data_ptr(), len(rows_t), xc.data_ptr(),
                                          y.data_ptr(), nrhs, self.N,

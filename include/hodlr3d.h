@@ -165,7 +165,9 @@ int hodlr3d_matvec_transpose(hodlr3d_t h, const double* x, double* y, int nrhs, 
                              int precision, void* stream);
 /* y[r] = sum_j K(rows[r], j) x[j], the dense FP64 product of sampled rows
  * (the reference drivers' check by columns, kernel::getCol,
- * src/kernel.cpp:27-35; K symmetric).  Device pointers, nrhs columns. */
+ * src/kernel.cpp:27-35; K symmetric).  Device pointers, nrhs columns; y is
+ * nrhs x nrows (column c at y + c nrows).  A row id outside [0, n) gives NaN
+ * in its outputs (the ids are on the device, so they are checked there). */
 int hodlr3d_dense_rows(hodlr3d_t h, const int64_t* rows, int64_t nrows, const double* x,
                        double* y, int nrhs, int64_t ldx, void* stream);
 

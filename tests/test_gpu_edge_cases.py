@@ -50,3 +50,24 @@ def test_engines_agree_on_ragged_trees(clustered, nrhs, transpose):
     yx = H.matvec(X, "fp64x", transpose=transpose)
     H.device_status()
     assert colerr(yx, y64) <= 1e-12
+
+
+def test_dense_rows_outside_the_point_set(clustered):
+    """Row ids outside [0, n): the Python mirror refuses them; through the C ABI
+    (device ids, checked by the kernel) their outputs are NaN and the others
+    are unaffected."""
+    from hodlr3d_gb300 import _lib
+    H = clustered
+    x = torch.tensor(np.random.default_rng(2).standard_normal(H.N), device="cuda")
+    with pytest.raises(ValueError):
+        H.dense_rows([0, H.N], x)
+    rows = torch.tensor([3, -1, H.N, 7], dtype=torch.int64, device="cuda")
+    y = torch.empty(4, dtype=torch.float64, device="cuda")
+    st = _lib.lib().hodlr3d_dense_rows(H.handle, rows.data_ptr(), 4, x.data_ptr(), y.data_ptr(),
+                                       1, H.N, torch.cuda.current_stream().cuda_stream)
+    assert st == _lib.OK
+    torch.cuda.synchronize()
+    H.device_status()
+    good = H.dense_rows([3, 7], x)
+    assert torch.isnan(y[1]) and torch.isnan(y[2])
+    assert torch.equal(y[[0, 3]], good)
