@@ -18,7 +18,9 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <new>
 #include <numeric>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -42,6 +44,23 @@ int set_error(int code, const char* fmt, ...) {
   va_end(ap);
   g_last_error = buf;
   return code;
+}
+
+// The C entry points are function-try-blocks whose handler returns this: an
+// exception (a host allocation that failed) becomes a status code instead of
+// crossing the C ABI.
+int exception_status() noexcept {
+  try {
+    throw;
+  } catch (const std::bad_alloc&) {
+    return set_error(HODLR3D_ERR_OUT_OF_MEMORY, "host allocation failed");
+  } catch (const std::length_error&) {
+    return set_error(HODLR3D_ERR_OUT_OF_MEMORY, "host allocation too large");
+  } catch (const std::exception& e) {
+    return set_error(HODLR3D_ERR_INVALID_ARG, "unexpected error: %s", e.what());
+  } catch (...) {
+    return set_error(HODLR3D_ERR_INVALID_ARG, "unexpected error");
+  }
 }
 
 #define H3D_CUDA(call)                                                                   \
@@ -977,8 +996,10 @@ int load_factors(const char* path, const hodlr3d_options* opt, hodlr3d_t* out) {
   if (std::fread(magic, 1, 8, F.f) != 8 || std::memcmp(magic, kFactMagic, 8) != 0)
     return set_error(HODLR3D_ERR_IO, "%s is not a hodlr3d factor file (version 1)", path);
   FileHeader hd{};
+  // sizes are checked before anything is allocated from them: the point count
+  // within what hodlr3d_create takes, at most one pool per pair
   if (!F.read(&hd, sizeof hd) || hd.version != 1 || hd.header_bytes != sizeof(FileHeader) || hd.n < 2 ||
-      hd.npairs < 0 || hd.npools < 0)
+      hd.n > INT32_MAX / 2 || hd.npairs < 0 || hd.npools < 0 || hd.npools > std::max<int64_t>(hd.npairs, 1))
     return set_error(HODLR3D_ERR_IO, "%s: unreadable header", path);
   std::vector<double> xyz(3 * (size_t)hd.n);
   if (!F.read(xyz.data(), sizeof(double) * xyz.size())) return set_error(HODLR3D_ERR_IO, "%s: truncated", path);
@@ -1005,7 +1026,7 @@ int load_factors(const char* path, const hodlr3d_options* opt, hodlr3d_t* out) {
   h->h_fac_off.assign(np, 0);
   for (int64_t p = 0; p < np; ++p) {
     const int r = pr[p].rank;
-    if (r < 0 || r > h->N || pr[p].pool < -1 || pr[p].pool >= hd.npools)
+    if (r < 0 || r > h->N || pr[p].pool < -1 || pr[p].pool >= hd.npools || (pr[p].pool < 0 && r > 0))
       return set_error(HODLR3D_ERR_IO, "%s: corrupt pair record %lld", path, (long long)p);
     h->h_rank[p] = r;
     h->h_piv_rows[p].resize(r);
@@ -1043,6 +1064,10 @@ int load_factors(const char* path, const hodlr3d_options* opt, hodlr3d_t* out) {
     const int64_t r = pr[p].rank;
     if (pr[p].off < 0 || pr[p].off + r * ((a1 - a0) + (b1 - b0)) > counts[pr[p].pool])
       return set_error(HODLR3D_ERR_IO, "%s: pair %lld lies outside its pool", path, (long long)p);
+    for (int l = 0; l < r; ++l)
+      if (h->h_piv_rows[p][l] < 0 || h->h_piv_rows[p][l] >= a1 - a0 || h->h_piv_cols[p][l] < 0 ||
+          h->h_piv_cols[p][l] >= b1 - b0)
+        return set_error(HODLR3D_ERR_IO, "%s: pivot of pair %lld outside its boxes", path, (long long)p);
     double* base = h->pools[pr[p].pool]->as<double>() + pr[p].off;
     h->h_fac_pool[p] = pr[p].pool;
     h->h_fac_off[p] = pr[p].off;
@@ -1738,7 +1763,7 @@ void hodlr3d_default_options(hodlr3d_options* opt) {
 }
 
 int hodlr3d_create(const double* xyz, int64_t n, int nP1D, double L, int tol_pow, int kernel_id,
-                   const hodlr3d_options* opt, hodlr3d_t* out) {
+                   const hodlr3d_options* opt, hodlr3d_t* out) try {
   if (!out) return set_error(HODLR3D_ERR_INVALID_ARG, "null output handle");
   *out = nullptr;
   if (!xyz || n < 2) return set_error(HODLR3D_ERR_INVALID_ARG, "need at least 2 points");
@@ -1792,6 +1817,8 @@ int hodlr3d_create(const double* xyz, int64_t n, int nP1D, double L, int tol_pow
   }
   *out = h;
   return HODLR3D_OK;
+} catch (...) {
+  return exception_status();
 }
 
 void hodlr3d_destroy(hodlr3d_t h) {
@@ -1801,38 +1828,48 @@ void hodlr3d_destroy(hodlr3d_t h) {
   delete h;
 }
 
-int hodlr3d_assemble(hodlr3d_t h) {
+int hodlr3d_assemble(hodlr3d_t h) try {
   H3D_TRY(check_handle(h));
   return assemble(h);
+} catch (...) {
+  return exception_status();
 }
 
-int hodlr3d_save(hodlr3d_t h, const char* path) {
+int hodlr3d_save(hodlr3d_t h, const char* path) try {
   H3D_TRY(check_handle(h));
   if (!path) return set_error(HODLR3D_ERR_INVALID_ARG, "null path");
   return save_factors(h, path);
+} catch (...) {
+  return exception_status();
 }
 
-int hodlr3d_load(const char* path, const hodlr3d_options* opt, hodlr3d_t* out) {
+int hodlr3d_load(const char* path, const hodlr3d_options* opt, hodlr3d_t* out) try {
   if (!out) return set_error(HODLR3D_ERR_INVALID_ARG, "null output handle");
   *out = nullptr;
   if (!path) return set_error(HODLR3D_ERR_INVALID_ARG, "null path");
   return load_factors(path, opt, out);
+} catch (...) {
+  return exception_status();
 }
 
 int hodlr3d_matvec(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld, int precision,
-                   void* stream) {
+                   void* stream) try {
   H3D_TRY(check_handle(h));
   return matvec_device(h, x, y, nrhs, ld, precision, (cudaStream_t)stream, false);
+} catch (...) {
+  return exception_status();
 }
 
 int hodlr3d_matvec_transpose(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
-                             int precision, void* stream) {
+                             int precision, void* stream) try {
   H3D_TRY(check_handle(h));
   return matvec_device(h, x, y, nrhs, ld, precision, (cudaStream_t)stream, true);
+} catch (...) {
+  return exception_status();
 }
 
 int hodlr3d_matvec_noalloc(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
-                           int precision, void* stream) {
+                           int precision, void* stream) try {
   H3D_TRY(check_handle(h));
   if (!h->assembled) return set_error(HODLR3D_ERR_NOT_ASSEMBLED, "hodlr3d_assemble has not run");
   if (!x || !y) return set_error(HODLR3D_ERR_INVALID_ARG, "null vector");
@@ -1877,10 +1914,12 @@ int hodlr3d_matvec_noalloc(hodlr3d_t h, const double* x, double* y, int nrhs, in
                                     x, ld, y, ld, nrhs, precision, 0, nullptr);
   H3D_CUDA(cudaGetLastError());
   return HODLR3D_OK;
+} catch (...) {
+  return exception_status();
 }
 
 int hodlr3d_matvec_host(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
-                        int precision) {
+                        int precision) try {
   H3D_TRY(check_handle(h));
   if (!x || !y) return set_error(HODLR3D_ERR_INVALID_ARG, "null vector");
   if (nrhs < 1 || nrhs > 64 || ld < h->N) return set_error(HODLR3D_ERR_INVALID_ARG, "bad nrhs or ld");
@@ -1895,9 +1934,11 @@ int hodlr3d_matvec_host(hodlr3d_t h, const double* x, double* y, int nrhs, int64
   H3D_CUDA(cudaMemcpy2DAsync(y, pitch, h->stage_y.p, col, col, nrhs, cudaMemcpyDeviceToHost, s));
   H3D_CUDA(cudaStreamSynchronize(s));
   return HODLR3D_OK;
+} catch (...) {
+  return exception_status();
 }
 
-int hodlr3d_matvec_host_rows(hodlr3d_t h, const double* x, double* y, int nrhs, int precision) {
+int hodlr3d_matvec_host_rows(hodlr3d_t h, const double* x, double* y, int nrhs, int precision) try {
   H3D_TRY(check_handle(h));
   if (!x || !y) return set_error(HODLR3D_ERR_INVALID_ARG, "null vector");
   if (nrhs < 1 || nrhs > 64) return set_error(HODLR3D_ERR_INVALID_ARG, "bad nrhs");
@@ -1915,10 +1956,12 @@ int hodlr3d_matvec_host_rows(hodlr3d_t h, const double* x, double* y, int nrhs, 
   H3D_CUDA(cudaMemcpyAsync(y, h->stage_t.p, bytes, cudaMemcpyDeviceToHost, s));
   H3D_CUDA(cudaStreamSynchronize(s));
   return HODLR3D_OK;
+} catch (...) {
+  return exception_status();
 }
 
 int hodlr3d_dense_rows(hodlr3d_t h, const int64_t* rows, int64_t nrows, const double* x, double* y,
-                       int nrhs, int64_t ldx, void* stream) {
+                       int nrhs, int64_t ldx, void* stream) try {
   H3D_TRY(check_handle(h));
   if (!rows || !x || !y || nrows < 0 || nrhs < 1 || ldx < h->N)
     return set_error(HODLR3D_ERR_INVALID_ARG, "bad arguments");
@@ -1930,11 +1973,13 @@ int hodlr3d_dense_rows(hodlr3d_t h, const int64_t* rows, int64_t nrows, const do
   ++h->launches;
   H3D_CUDA(cudaGetLastError());
   return HODLR3D_OK;
+} catch (...) {
+  return exception_status();
 }
 
 int hodlr3d_gmres(hodlr3d_t h, const double* b, double* x, int nrhs, int64_t ld,
                   const hodlr3d_gmres_params* prm, hodlr3d_gmres_result* res, double* hist,
-                  int hist_cap, int* n_hist, void* stream) {
+                  int hist_cap, int* n_hist, void* stream) try {
   H3D_TRY(check_handle(h));
   if (!h->assembled) return set_error(HODLR3D_ERR_NOT_ASSEMBLED, "hodlr3d_assemble has not run");
   if (!b || !x || !prm || nrhs < 1 || nrhs > 64 || ld < h->N || prm->maxit < 1 || !(prm->tol > 0))
@@ -2053,9 +2098,11 @@ int hodlr3d_gmres(hodlr3d_t h, const double* b, double* x, int nrhs, int64_t ld,
     return set_error(HODLR3D_ERR_NO_CONVERGENCE, "GMRES reached %d iterations at %.3e", total_it, final_err);
   }
   return HODLR3D_OK;
+} catch (...) {
+  return exception_status();
 }
 
-int hodlr3d_get_stats(hodlr3d_t h, hodlr3d_stats* s) {
+int hodlr3d_get_stats(hodlr3d_t h, hodlr3d_stats* s) try {
   if (!h || !s) return set_error(HODLR3D_ERR_INVALID_ARG, "null argument");
   std::memset(s, 0, sizeof(*s));
   s->n_points = h->N;
@@ -2105,26 +2152,32 @@ int hodlr3d_get_stats(hodlr3d_t h, hodlr3d_stats* s) {
   s->near_entries = ne;
   s->memory_entries = mem;
   return HODLR3D_OK;
+} catch (...) {
+  return exception_status();
 }
 
-int hodlr3d_get_tree(hodlr3d_t h, int32_t* perm, int64_t* leaf_off) {
+int hodlr3d_get_tree(hodlr3d_t h, int32_t* perm, int64_t* leaf_off) try {
   if (!h) return set_error(HODLR3D_ERR_INVALID_ARG, "null handle");
   if (perm) std::copy(h->h_perm.begin(), h->h_perm.end(), perm);
   if (leaf_off)
     for (int64_t k = 0; k <= h->nleaf; ++k) leaf_off[k] = h->h_leaf_off[k];
   return HODLR3D_OK;
+} catch (...) {
+  return exception_status();
 }
 
-int hodlr3d_get_neighbors(hodlr3d_t h, int level, int32_t* nbr) {
+int hodlr3d_get_neighbors(hodlr3d_t h, int level, int32_t* nbr) try {
   H3D_TRY(check_handle(h));
   if (!nbr || level < 0 || level > h->levels) return set_error(HODLR3D_ERR_INVALID_ARG, "bad level");
   const int64_t nb = int64_t(1) << (3 * level);
   H3D_CUDA(cudaMemcpy(nbr, h->nbr_all.as<int32_t>() + 26 * h3d::level_base(level),
                       sizeof(int32_t) * 26 * nb, cudaMemcpyDeviceToHost));
   return HODLR3D_OK;
+} catch (...) {
+  return exception_status();
 }
 
-int hodlr3d_get_pairs(hodlr3d_t h, int32_t* lts) {
+int hodlr3d_get_pairs(hodlr3d_t h, int32_t* lts) try {
   if (!h || !lts) return set_error(HODLR3D_ERR_INVALID_ARG, "null argument");
   for (int64_t p = 0; p < h->npairs; ++p) {
     const int j = h->h_pair_level[p];
@@ -2133,16 +2186,20 @@ int hodlr3d_get_pairs(hodlr3d_t h, int32_t* lts) {
     lts[3 * p + 2] = (int32_t)(h->h_pair_src[p] - h3d::level_base(j));
   }
   return HODLR3D_OK;
+} catch (...) {
+  return exception_status();
 }
 
-int hodlr3d_get_ranks(hodlr3d_t h, int32_t* rank) {
+int hodlr3d_get_ranks(hodlr3d_t h, int32_t* rank) try {
   if (!h || !rank) return set_error(HODLR3D_ERR_INVALID_ARG, "null argument");
   if (!h->assembled) return set_error(HODLR3D_ERR_NOT_ASSEMBLED, "not assembled");
   std::copy(h->h_rank.begin(), h->h_rank.end(), rank);
   return HODLR3D_OK;
+} catch (...) {
+  return exception_status();
 }
 
-int hodlr3d_get_pivots(hodlr3d_t h, int32_t* rows, int32_t* cols) {
+int hodlr3d_get_pivots(hodlr3d_t h, int32_t* rows, int32_t* cols) try {
   if (!h || !rows || !cols) return set_error(HODLR3D_ERR_INVALID_ARG, "null argument");
   if (!h->assembled) return set_error(HODLR3D_ERR_NOT_ASSEMBLED, "not assembled");
   int64_t w = 0;
@@ -2158,9 +2215,11 @@ int hodlr3d_get_pivots(hodlr3d_t h, int32_t* rows, int32_t* cols) {
     }
   }
   return HODLR3D_OK;
+} catch (...) {
+  return exception_status();
 }
 
-int hodlr3d_get_pair_factors(hodlr3d_t h, int64_t pair, double* U, double* V) {
+int hodlr3d_get_pair_factors(hodlr3d_t h, int64_t pair, double* U, double* V) try {
   H3D_TRY(check_handle(h));
   if (!h->assembled) return set_error(HODLR3D_ERR_NOT_ASSEMBLED, "not assembled");
   if (pair < 0 || pair >= h->npairs) return set_error(HODLR3D_ERR_INVALID_ARG, "pair out of range");
@@ -2172,17 +2231,21 @@ int hodlr3d_get_pair_factors(hodlr3d_t h, int64_t pair, double* U, double* V) {
   if (U && r) H3D_CUDA(cudaMemcpy(U, h->h_u64[pair], sizeof(double) * r * (a1 - a0), cudaMemcpyDeviceToHost));
   if (V && r) H3D_CUDA(cudaMemcpy(V, h->h_v64[pair], sizeof(double) * r * (b1 - b0), cudaMemcpyDeviceToHost));
   return HODLR3D_OK;
+} catch (...) {
+  return exception_status();
 }
 
 int64_t hodlr3d_launch_count(hodlr3d_t h) { return h ? h->launches : 0; }
 
-int hodlr3d_set_engine(hodlr3d_t h, int engine) {
+int hodlr3d_set_engine(hodlr3d_t h, int engine) try {
   if (!h || engine < 0 || engine > 3) return set_error(HODLR3D_ERR_INVALID_ARG, "engine must be 0, 1, 2 or 3");
   h->engine = engine;
   return HODLR3D_OK;
+} catch (...) {
+  return exception_status();
 }
 
-int hodlr3d_device_status(hodlr3d_t h) {
+int hodlr3d_device_status(hodlr3d_t h) try {
   H3D_TRY(check_handle(h));
   H3D_CUDA(cudaDeviceSynchronize());
   int v = 0;
@@ -2191,17 +2254,21 @@ int hodlr3d_device_status(hodlr3d_t h) {
     return set_error(HODLR3D_ERR_CUDA, "a tensor-core block's operand table overflowed (results of that call are invalid)");
   if (v) return set_error(HODLR3D_ERR_CUDA, "a tensor-core wait gave up (results of that call are invalid)");
   return HODLR3D_OK;
+} catch (...) {
+  return exception_status();
 }
 
-int hodlr3d_set_profiling(hodlr3d_t h, int enable) {
+int hodlr3d_set_profiling(hodlr3d_t h, int enable) try {
   if (!h) return set_error(HODLR3D_ERR_INVALID_ARG, "null handle");
   h->profiling = enable != 0;
   h->prof.spans.clear();
   h->prof.used = 0;
   return HODLR3D_OK;
+} catch (...) {
+  return exception_status();
 }
 
-int hodlr3d_profile_report(hodlr3d_t h, char* buf, int cap) {
+int hodlr3d_profile_report(hodlr3d_t h, char* buf, int cap) try {
   H3D_TRY(check_handle(h));
   if (!buf || cap <= 0) return set_error(HODLR3D_ERR_INVALID_ARG, "bad buffer");
   std::vector<std::string> names;
@@ -2231,6 +2298,8 @@ int hodlr3d_profile_report(hodlr3d_t h, char* buf, int cap) {
   h->prof.used = 0;
   snprintf(buf, (size_t)cap, "%s", out.c_str());
   return HODLR3D_OK;
+} catch (...) {
+  return exception_status();
 }
 
 }  // extern "C"

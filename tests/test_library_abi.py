@@ -91,14 +91,22 @@ def test_factor_header_reader(tmp_path):
 
 
 def test_factor_file_validation_before_any_device_work(tmp_path):
-    """Wrong magic, wrong version and truncated points are refused with
-    HODLR3D_ERR_IO while reading, before the tree is rebuilt on a device."""
+    """Wrong magic, wrong version, truncated points and header sizes that no
+    saved operator has (more points than hodlr3d_create takes, more pools
+    than pairs, negative counts) are refused with HODLR3D_ERR_IO while
+    reading, before anything is allocated from them or the tree is rebuilt
+    on a device."""
     L = _lib.lib()
     h = ctypes.c_void_p()
     cases = {
         "magic.h3d": b"H3DFACT9" + _factor_header()[8:],
         "version.h3d": _factor_header(version=2),
         "truncated.h3d": _factor_header(n=64) + b"\0" * 100,  # 64 points need 1536 bytes
+        "huge_n.h3d": _factor_header(n=1 << 60),
+        "one_point.h3d": _factor_header(n=1),
+        "pools.h3d": _factor_header(npairs=10, npools=11),
+        "neg_pairs.h3d": _factor_header(npairs=-1),
+        "neg_pools.h3d": _factor_header(npools=-3),
     }
     for name, data in cases.items():
         p = tmp_path / name
