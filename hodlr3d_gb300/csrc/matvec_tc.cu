@@ -237,7 +237,6 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
   // 4 kq .. 4 kq + 3 of every chunk and accumulator columns 8 kq .. 8 kq + 7,
   // kq = w / 4; each copies B's k quad qb of column cb.
   const int w = tid >> 5, lane = tid & 31, kq = w >> 2;
-  const bool copies_b = true;
   CopyMap m;
   m.cb = 8 * (tid >> 7) + ((tid >> 2) & 7);
   m.qb = 4 * ((tid >> 5) & 3) + (tid & 3);
@@ -257,7 +256,7 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
   int nload = 0;
   for (int i = 0; i < kAhead; ++i) {
     if (nload < nch) {
-      if (copies_b) src.load_b(nload, smem + (nload % kSlots) * SLOT_BYTES, m);
+      src.load_b(nload, smem + (nload % kSlots) * SLOT_BYTES, m);
       ++nload;
     }
     cp_async_commit();
@@ -290,7 +289,7 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
                                      (uint32_t)(((c / kABuf) - 1) & 1), kWaitLimit, kWaitHintNs))
       atomicExch(err, 1);
     if (nload < nch) {
-      if (copies_b) src.load_b(nload, smem + (nload % kSlots) * SLOT_BYTES, m);
+      src.load_b(nload, smem + (nload % kSlots) * SLOT_BYTES, m);
       ++nload;
     }
     cp_async_commit();
@@ -321,7 +320,7 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
         tc::tmem_st16(ta, hi);
         tc::tmem_st16(ta + (uint32_t)KC, lo);
       }
-      if (copies_b && src.fresh_b(c)) {
+      if (src.fresh_b(c)) {
         // the B segment this thread copied: low part next to it
         unsigned char* sb = slot + m.offB;
         const float4 xb = *reinterpret_cast<const float4*>(sb);

@@ -278,6 +278,8 @@ class HODLR3D:
             raise TypeError("expected a CUDA torch tensor")
         if x.dtype != torch.float64:
             raise TypeError("expected float64")
+        if x.device.index != self.device:
+            raise ValueError(f"the operator lives on cuda:{self.device}, the tensor on {x.device}")
         shape = tuple(x.shape)
         xx = x.reshape(-1, 1) if x.dim() == 1 else x
         if xx.dim() != 2 or xx.shape[0] != self.N:

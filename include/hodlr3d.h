@@ -146,7 +146,8 @@ int hodlr3d_matvec(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld
  * until exit, and sizes needing more are refused with HODLR3D_ERR_INVALID_ARG.
  * The first call on a device looks the array's address up (make it before
  * any stream capture).  All calls share the array, so calls that overlap on
- * the GPU race.  Device pointers, enqueued on `stream`. */
+ * the GPU race.  It runs the CUDA-core kernels only: HODLR3D_FP64X is
+ * computed in the FP64 form.  Device pointers, enqueued on `stream`. */
 int hodlr3d_matvec_noalloc(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
                            int precision, void* stream);
 /* Same with host pointers (pageable or pinned): copies in, multiplies,
