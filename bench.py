@@ -460,6 +460,20 @@ def run_ours(args):
     except RuntimeError as e:  # capture refused by the runtime: report, keep going
         graph = {"error": str(e)[:200]}
 
+    # ---- the engine autotuner over this operator (after the timed
+    # measurements; the automatic choice returns to the rules afterwards) -----
+    tune = None
+    if not args.no_autotune:
+        t = time.perf_counter()
+        rows = H.autotune(reps=3)
+        ch = H.tuning()
+        H.autotune(reps=0)
+        counts = (1, 2, 4, 8, 16, 32, 64)
+        tune = {"seconds": time.perf_counter() - t,
+                "forward": {n: ch["forward"][n - 1] for n in counts},
+                "transpose": {n: ch["transpose"][n - 1] for n in counts},
+                "ms": {f"{'AT' if tr else 'A'}_{n}_{e}": round(ms, 3) for tr, n, e, ms in rows}}
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -476,6 +490,7 @@ def run_ours(args):
             "gpu_launches": int(launches), "clocks": clocks,
             "fp64_1rhs": {"rhs_per_s": 1e3 / ms64, "ms": ms64},
             "cuda_graph": graph,
+            "autotune": tune,
             "mixed_1rhs": one,
             "fp64x_1rhs": fp64x,
             "speedup_mixed_batched_vs_fp64": value / ws / (1e3 / ms64),
@@ -504,6 +519,7 @@ def main():
     ap.add_argument("--diag", type=float, default=float("nan"),
                     help="diagonal value override (e.g. 1 for exp(-r), Qchoice 1)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="skip the engine autotuner's table")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

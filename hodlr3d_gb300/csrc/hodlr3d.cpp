@@ -259,6 +259,9 @@ struct hodlr3d_handle {
   bool profiling = false;
   Prof prof;
   int engine = 0;   // 0 auto, 1 SIMT kernels, 2 tensor-core kernels, 3 few-column kernels
+  // automatic choice for the mixed product, per (transpose, nrhs), from the
+  // timings of hodlr3d_autotune: 0 = the column-count rules, else an engine
+  int8_t tuned[2][65] = {};
   DevBuf dev_err;   // set by kernels whose bounded waits gave up
   bool leaves_aligned = false;  // every leaf population a multiple of 4
   DevBuf knear, near_off;       // FP32 near-field blocks of the tensor-core engine
@@ -740,6 +743,7 @@ int assemble(hodlr3d_t h) {
 // copies, the matvec's per-pair tables and their device copies.
 int finish_assembly(hodlr3d_t h, double t_start) {
   const int64_t np = h->npairs;
+  std::memset(h->tuned, 0, sizeof h->tuned);  // timings of another operator
   if (h->opt.keep_fp32) H3D_TRY(group_fp32(h));
   // per-pair tables for the matvec: T offsets, slice work items of the
   // non-leaf pairs, partial offsets of the pairs above level d - 1
@@ -1571,18 +1575,21 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
   // are faster.
   const bool mixed = precision == HODLR3D_MIXED;
   const bool fp64x = precision == HODLR3D_FP64X;
+  // the engine of this call: forced, tuned (automatic choice after
+  // hodlr3d_autotune, mixed form) or 0 for the rules below
+  const int engine = h->engine == 0 && mixed ? h->tuned[trans ? 1 : 0][nrhs] : h->engine;
   // trees the tensor-core engine takes (16-byte aligned leaf rows, bounded tables)
   const bool tc_tree = h->max_leaf <= 128 && h->leaves_aligned && h->tc_entries <= h3d::tc_max_entries();
   const int gemv_max = trans ? kGemvTransposeMax : (tc_tree ? kGemvForwardMax : kGemvForwardNoTcMax);
   bool use_gemv = false;
   // fp64x: the few-column kernels (automatic or forced); forcing the CUDA-core
   // kernels gives the FP64 form; the tensor cores have no FP64-accurate form
-  if (fp64x && h->engine == 2)
+  if (fp64x && engine == 2)
     return set_error(HODLR3D_ERR_UNSUPPORTED,
                      "the tensor-core engine has no FP64-accurate form (use HODLR3D_MIXED or "
                      "another engine)");
-  if ((fp64x && h->engine != 1) ||
-      (mixed && (h->engine == 3 || (h->engine == 0 && nrhs <= gemv_max)))) {
+  if ((fp64x && engine != 1) ||
+      (mixed && (engine == 3 || (engine == 0 && nrhs <= gemv_max)))) {
     H3D_TRY(ensure_near_blocks(h, nr, s));
     H3D_TRY(ensure_gemv(h, s));
     use_gemv = h->gemv_ok;
@@ -1606,22 +1613,117 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
     precision = HODLR3D_FP64;
     far = far_op(h, false);
   }
-  if (h->engine == 3 && !use_gemv && !fp64x)
+  if (engine == 3 && !use_gemv && !fp64x)
     return set_error(HODLR3D_ERR_UNSUPPORTED,
                      "the few-column engine needs the mixed form, leaves whose near-field inputs "
                      "fit its shared memory and fewer than 2^31 rows of T");
   if (use_gemv) return run_gemv(h, x, y, nrhs, ld, s, trans, fp64x);
   const bool tc_ok = mixed && !trans && tc_tree;
-  if (h->engine == 2 && !tc_ok)
+  if (engine == 2 && !tc_ok)
     return set_error(HODLR3D_ERR_UNSUPPORTED,
                      "the tensor-core engine needs A x (not the transpose) in the mixed form, "
                      "leaves of at most 128 points, each a multiple of 4, and at most %d pairs per "
                      "block (this tree: %d)", h3d::tc_max_entries(), h->tc_entries);
-  if (tc_ok && h->engine != 1) return run_tc(h, far, nr, x, y, nrhs, ld, s);
+  if (tc_ok && engine != 1) return run_tc(h, far, nr, x, y, nrhs, ld, s);
   // the CUDA-core engine (matvec.cu)
   h->launches += h3d::launch_matvec(s, h->N, h->perm.as<int32_t>(), far, nr, B, x, ld, y, ld, nrhs,
                                     precision, trans ? 1 : 0, h->profiling ? &h->prof : nullptr);
   H3D_CUDA(cudaGetLastError());
+  return HODLR3D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// autotuning of the automatic engine choice
+// ---------------------------------------------------------------------------
+// Column counts timed; a count between two of them takes the choice of the
+// next one up (the engines' costs step at powers of two: the tensor cores pad
+// to 32 columns, the CUDA-core kernels to the next power of two, the
+// few-column kernels run passes of 4 or 8).
+constexpr int kTuneCounts[] = {1, 2, 4, 8, 16, 32, 64};
+constexpr int kNumTuneCounts = sizeof(kTuneCounts) / sizeof(kTuneCounts[0]);
+
+struct EventPair {
+  cudaEvent_t a = nullptr, b = nullptr;
+  ~EventPair() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+};
+
+// Times every engine that runs the mixed product of this operator (A x: CUDA
+// cores, tensor cores, few-column kernels; A^T x: CUDA cores, few-column) at
+// each count of kTuneCounts, `reps` timed products after one untimed, the
+// median kept; the fastest fills h->tuned.  The inputs are one constant (every
+// byte 0x3F: 4.8e-4; no kernel branches on values).  The forced engine
+// (hodlr3d_set_engine) is restored.
+int autotune(hodlr3d_t h, int reps, std::string& report) {
+  std::memset(h->tuned, 0, sizeof h->tuned);
+  report.clear();
+  if (reps == 0) return HODLR3D_OK;
+  if (!h->assembled) return set_error(HODLR3D_ERR_NOT_ASSEMBLED, "hodlr3d_assemble has not run");
+  if (!h->opt.keep_fp32) return set_error(HODLR3D_ERR_INVALID_ARG, "the mixed form needs keep_fp32");
+  const int64_t N = h->N;
+  const size_t bytes = sizeof(double) * N * 64;
+  DevBuf X, Y;
+  H3D_CUDA(X.ensure(bytes));
+  H3D_CUDA(Y.ensure(bytes));
+  cudaStream_t s = h->stream;
+  H3D_CUDA(cudaMemsetAsync(X.p, 0x3F, bytes, s));
+  EventPair ev;
+  H3D_CUDA(cudaEventCreate(&ev.a));
+  H3D_CUDA(cudaEventCreate(&ev.b));
+  const int forced = h->engine;
+  int8_t choice[2][kNumTuneCounts] = {};
+  char line[160];
+  report = "transpose nrhs engine ms\n";
+  int st = HODLR3D_OK;
+  for (int tr = 0; tr < 2 && st == HODLR3D_OK; ++tr) {
+    for (int ci = 0; ci < kNumTuneCounts && st == HODLR3D_OK; ++ci) {
+      const int nrhs = kTuneCounts[ci];
+      float best = 0.f;
+      for (int eng = 1; eng <= 3; ++eng) {
+        if (tr && eng == 2) continue;  // no tensor-core transpose
+        h->engine = eng;
+        // untimed product: builds the engine's tables and buffers
+        st = matvec_device(h, X.as<double>(), Y.as<double>(), nrhs, N, HODLR3D_MIXED, s, tr != 0);
+        if (st == HODLR3D_ERR_UNSUPPORTED) {  // this tree does not suit the engine
+          st = HODLR3D_OK;
+          continue;
+        }
+        if (st != HODLR3D_OK) break;
+        std::vector<float> ms(reps);
+        for (int r = 0; r < reps && st == HODLR3D_OK; ++r) {
+          cudaError_t e = cudaEventRecord(ev.a, s);
+          if (e == cudaSuccess) {
+            st = matvec_device(h, X.as<double>(), Y.as<double>(), nrhs, N, HODLR3D_MIXED, s, tr != 0);
+            e = cudaEventRecord(ev.b, s);
+          }
+          if (e == cudaSuccess) e = cudaEventSynchronize(ev.b);
+          if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[r], ev.a, ev.b);
+          if (e != cudaSuccess && st == HODLR3D_OK)
+            st = set_error(HODLR3D_ERR_CUDA, "autotune timing: %s", cudaGetErrorString(e));
+        }
+        if (st != HODLR3D_OK) break;
+        std::sort(ms.begin(), ms.end());
+        const float med = ms[reps / 2];
+        std::snprintf(line, sizeof line, "%d %d %d %.6f\n", tr, nrhs, eng, med);
+        report += line;
+        if (choice[tr][ci] == 0 || med < best) {
+          choice[tr][ci] = (int8_t)eng;
+          best = med;
+        }
+      }
+    }
+  }
+  h->engine = forced;
+  if (st != HODLR3D_OK) return st;
+  for (int tr = 0; tr < 2; ++tr) {
+    int ci = 0;
+    for (int n = 1; n <= 64; ++n) {
+      while (kTuneCounts[ci] < n) ++ci;
+      h->tuned[tr][n] = choice[tr][ci];
+    }
+  }
   return HODLR3D_OK;
 }
 
@@ -2240,6 +2342,30 @@ int64_t hodlr3d_launch_count(hodlr3d_t h) { return h ? h->launches : 0; }
 int hodlr3d_set_engine(hodlr3d_t h, int engine) try {
   if (!h || engine < 0 || engine > 3) return set_error(HODLR3D_ERR_INVALID_ARG, "engine must be 0, 1, 2 or 3");
   h->engine = engine;
+  return HODLR3D_OK;
+} catch (...) {
+  return exception_status();
+}
+
+int hodlr3d_autotune(hodlr3d_t h, int reps, char* report, int cap) try {
+  H3D_TRY(check_handle(h));
+  if (reps < 0 || reps > 1000) return set_error(HODLR3D_ERR_INVALID_ARG, "reps must be in 0..1000");
+  std::string rep;
+  H3D_TRY(autotune(h, reps, rep));
+  if (report && cap > 0) {
+    const size_t n = std::min(rep.size(), (size_t)cap - 1);
+    std::memcpy(report, rep.data(), n);
+    report[n] = 0;
+  }
+  return HODLR3D_OK;
+} catch (...) {
+  return exception_status();
+}
+
+int hodlr3d_get_tuning(hodlr3d_t h, int32_t* choice) try {
+  if (!h || !choice) return set_error(HODLR3D_ERR_INVALID_ARG, "null argument");
+  for (int t = 0; t < 2; ++t)
+    for (int n = 1; n <= 64; ++n) choice[64 * t + n - 1] = h->tuned[t][n];
   return HODLR3D_OK;
 } catch (...) {
   return exception_status();

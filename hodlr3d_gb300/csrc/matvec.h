@@ -119,8 +119,8 @@ struct TcBuffers {
   const void* nmaps;
 };
 
-// Tensor-core mixed-precision product A X for 17..32 right-hand sides (padded
-// to 32); leaves of at most 128 points whose populations are multiples of 4
+// Tensor-core mixed-precision product A X for 1..32 right-hand sides (zero
+// padded to 32); leaves of at most 128 points whose populations are multiples of 4
 // (16-byte aligned operand rows).  Returns the number of launches.
 int launch_matvec_tc(cudaStream_t s, int64_t N, const int32_t* perm, const FarOp& far,
                      const NearOp& near, const TcBuffers& B, const double* X, int64_t ldx,

@@ -1,5 +1,5 @@
 // Tensor-core (tcgen05, kind::tf32, 3xTF32) engine of the mixed-precision
-// matvec for 17..32 right-hand sides (padded to 32).  Same operator and same
+// matvec for up to 32 right-hand sides (zero padded to 32).  Same operator and same
 // owner writes as the CUDA-core engine in matvec.cu; the products run on the
 // 5th-generation tensor cores with FP32 accumulators in TMEM.
 //

@@ -245,6 +245,31 @@ class HODLR3D:
         mixed A x) or 'gemv' (few-column FP32 kernels, mixed A x and A^T x)."""
         check(self._L.hodlr3d_set_engine(self.handle, {"auto": 0, "simt": 1, "tc": 2, "gemv": 3}[engine]))
 
+    ENGINES = ("auto", "simt", "tc", "gemv")
+
+    def autotune(self, reps: int = 3) -> list:
+        """Times every engine that runs the mixed product of this operator at
+        1, 2, 4, 8, 16, 32 and 64 right-hand sides (A x and A^T x) and makes
+        the automatic choice follow the fastest; reps=0 returns to the
+        column-count rules.  Returns the timings as (transpose, nrhs, engine,
+        ms) tuples."""
+        buf = ctypes.create_string_buffer(1 << 14)
+        check(self._L.hodlr3d_autotune(self.handle, int(reps), buf, len(buf)))
+        rows = []
+        for line in buf.value.decode().splitlines()[1:]:
+            t, n, e, ms = line.split()
+            rows.append((bool(int(t)), int(n), self.ENGINES[int(e)], float(ms)))
+        return rows
+
+    def tuning(self) -> dict:
+        """The automatic engine per column count after autotune():
+        {"forward": [...], "transpose": [...]} over nrhs = 1..64, None where the
+        column-count rules apply."""
+        c = np.zeros(128, np.int32)
+        check(self._L.hodlr3d_get_tuning(self.handle, c.ctypes.data))
+        names = [None if v == 0 else self.ENGINES[v] for v in c]
+        return {"forward": names[:64], "transpose": names[64:]}
+
     def device_status(self) -> None:
         """Raises if a bounded device wait gave up in an earlier call."""
         check(self._L.hodlr3d_device_status(self.handle))

@@ -5,12 +5,13 @@
 // signatures; the vector type is a template parameter so Eigen::VectorXd (or
 // std::vector<double>) works unchanged: it needs data(), size() and resize().
 // The kernel is chosen by Qchoice (src/kernel.cpp:65-227) instead of a
-// user-compiled getMatrixEntry; kernels 0-10, 13, 15 and 16 run on the GPU.
+// user-compiled getMatrixEntry; every Qchoice 0-16 runs on the GPU.
 // Errors are thrown as hodlr3d_gb300::Error (the reference has no error path).
 #ifndef HODLR3D_GB300_FACADE_HPP
 #define HODLR3D_GB300_FACADE_HPP
 
 #include <cmath>
+#include <cstring>
 #include <stdexcept>
 #include <memory>
 #include <string>
@@ -92,6 +93,16 @@ class HODLR3D {
     hodlr3d_t h = nullptr;
     hodlr3d_gb300::check(hodlr3d_load(path.c_str(), nullptr, &h));
     return std::unique_ptr<HODLR3D>(new HODLR3D(h));
+  }
+
+  // Engine autotuning for this operator (no reference counterpart): the
+  // automatic choice of the mixed form follows the timings; reps = 0 returns
+  // to the column-count rules.  Returns the timing table as text.
+  std::string autotune(int reps = 3) {
+    std::string report(1 << 14, '\0');
+    hodlr3d_gb300::check(hodlr3d_autotune(tree.h, reps, &report[0], (int)report.size()));
+    report.resize(std::strlen(report.c_str()));
+    return report;
   }
 
   // Ab = A b (host vectors); Ab is resized like the reference's (src/HODLR3DTree.cpp:1782).

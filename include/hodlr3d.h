@@ -209,8 +209,24 @@ int64_t hodlr3d_launch_count(hodlr3d_t h);
  * more; HODLR3D_FP64X: the few-column kernels; otherwise CUDA-core kernels),
  * 1 = CUDA-core kernels only (HODLR3D_FP64X becomes HODLR3D_FP64), 2 = tensor
  * cores only, 3 = few-column kernels only (HODLR3D_ERR_UNSUPPORTED where the
- * chosen engine does not apply). */
+ * chosen engine does not apply).  After hodlr3d_autotune the automatic
+ * choice of the mixed form follows its timings instead of these rules. */
 int hodlr3d_set_engine(hodlr3d_t h, int engine);
+/* Autotuner of the automatic engine choice over this operator's own rank
+ * histogram: times every engine that runs the mixed-precision product (A x:
+ * CUDA cores, tensor cores, few-column kernels; A^T x: CUDA cores and
+ * few-column kernels) at 1, 2, 4, 8, 16, 32 and 64 right-hand sides, `reps`
+ * timed products each after an untimed one (median), and makes engine 0 use
+ * the fastest; a count between two timed ones takes the choice of the next
+ * one up.  Blocks the calling thread; allocates two n x 64 work arrays for
+ * its duration.  reps = 0 returns to the column-count rules; a new assembly
+ * or load does too.  report (optional, cap bytes, NUL-terminated, truncated):
+ * one line "transpose nrhs engine ms" per timing.  No reference counterpart. */
+int hodlr3d_autotune(hodlr3d_t h, int reps, char* report, int cap);
+/* The automatic choice after hodlr3d_autotune: choice[64 t + nrhs - 1] for
+ * t = 0 (A x) and 1 (A^T x), nrhs 1..64; an engine number, or 0 where the
+ * column-count rules apply. */
+int hodlr3d_get_tuning(hodlr3d_t h, int32_t* choice);
 /* Synchronises the device and reports HODLR3D_ERR_CUDA if a bounded
  * tensor-core wait gave up in an earlier call on this handle. */
 int hodlr3d_device_status(hodlr3d_t h);

@@ -2,6 +2,7 @@
 // written against the hodlr3d_gb300 C++ facade: a uniform grid, the matvec
 // checked against the dense sum of columns, and the GMRES solve of
 // b = K x_true.  Exit status 0 when both meet their tolerances.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <vector>
@@ -92,8 +93,18 @@ int main(int argc, char** argv) {
   }
   std::remove(path.c_str());
   printf("loaded_same=%d fp64x_rel_diff=%.3e\n", (int)same, std::sqrt(dx / dn));
+  // engine autotuning: the mixed product under the tuned automatic choice
+  const std::string table = G2->autotune(1);
+  G2->precision = HODLR3D_MIXED;
+  std::vector<double> Hbm;
+  G2->MatVecProduct(b, Hbm);
+  double dm = 0.0;
+  for (int t = 0; t < N; ++t) dm += (Hbm[t] - Hb[t]) * (Hbm[t] - Hb[t]);
+  const bool tuned = table.find("transpose nrhs engine ms") == 0 && std::sqrt(dm / dn) < 2e-6;
+  printf("autotune_lines=%d mixed_rel_diff=%.3e\n", (int)std::count(table.begin(), table.end(), '\n'),
+         std::sqrt(dm / dn));
   const bool ok = err < 1e-8 && gerr <= 1e-10 && std::sqrt(fe / fn) < 1e-8 && same &&
-                  std::sqrt(dx / dn) < 1e-12;
+                  std::sqrt(dx / dn) < 1e-12 && tuned;
   delete H;
   return ok ? 0 : 1;
 }
