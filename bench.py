@@ -212,16 +212,13 @@ def measured_traffic(kernel, args):
     return e["bytes_per_launch"]
 
 
-def level_bytes(H, nr_pad, s):
-    """Algorithmic bytes per launch of each matvec kernel, both engines: the
-    factor entries it streams (s bytes each), plus its right-hand-side,
-    intermediate (T, slice partials) and output traffic counted once; the
-    tensor-core leaf kernel also streams the FP32 near-field blocks."""
+def pair_sizes(H):
+    """Per compressed pair (level, target box, source box): its rank and the
+    populations n of the target box and m of the source box."""
     P = H.pairs()
     R = H.ranks().astype(np.int64)
     off = H.leaf_offsets()
     d = int(P[:, 0].max()) if len(P) else 0
-    N = H.N
 
     def sizes(level, boxes):
         sh = 3 * (d - level)
@@ -233,6 +230,36 @@ def level_bytes(H, nr_pad, s):
         sel = P[:, 0] == j
         n[sel] = sizes(j, P[sel, 1].astype(np.int64))
         m[sel] = sizes(j, P[sel, 2].astype(np.int64))
+    return P, R, n, m, d, off
+
+
+# FP64 arithmetic rate for the assembly's fraction: GB300's nominal dense FP64
+ASSEMBLY_PEAK_GFLOPS = 1250.0
+
+
+def aca_work(H):
+    """Work of the partially pivoted ACA (src/ACA.cpp:127-238) at the ranks it
+    produced.  Iteration k of a pair evaluates one residual row (m kernel
+    entries) and one residual column (n), subtracts the k earlier terms from
+    each (k (n + m) FMAs) and updates the norm estimate with k cross terms
+    (k (n + m) FMAs); one more row and column end the loop.  Evaluations
+    E = sum (r + 1)(n + m); FP64 flops = 9 E (an entry: 3 subtractions, 3 for
+    r^2, square root and division counted as 1, the scale, the diagonal
+    select) + sum 2 r (r - 1)(n + m)."""
+    _, R, n, m, _, _ = pair_sizes(H)
+    nm = n + m
+    evals = int(((R + 1) * nm).sum())
+    flops = 9 * evals + int((2 * R * (R - 1) * nm).sum())
+    return evals, flops
+
+
+def level_bytes(H, nr_pad, s):
+    """Algorithmic bytes per launch of each matvec kernel, both engines: the
+    factor entries it streams (s bytes each), plus its right-hand-side,
+    intermediate (T, slice partials) and output traffic counted once; the
+    tensor-core leaf kernel also streams the FP32 near-field blocks."""
+    P, R, n, m, d, off = pair_sizes(H)
+    N = H.N
     leaf = P[:, 0] == d
     up = ~leaf
     above = P[:, 0] < d - 1
@@ -294,6 +321,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     t_setup = time.perf_counter() - t
     st = H.stats()
+    aca_evals, aca_flops = aca_work(H)
     nrhs = args.nrhs
     X = torch.tensor(charges_normal(N, nrhs, seed=11), device=dev).reshape(N, nrhs)
     x1 = X[:, 0].contiguous()
@@ -500,7 +528,14 @@ def run_ours(args):
             "assembly": {"seconds": st["assemble_seconds"], "tree_seconds": st["tree_seconds"],
                          "pairs": st["n_pairs"], "max_rank": st["max_rank"],
                          "factor_bytes_fp32": st["factor_bytes_fp32"],
-                         "factor_bytes_fp64": st["factor_bytes_fp64"]},
+                         "factor_bytes_fp64": st["factor_bytes_fp64"],
+                         "roofline": {"bound": "fp64", "entry_evaluations": aca_evals,
+                                      "flops": aca_flops,
+                                      "achieved": aca_flops / st["assemble_seconds"] / 1e9,
+                                      "peak": ASSEMBLY_PEAK_GFLOPS, "unit": "GFLOP/s",
+                                      "peak_kind": "nominal",
+                                      "frac": aca_flops / st["assemble_seconds"] / 1e9
+                                      / ASSEMBLY_PEAK_GFLOPS}},
         }
         print(json.dumps(line), flush=True)
     H.close()
