@@ -529,6 +529,9 @@ def run_ours(args):
                          "pairs": st["n_pairs"], "max_rank": st["max_rank"],
                          "factor_bytes_fp32": st["factor_bytes_fp32"],
                          "factor_bytes_fp64": st["factor_bytes_fp64"],
+                         "aca_batches": st["aca_batches"],
+                         "aca_kernel_seconds": st["aca_kernel_seconds"],
+                         "finish_seconds": st["finish_seconds"],
                          "roofline": {"bound": "fp64", "entry_evaluations": aca_evals,
                                       "flops": aca_flops,
                                       "achieved": aca_flops / st["assemble_seconds"] / 1e9,

@@ -43,7 +43,8 @@ class Stats(ctypes.Structure):
                 ("v_entries", ctypes.c_int64), ("factor_bytes_fp64", ctypes.c_int64),
                 ("factor_bytes_fp32", ctypes.c_int64), ("near_entries", ctypes.c_int64),
                 ("tree_seconds", ctypes.c_double), ("assemble_seconds", ctypes.c_double),
-                ("aca_batches", ctypes.c_int)]
+                ("aca_batches", ctypes.c_int), ("aca_kernel_seconds", ctypes.c_double),
+                ("finish_seconds", ctypes.c_double)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

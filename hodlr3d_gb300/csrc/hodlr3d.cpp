@@ -161,6 +161,15 @@ struct DevBuf {
   }
 };
 
+// two CUDA events for a timed span, destroyed with the scope
+struct EventPair {
+  cudaEvent_t a = nullptr, b = nullptr;
+  ~EventPair() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+};
+
 }  // namespace
 
 struct hodlr3d_handle {
@@ -225,6 +234,8 @@ struct hodlr3d_handle {
   int max_rank = 0;
   double assemble_seconds = 0.0;
   int aca_batches = 0;
+  double aca_kernel_seconds = 0.0;  // device time of the ACA kernels of the last assembly
+  double finish_seconds = 0.0;      // finish_assembly of the last assembly or load
   // matvec work buffers
   DevBuf xsorted, tbuf, pbuf, ynl, stage_x, stage_y, stage_t;
   int mv_nrhs_cap = 0;
@@ -613,10 +624,15 @@ int run_aca_batch(hodlr3d_t h, std::vector<HostTask>& batch, std::vector<HostTas
   }
   const int grid = std::max(1, std::min(nt, h->num_sms * per_sm));
   h3d::PointsF64 P{h->xs.as<double>(), h->ys.as<double>(), h->zs.as<double>()};
+  EventPair ev;
+  H3D_CUDA(cudaEventCreate(&ev.a));
+  H3D_CUDA(cudaEventCreate(&ev.b));
+  H3D_CUDA(cudaEventRecord(ev.a, s));
   H3D_CUDA(h3d::launch_aca(s, block, grid, d_tasks.as<h3d::AcaTask>(), nt, d_counter.as<int>(), P,
                            h->kd, h->tol, d_ws.as<double>(), d_fl.as<unsigned char>(),
                            d_pv.as<int32_t>(), d_rank.as<int32_t>(), d_status.as<int32_t>(),
                            cap_max));
+  H3D_CUDA(cudaEventRecord(ev.b, s));
   ++h->launches;
   std::vector<int32_t> rk(nt), st(nt), pvh(pv);
   H3D_CUDA(cudaMemcpyAsync(rk.data(), d_rank.p, sizeof(int32_t) * nt, cudaMemcpyDeviceToHost, s));
@@ -624,6 +640,9 @@ int run_aca_batch(hodlr3d_t h, std::vector<HostTask>& batch, std::vector<HostTas
   if (pv) H3D_CUDA(cudaMemcpyAsync(pvh.data(), d_pv.p, sizeof(int32_t) * pv, cudaMemcpyDeviceToHost, s));
   H3D_CUDA(cudaStreamSynchronize(s));
   H3D_CUDA(cudaGetLastError());
+  float aca_ms = 0.f;
+  H3D_CUDA(cudaEventElapsedTime(&aca_ms, ev.a, ev.b));
+  h->aca_kernel_seconds += 1e-3 * aca_ms;
   // finished tasks -> exact-size pools; capacity overflows -> retried with twice the capacity
   std::vector<int64_t> dst(nt, 0);
   int64_t total = 0;
@@ -690,6 +709,7 @@ int assemble(hodlr3d_t h) {
   h->v32_pool = nullptr;
   h->u32_pool = nullptr;
   h->aca_batches = 0;
+  h->aca_kernel_seconds = 0.0;
   const int cap0 = h->opt.rank_cap > 0 ? h->opt.rank_cap : 256;
   std::vector<HostTask> todo;
   todo.reserve(np);
@@ -742,6 +762,7 @@ int assemble(hodlr3d_t h) {
 // Everything after the factors exist (assembly or hodlr3d_load): the FP32
 // copies, the matvec's per-pair tables and their device copies.
 int finish_assembly(hodlr3d_t h, double t_start) {
+  const double t_finish = now_s();
   const int64_t np = h->npairs;
   std::memset(h->tuned, 0, sizeof h->tuned);  // timings of another operator
   if (h->opt.keep_fp32) H3D_TRY(group_fp32(h));
@@ -845,6 +866,7 @@ int finish_assembly(hodlr3d_t h, double t_start) {
   h->maps_built = false;
   h->gemv_built = false;
   h->assembled = true;
+  h->finish_seconds = now_s() - t_finish;
   h->assemble_seconds = now_s() - t_start;
   return HODLR3D_OK;
 }
@@ -1079,6 +1101,7 @@ int load_factors(const char* path, const hodlr3d_options* opt, hodlr3d_t* out) {
     h->h_v64[p] = base + r * (a1 - a0);
   }
   h->aca_batches = 0;
+  h->aca_kernel_seconds = 0.0;
   H3D_TRY(finish_assembly(h, t_start));
   *out = guard.release();
   return HODLR3D_OK;
@@ -1641,14 +1664,6 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
 // few-column kernels run passes of 4 or 8).
 constexpr int kTuneCounts[] = {1, 2, 4, 8, 16, 32, 64};
 constexpr int kNumTuneCounts = sizeof(kTuneCounts) / sizeof(kTuneCounts[0]);
-
-struct EventPair {
-  cudaEvent_t a = nullptr, b = nullptr;
-  ~EventPair() {
-    if (a) cudaEventDestroy(a);
-    if (b) cudaEventDestroy(b);
-  }
-};
 
 // Times every engine that runs the mixed product of this operator (A x: CUDA
 // cores, tensor cores, few-column kernels; A^T x: CUDA cores, few-column) at
@@ -2220,6 +2235,8 @@ int hodlr3d_get_stats(hodlr3d_t h, hodlr3d_stats* s) try {
   s->tree_seconds = h->tree_seconds;
   s->assemble_seconds = h->assemble_seconds;
   s->aca_batches = h->aca_batches;
+  s->aca_kernel_seconds = h->aca_kernel_seconds;
+  s->finish_seconds = h->finish_seconds;
   // near blocks and the reference's memory count (findMemory, src/HODLR3DTree.cpp:1757-1778)
   const int d = h->levels;
   double mem = 0.0;

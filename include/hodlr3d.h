@@ -18,7 +18,7 @@
 extern "C" {
 #endif
 
-#define HODLR3D_ABI_VERSION 1
+#define HODLR3D_ABI_VERSION 2
 
 typedef struct hodlr3d_handle* hodlr3d_t;
 
@@ -74,6 +74,9 @@ typedef struct hodlr3d_stats {
   double tree_seconds;      /* last hodlr3d_create, device tree + lists */
   double assemble_seconds;  /* last hodlr3d_assemble */
   int aca_batches;          /* assembly batches of the last hodlr3d_assemble */
+  double aca_kernel_seconds; /* device time of its ACA kernels (CUDA events) */
+  double finish_seconds;    /* FP32 grouping and matvec tables of the last
+                               hodlr3d_assemble or hodlr3d_load */
 } hodlr3d_stats;
 
 typedef struct hodlr3d_gmres_params {
