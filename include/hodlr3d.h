@@ -53,8 +53,10 @@ typedef struct hodlr3d_options {
   int device;                 /* CUDA device ordinal (0) */
   double diag_override;       /* NaN: the reference diagonal (Kii for kernel 16, else 0) */
   int keep_fp32;              /* also keep FP32 copies of the factors for HODLR3D_MIXED (1) */
-  size_t aca_workspace_bytes; /* device workspace for one assembly batch (0: 8 GiB) */
-  int rank_cap;               /* first per-pair rank capacity above leaf size (0: 256) */
+  size_t aca_workspace_bytes; /* device workspace for one assembly batch (0: 32 GiB or a
+                                 quarter of the free device memory, whichever is less) */
+  int rank_cap;               /* first per-pair rank capacity above leaf size (0: 128); a pair
+                                 that reaches it runs again with twice the capacity */
 } hodlr3d_options;
 
 typedef struct hodlr3d_stats {
