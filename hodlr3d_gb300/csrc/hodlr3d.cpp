@@ -712,9 +712,9 @@ int assemble(hodlr3d_t h) {
   h->aca_kernel_seconds = 0.0;
   // first rank capacity above leaf size: pairs that reach it run again with
   // twice the capacity (same ranks and pivots).  128 and the workspace below:
-  // at 64^3 (1/r, tol 1e-10) 4 batches and 6.8 s against 20 and 8.9 s with
-  // 256 and 8 GiB (each batch waits for its slowest pair); 96 costs more in
-  // repeated pairs than it saves.
+  // at 64^3 (1/r, tol 1e-10) 4 batches and 6.7-7.7 s against 20 and
+  // 8.9-11.1 s with 256 and 8 GiB in the same process (each batch waits for
+  // its slowest pair); 96 costs more in repeated pairs than it saves.
   const int cap0 = h->opt.rank_cap > 0 ? h->opt.rank_cap : 128;
   std::vector<HostTask> todo;
   todo.reserve(np);
