@@ -253,11 +253,28 @@ def aca_work(H):
     return evals, flops
 
 
-def level_bytes(H, nr_pad, s):
-    """Algorithmic bytes per launch of each matvec kernel, both engines: the
+# few-column engine chunking (hodlr3d_gb300/csrc/matvec.h): V-stack columns
+# per forward work item, U rows per transposed work item
+GEMV_COLS = 1024
+GEMV_ROWS_T = 256
+
+
+def engine_of(kernels) -> str:
+    """The matvec engine whose kernels a profile report names."""
+    if "leaf_tc" in kernels:
+        return "tc"
+    if "uy" in kernels or "vy" in kernels:
+        return "gemv"
+    return "simt"
+
+
+def level_bytes(H, nr_pad, s, engine):
+    """Algorithmic bytes per launch of each kernel of one matvec engine
+    ("simt", "tc" or "gemv"), keyed by the names its profiler spans carry: the
     factor entries it streams (s bytes each), plus its right-hand-side,
-    intermediate (T, slice partials) and output traffic counted once; the
-    tensor-core leaf kernel also streams the FP32 near-field blocks."""
+    intermediate (T, slice or chunk partials) and output traffic counted once;
+    the tensor-core leaf kernel and the few-column output kernels also stream
+    the FP32 near-field blocks."""
     P, R, n, m, d, off = pair_sizes(H)
     N = H.N
     leaf = P[:, 0] == d
@@ -272,8 +289,16 @@ def level_bytes(H, nr_pad, s):
     u_leaf, v_leaf = int((R[leaf] * n[leaf]).sum()) * s, int((R[leaf] * m[leaf]).sum()) * s
     ynl = N * nr_pad * 8
     y = N * min(nr_pad, 64) * 8
-    # FP32 near-field blocks of the tensor-core engine: every leaf with itself
-    # and its face / edge neighbours (vertex neighbours are compressed pairs)
+    gather = y + xb
+    if engine == "simt":
+        return {"gather": gather,
+                "vtx": v_up + xb + t_up + parts,
+                "tred": parts + t_up,
+                "ut": u_up + t_up + ynl,
+                "leaf": u_leaf + v_leaf + xb + ynl + y}
+    # FP32 near-field blocks (tensor-core and few-column engines): every leaf
+    # with itself and its face / edge neighbours (vertex neighbours are
+    # compressed pairs)
     nl = len(off) - 1
     cnt = np.diff(off)
     cnt4 = (cnt + 3) // 4 * 4
@@ -282,26 +307,28 @@ def level_bytes(H, nr_pad, s):
                        for dx in (-1, 0, 1) if (dx, dy, dz) != (0, 0, 0)])
     nbn = np.where((nb >= 0) & ~vertex[None, :], cnt4[np.maximum(nb, 0)], 0).sum(axis=1)
     near = int((cnt * (cnt4 + nbn)).sum()) * 4
-    b = {
-        "gather": y + xb,
-        # CUDA-core engine
-        "vtx": v_up + xb + t_up + parts,
-        "tred": parts + t_up,
-        "ut": u_up + t_up + ynl,
-        "leaf": u_leaf + v_leaf + xb + ynl + y,
-        # tensor-core engine
-        "ta_slice": v_up + xb + t_up + parts,
-        "ta_leaf": v_leaf + xb + t_leaf,
-        "ut_tc": u_up + t_up + ynl,
-        "leaf_tc": u_leaf + near + t_leaf + xb + ynl + y,
-        # few-column engine (A x, then A^T x)
-        "vt": v_up + v_leaf + xb + t_up + t_leaf,
-        "uy": u_up + u_leaf + near + t_up + t_leaf + xb + y,
-        "ut": u_up + u_leaf + xb + t_up + t_leaf,
-        "tred_t": t_up,
-        "vy": v_up + v_leaf + near + t_up + t_leaf + xb + y,
-    }
-    return b
+    if engine == "tc":
+        return {"gather": gather,
+                "ta_slice": v_up + xb + t_up + parts,
+                "tred": parts + t_up,
+                "ta_leaf": v_leaf + xb + t_leaf,
+                "ut_tc": u_up + t_up + ynl,
+                "leaf_tc": u_leaf + near + t_leaf + xb + ynl + y}
+    # few-column engine: chunk partials of the V stacks wider than GEMV_COLS
+    # (forward) and of the U blocks taller than GEMV_ROWS_T (transpose), each
+    # read once and reduced into the pair's rows of T
+    nch = -(-((m + 3) // 4 * 4) // GEMV_COLS)
+    ncht = -(-n // GEMV_ROWS_T)
+    r4 = (R + 3) // 4 * 4
+    tred = int((R * (nch + 1))[nch > 1].sum()) * nr_pad * s
+    tred_t = int((r4 * ncht + R)[ncht > 1].sum()) * nr_pad * s
+    return {"gather": gather,
+            "vt": v_up + v_leaf + xb + t_up + t_leaf,
+            "tred": tred,
+            "uy": u_up + u_leaf + near + t_up + t_leaf + xb + y,
+            "ut": u_up + u_leaf + xb + t_up + t_leaf,
+            "tred_t": tred_t,
+            "vy": v_up + v_leaf + near + t_up + t_leaf + xb + y}
 
 
 def run_ours(args):
@@ -378,7 +405,7 @@ def run_ours(args):
     H.set_profiling(False)
     kern_ms = {k: v[1] / v[0] for k, v in rep.items()}
     nr_pad = 1 << (nrhs - 1).bit_length()
-    alg = level_bytes(H, nr_pad, 4)
+    alg = level_bytes(H, nr_pad, 4, engine_of(kern_ms))
     top = max(kern_ms, key=kern_ms.get)
     hbm, peak_kind = peaks()
     achieved = alg[top] / (kern_ms[top] * 1e-3) / 1e9
@@ -403,7 +430,7 @@ def run_ours(args):
     for name, tr in (("forward", False), ("transpose", True)):
         ms1 = timed(lambda: H.matvec(x1, "mixed", transpose=tr), max(3, args.steps // 2), 3)
         k1 = kernel_split(lambda: H.matvec(x1, "mixed", transpose=tr))
-        a1 = level_bytes(H, 1, 4)
+        a1 = level_bytes(H, 1, 4, engine_of(k1))
         t1 = max(k1, key=k1.get)
         ach = a1[t1] / (k1[t1] * 1e-3) / 1e9
         one[name] = {"ms": ms1, "rhs_per_s": 1e3 / ms1, "kernel_ms": k1,
@@ -419,7 +446,8 @@ def run_ours(args):
     kx = kernel_split(lambda: H.matvec(x1, "fp64x"))
     y64, yx = H.matvec(x1, "fp64"), H.matvec(x1, "fp64x")
     fp64x = {"ms": msx, "rhs_per_s": 1e3 / msx, "kernel_ms": kx,
-             "whole_GBps": 2 * sum(level_bytes(H, 1, 4)[k] for k in kx) / (msx * 1e-3) / 1e9,
+             "whole_GBps": 2 * sum(level_bytes(H, 1, 4, engine_of(kx))[k] for k in kx)
+             / (msx * 1e-3) / 1e9,
              "rel_diff_vs_fp64": float((torch.linalg.norm(yx - y64) / torch.linalg.norm(y64)).item()),
              "speedup_vs_fp64_1rhs": ms64 / msx}
 
