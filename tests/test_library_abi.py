@@ -76,7 +76,7 @@ def test_no_device_or_tree_error_is_reported():
 
 def _factor_header(version=1, n=64, npairs=0, npools=0):
     import struct
-    # FileHeader (hodlr3d.cpp): version, header bytes, n, nP1D, tol_pow, L, kernel, levels,
+    # FileHeader (hodlr3d_gb300/csrc/factors.cpp): version, header bytes, n, nP1D, tol_pow, L, kernel, levels,
     # diag, npairs, npools, reserved, lists hash
     return b"H3DFACT1" + struct.pack("<IIqiidiidqiiQ", version, 72, n, 4, 10, 1.0, 16, 1, 0.5,
                                      npairs, npools, 0, 0x1234)
