@@ -3,7 +3,8 @@
 * ``matvec(H, x)``: y = A x; its backward is the hand-written transpose
   product A^T g (V (U^T g) on the compressed pairs, transposed near field).
 * ``solve(H, b)``: x = A^{-1} b by GMRES; its backward is the adjoint solve
-  A^T lambda = g, and grad_b = lambda.
+  A^T lambda = g, and grad_b = lambda (``transpose=True`` solves A^T x = b,
+  whose backward solves with A).
 
 Both take CUDA float64 tensors of shape (N,) or (N, nrhs).
 """
@@ -35,7 +36,10 @@ class _Solve(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, g):
-        lam, _ = ctx.H.gmres(g.contiguous(), transpose=True, **ctx.opts)
+        # the adjoint of a solve with A is a solve with A^T, and conversely
+        opts = dict(ctx.opts)
+        opts["transpose"] = not opts.get("transpose", False)
+        lam, _ = ctx.H.gmres(g.contiguous(), **opts)
         return lam, None, None
 
 

@@ -81,6 +81,20 @@ def test_solve_backward_is_the_adjoint_solve(op, precision, stol, tol):
     assert rel <= 10 * stol, rel
 
 
+def test_transposed_solve_backward_solves_with_a(op):
+    """solve(..., transpose=True) gives x = A^-T b; its gradient solves A lambda = w."""
+    from hodlr3d_gb300 import autograd
+    H = op
+    b = rand(H, 1, 13).requires_grad_(True)
+    w = rand(H, 1, 14)
+    x = autograd.solve(H, b, tol=1e-12, transpose=True)
+    res = H.matvec(x.detach(), "fp64", transpose=True) - b.detach()
+    assert torch.linalg.norm(res) <= 1e-10 * torch.linalg.norm(b.detach())
+    (x * w).sum().backward()
+    res = H.matvec(b.grad, "fp64") - w
+    assert torch.linalg.norm(res) <= 1e-10 * torch.linalg.norm(w)
+
+
 def test_solve_central_difference(op):
     """d/de <w, A^-1 (b + e c)> at e = 0 by central differences (exact for a
     linear map up to the solver tolerance) against <grad_b, c>."""
