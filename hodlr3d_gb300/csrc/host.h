@@ -105,6 +105,9 @@ struct EventPair {
   } while (0)
 
 
+// the handle (include/hodlr3d.h's opaque hodlr3d_t) owns its device buffers
+using hodlr3d_host::DevBuf;
+
 struct hodlr3d_handle {
   // problem
   int64_t N = 0;
@@ -122,7 +125,7 @@ struct hodlr3d_handle {
   cudaStream_t stream = nullptr;
   int64_t launches = 0;
   // tree (device)
-  hodlr3d_host::DevBuf xyz, perm, leaf_off, xs, ys, zs, xl, yl, zl, centre, nbr_all, nbr_leaf, il_ptr, pair_tgt,
+  DevBuf xyz, perm, leaf_off, xs, ys, zs, xl, yl, zl, centre, nbr_all, nbr_leaf, il_ptr, pair_tgt,
       pair_src, rev;
   std::vector<int32_t> h_perm, h_leaf_off, h_pair_tgt, h_pair_src, h_pair_level;
   std::vector<int64_t> h_il_ptr;
@@ -133,7 +136,7 @@ struct hodlr3d_handle {
   bool assembled = false;
   std::vector<int32_t> h_rank;
   std::vector<std::vector<int32_t>> h_piv_rows, h_piv_cols;  // local pivots per pair
-  std::vector<hodlr3d_host::DevBuf*> pools;
+  std::vector<DevBuf*> pools;
   std::vector<int64_t> h_fac_off;       // per pair: element offset of its FP64 U in its pool (V follows)
   std::vector<int32_t> h_fac_pool;      // per pair: index of its FP64 pool in `pools` (-1: rank 0 or none)
   std::vector<double*> h_u64, h_v64;
@@ -141,7 +144,7 @@ struct hodlr3d_handle {
   // FP32 V of the pairs of each source box, contiguous in the order of its
   // reverse list: per box (all levels numbered together) the float offset in
   // v32_pool of its first pair and its rows (the sum of the ranks)
-  hodlr3d_host::DevBuf* v32_pool = nullptr;
+  DevBuf* v32_pool = nullptr;
   std::vector<int64_t> h_vbox_off;
   std::vector<int32_t> h_vbox_rows;
   // FP32 U of the pairs of each target box side by side: one row-major
@@ -149,17 +152,17 @@ struct hodlr3d_handle {
   // u32_pool + h_ubox_off[b]; pair p at column h_coff[p], row stride
   // h_ustride[p] = R_b.  The tensor-core T uses the same grouping: T of box b
   // is 32 x R_b at 32-wide offset h_tbox_off[b].
-  hodlr3d_host::DevBuf* u32_pool = nullptr;
+  DevBuf* u32_pool = nullptr;
   // FP64-accurate form: lo parts of the FP32 copies (FP64 value minus the
   // FP32 value, rounded), same layouts; built on first use
-  hodlr3d_host::DevBuf u32lo_pool, v32lo_pool, knearlo;
+  DevBuf u32lo_pool, v32lo_pool, knearlo;
   bool lo_built = false;
   bool lo_unavailable = false;  // the lo parts did not fit: fp64x is the FP64 form
   std::vector<int32_t> h_pair_m, h_pair_n;  // per pair: source and target box sizes
   std::vector<int64_t> h_ubox_off, h_tbox_off;
   std::vector<int32_t> h_rbox, h_ustride, h_coff;
-  hodlr3d_host::DevBuf ustride, tc_toff, tc_tld, tc_tbox, tc_rbox;
-  hodlr3d_host::DevBuf rank, u64, v64, u32, v32, tr_off, part_off, items, upper, pair_level;
+  DevBuf ustride, tc_toff, tc_tld, tc_tbox, tc_rbox;
+  DevBuf rank, u64, v64, u32, v32, tr_off, part_off, items, upper, pair_level;
   int64_t sum_rank = 0, sum_rank4 = 0, part_total = 0, n_items = 0, n_upper = 0, factor_entries = 0;
   int tc_entries = 0;  // largest table of a tensor-core block
   int64_t u_entries = 0, v_entries = 0;
@@ -170,7 +173,7 @@ struct hodlr3d_handle {
   double aca_kernel_seconds = 0.0;  // device time of the ACA kernels of the last assembly
   double finish_seconds = 0.0;      // finish_assembly of the last assembly or load
   // matvec work buffers
-  hodlr3d_host::DevBuf xsorted, tbuf, pbuf, ynl, stage_x, stage_y, stage_t;
+  DevBuf xsorted, tbuf, pbuf, ynl, stage_x, stage_y, stage_t;
   int mv_nrhs_cap = 0;
   // optional per-kernel timing of matvec launches
   struct Prof : h3d::MatvecProfiler {
@@ -206,33 +209,33 @@ struct hodlr3d_handle {
   // automatic choice for the mixed product, per (transpose, nrhs), from the
   // timings of hodlr3d_autotune: 0 = the column-count rules, else an engine
   int8_t tuned[2][65] = {};
-  hodlr3d_host::DevBuf dev_err;   // set by kernels whose bounded waits gave up
+  DevBuf dev_err;   // set by kernels whose bounded waits gave up
   bool leaves_aligned = false;  // every leaf population a multiple of 4
-  hodlr3d_host::DevBuf knear, near_off;       // FP32 near-field blocks of the tensor-core engine
-  hodlr3d_host::DevBuf tct;                   // X and T of the tensor-core engine (split-exact FP32)
-  hodlr3d_host::DevBuf tmaps;                 // tensor maps of the tensor-core engine: U, V, near blocks
+  DevBuf knear, near_off;       // FP32 near-field blocks of the tensor-core engine
+  DevBuf tct;                   // X and T of the tensor-core engine (split-exact FP32)
+  DevBuf tmaps;                 // tensor maps of the tensor-core engine: U, V, near blocks
   bool maps_built = false;
   bool near_built = false;
   std::vector<int32_t> h_nbr_leaf;  // host copy (tensor maps of the near-field blocks)
   std::vector<int64_t> h_near_off;  // 27 per leaf: near-block offsets, -1 for no neighbour
   std::vector<int64_t> h_near_base;  // per leaf: its near-field matrix (blocks side by side)
   std::vector<int32_t> h_near_ld;    // per leaf: row length of that matrix
-  hodlr3d_host::DevBuf near_base, near_ld;
+  DevBuf near_base, near_ld;
   int64_t near_floats = 0;
   // few-column engine (matvec_gemv.cu): tables over the grouped FP32 layouts
   bool gemv_built = false;
   bool gemv_ok = false;          // tree and layouts fit the few-column kernels
   bool gemv8_ok = false;         // ... in passes of 8 columns (mixed form)
-  hodlr3d_host::DevBuf gv_ubox_off, gv_vbox_off, gv_vbox_rows, gv_vrow0, gv_vrow_t, gv_trow_v, gv_tbase, gv_vpofs,
+  DevBuf gv_ubox_off, gv_vbox_off, gv_vbox_rows, gv_vrow0, gv_vrow_t, gv_trow_v, gv_tbase, gv_vpofs,
       gv_upofs, gv_vt_items, gv_vt_upper, gv_ut_items, gv_ut_upper, gv_x, gv_t, gv_tt, gv_p, gv_pt,
       gv_xl, gv_tl, gv_ttl, gv_pd, gv_ptd;
   int64_t gv_n_vt_items = 0, gv_n_vt_upper = 0, gv_n_ut_items = 0, gv_n_ut_upper = 0;
   // GMRES work buffers
-  hodlr3d_host::DevBuf g_Q, g_w, g_r, g_x, g_b, g_H, g_cs, g_sn, g_beta, g_hk, g_bnorm, g_err, g_part, g_y,
+  DevBuf g_Q, g_w, g_r, g_x, g_b, g_H, g_cs, g_sn, g_beta, g_hk, g_bnorm, g_err, g_part, g_y,
       g_kcol, g_brk, g_scal, g_d, g_coef;
 
   ~hodlr3d_handle() {
-    for (hodlr3d_host::DevBuf* b : pools) delete b;
+    for (DevBuf* b : pools) delete b;
     if (stream) cudaStreamDestroy(stream);
   }
 };
