@@ -54,8 +54,19 @@ def test_invalid_arguments_fail_cleanly():
     assert code == _lib.ERR_INVALID_ARG and not h.value
     code = L.hodlr3d_create(pts.ctypes.data, 10, 4, 1.0, 10, -1, None, ctypes.byref(h))
     assert code == _lib.ERR_INVALID_ARG and not h.value
-    # null handle
+    # null handle: every entry point that takes one refuses it
     assert L.hodlr3d_assemble(None) == _lib.ERR_INVALID_ARG
+    buf = ctypes.create_string_buffer(64)
+    choice = np.zeros(128, np.int32)
+    assert L.hodlr3d_autotune(None, 3, buf, 64) == _lib.ERR_INVALID_ARG
+    assert L.hodlr3d_get_tuning(None, choice.ctypes.data) == _lib.ERR_INVALID_ARG
+    assert L.hodlr3d_set_engine(None, 0) == _lib.ERR_INVALID_ARG
+    assert L.hodlr3d_matvec(None, None, None, 1, 10, 0, None) == _lib.ERR_INVALID_ARG
+    assert L.hodlr3d_dense_rows(None, None, 0, None, None, 1, 10, None) == _lib.ERR_INVALID_ARG
+    assert L.hodlr3d_get_stats(None, None) == _lib.ERR_INVALID_ARG
+    assert L.hodlr3d_device_status(None) == _lib.ERR_INVALID_ARG
+    assert L.hodlr3d_launch_count(None) == 0
+    L.hodlr3d_destroy(None)  # a no-op
     # factor files: bad arguments and a missing file fail before any device work
     assert L.hodlr3d_save(None, b"x.h3d") == _lib.ERR_INVALID_ARG
     assert L.hodlr3d_load(None, None, ctypes.byref(h)) == _lib.ERR_INVALID_ARG
