@@ -6,7 +6,14 @@ oracle/_ref/hodlr3d_ref, which is run on each case below; its dumps are
 canonicalised and stored as compressed .npz files.  Only needed where the
 reference checkout is present; the fixtures themselves are committed.
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <reference checkout> [--only NAME]
+
+(or HODLR3D_REFERENCE=<reference checkout> in the environment).  Each case is
+also run through oracle/_ref/hodlr3d_ref_plain, the same sources with plain
+left-to-right norms and dot products in the shim, and the number of blocks
+whose ACA rank differs between the two reduction orders is stored
+(rank_flips_plain_sums): it says how much "identical ranks" depends on the
+shim's canonical reduction order at the Eigen boundary.
 """
 from __future__ import annotations
 
@@ -46,6 +53,15 @@ CASES = {
     "grid16_q11_tol8": ("grid_cell_centres", (16,), 4, 1.0, 8, 11, "nan", 0, True),
     "grid16_q12_tol8": ("grid_cell_centres", (16,), 4, 1.0, 8, 12, "nan", 0, True),
     "grid16_q14_tol8": ("grid_cell_centres", (16,), 4, 1.0, 8, 14, "nan", 0, True),
+    # 32^3 grid at tol 1e-12 and 32768 uniform random points at tol 1e-12: the
+    # plain FP64 form at scale
+    "grid32_q16_tol12": ("grid_cell_centres", (32,), 4, 1.0, 12, 16, "nan", 0, False),
+    "rand32768_q16_tol12": ("uniform_random", (32768, 1), 4, 1.0, 12, 16, "nan", 0, False),
+    # 64^3 grid (depth 4, 262144 points), 1/r with quadrature diagonal, tol 1e-10:
+    # the operator of the solve/adjoint workload and of the batched-product benchmark
+    "grid64_q16_tol10": ("grid_cell_centres", (64,), 4, 1.0, 10, 16, "nan", 40, False),
+    # 64^3 grid, exp(-r) with diagonal 1, tol 1e-8: the precision/batching workload
+    "grid64_q1diag1_tol8": ("grid_cell_centres", (64,), 4, 1.0, 8, 1, "1.0", 0, False),
 }
 
 
@@ -57,8 +73,10 @@ def pivot_hash(rows: np.ndarray, cols: np.ndarray) -> int:
     return zlib.crc32(np.ascontiguousarray(np.stack([rows, cols]), np.int32).tobytes())
 
 
-def run_case(binary: str, name: str, spec) -> dict:
+def run_case(binary: str, name: str, spec, ranks_only: bool = False) -> dict:
     gen, args, nP1D, L, tol, q, diag, gmres_maxit, full_piv = spec
+    if ranks_only:
+        gmres_maxit = 0
     pts = getattr(workloads, gen)(*args)
     N = len(pts)
     charges = workloads.charges_uniform(N, seed=1)
@@ -78,6 +96,10 @@ def run_case(binary: str, name: str, spec) -> dict:
         assert N_ == N
         lv, bx, src = rd("il_level.i32", np.int32), rd("il_box.i32", np.int32), rd("il_idx.i32", np.int32)
         rank = rd("rank.i32", np.int32)
+        if ranks_only:
+            keep = lv >= 1
+            order = np.lexsort((src[keep], bx[keep], lv[keep]))
+            return dict(rank=rank[np.nonzero(keep)[0][order]])
         pp = rd("piv_ptr.i32", np.int32)
         rp, cp = rd("row_piv.i32", np.int32), rd("col_piv.i32", np.int32)
         keep = lv >= 1
@@ -106,10 +128,14 @@ def run_case(binary: str, name: str, spec) -> dict:
             out["row_piv"] = rows.astype(np.int16 if N < 32768 else np.int32)
             out["col_piv"] = cols.astype(np.int16 if N < 32768 else np.int32)
         else:
-            # one CRC32 per target box (level, box) over its pairs' pivots in canonical order
+            # one CRC32 per target box (level, box) over its pairs' pivots in
+            # canonical order; idx is sorted by (level, box, source), so every
+            # box is one run of it
+            key = pairs[:, 0].astype(np.int64) * (1 << 32) + pairs[:, 1]
+            starts = np.concatenate([[0], np.nonzero(np.diff(key))[0] + 1, [len(key)]])
             crcs = []
-            for key in np.unique(pairs[:, 0].astype(np.int64) * (1 << 32) + pairs[:, 1]):
-                sel = idx[(lv[idx].astype(np.int64) * (1 << 32) + bx[idx]) == key]
+            for a, b in zip(starts[:-1], starts[1:]):
+                sel = idx[a:b]
                 rows = np.concatenate([rp[pp[i]:pp[i + 1]] for i in sel])
                 cols = np.concatenate([cp[pp[i]:pp[i + 1]] for i in sel])
                 crcs.append(pivot_hash(rows, cols))
@@ -125,15 +151,22 @@ def run_case(binary: str, name: str, spec) -> dict:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", default=None)
+    ap.add_argument("--ref", default=os.environ.get("HODLR3D_REFERENCE"))
+    ap.add_argument("--only", default=None, help="comma-separated case names")
     a = ap.parse_args()
+    if not a.ref:
+        ap.error("give --ref <reference checkout> or set HODLR3D_REFERENCE")
     subprocess.run(["make", "-s", "-j8", "-f", "oracle/Makefile.ref", f"REF={a.ref}"], cwd=ROOT, check=True)
     binary = os.path.join(ROOT, "oracle", "_ref", "hodlr3d_ref")
+    plain = os.path.join(ROOT, "oracle", "_ref", "hodlr3d_ref_plain")
+    only = set(a.only.split(",")) if a.only else None
     for name, spec in CASES.items():
-        if a.only and name != a.only:
+        if only and name not in only:
             continue
         data = run_case(binary, name, spec)
+        alt = run_case(plain, name + " (plain sums)", spec, ranks_only=True)
+        data["rank_flips_plain_sums"] = np.int64(np.count_nonzero(alt["rank"] != data["rank"]))
+        print(name, ": blocks whose rank changes with plain sums:", int(data["rank_flips_plain_sums"]))
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **data)
 
 
