@@ -9,8 +9,8 @@ HBM.  `e2e` is the same product through the C-ABI host entry point
 (hodlr3d_matvec_host: host buffers, copies inside the timed region).  The
 FP64 form at one right-hand side and the GMRES solves are reported beside it.
 `--impl reference` times the reference algorithm on the host cores (the CPU
-oracle port of it: the reference's sources do not travel with this package)
-on a bounded sample of the same workload.  For N > 1 (torchrun) every
+oracle port of it: the reference's sources do not travel with this package):
+it assembles the whole operator, then every step is one complete FP64 matvec.  For N > 1 (torchrun) every
 rank runs an independent replica; value = all ranks' right-hand sides / max time.
 """
 from __future__ import annotations
@@ -124,40 +124,39 @@ def max_over_ranks(ws, v: float) -> float:
 
 
 # ----------------------------------------------------------------------------
-def cpu_sample(pts, tol_pow, steps, warmup, threads, n_leaves=16, qchoice=16, diag=float("nan")):
-    """Times the reference algorithm (the CPU oracle, CUR form with the kernel
-    entries re-evaluated as src/HODLR3DTree.cpp:1660-1755 does) on a bounded
-    sample: the far field of the ancestors of n_leaves spread-out leaves at
-    every level plus their near field, each level scaled by its box count.
-    Returns seconds per full matvec (one right-hand side) per step."""
+def cpu_full_product(pts, tol_pow, steps, warmup, threads, qchoice=16, diag=float("nan")):
+    """Times the reference algorithm on the host cores: the CPU oracle (the
+    reference's CUR form, src/ACA.cpp:127-238, with the kernel entries of Ac,
+    Ar and the near-field blocks re-evaluated at every product as
+    src/HODLR3DTree.cpp:1660-1755 does) assembles the whole operator, then
+    every step is one complete FP64 matvec (all boxes of every level and the
+    whole near field, one right-hand side), timed by the wall clock.
+    Returns (seconds per step for the timed steps, assembly seconds)."""
     from oracle import oracle as orc
     orc.set_threads(threads)
     o = orc.Oracle(pts, 4, 1.0, tol_pow, qchoice, diag)
-    d = o.levels
-    nleaf = 8 ** d
-    leaves = np.linspace(0, nleaf - 1, n_leaves).astype(np.int64)
-    sel = {j: sorted({int(l >> (3 * (d - j))) for l in leaves}) for j in range(1, d + 1)}
-    lv = np.concatenate([[j] * len(b) for j, b in sel.items()]).astype(np.int32)
-    bx = np.concatenate([b for b in sel.values()]).astype(np.int32)
     t = time.perf_counter()
-    o.assemble(lv, bx)
+    o.assemble()
     t_aca = time.perf_counter() - t
     x = np.random.default_rng(5).standard_normal(o.N)
     out = []
     for it in range(warmup + steps):
-        total = 0.0
-        for j in range(1, d + 1):
-            b = np.array(sel[j], np.int32)
-            t = time.perf_counter()
-            o.matvec(x, np.full(len(b), j, np.int32), b)
-            total += (time.perf_counter() - t) * (8 ** j) / len(b)
+        t = time.perf_counter()
+        o.matvec(x)
+        dt = time.perf_counter() - t
         if it >= warmup:
-            out.append(total)
-    desc = (f"far field of the ancestors of {n_leaves} spread leaves at every level "
-            f"({', '.join(f'L{j}:{len(b)}/{8**j}' for j, b in sel.items())} target boxes) plus their "
-            f"near field, CUR form with re-evaluated entries as the reference, scaled by box count; "
-            f"sample ACA {t_aca:.1f}s")
-    return out, desc
+            out.append(dt)
+    return out, t_aca
+
+
+def cpu_model():
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
 
 
 def run_reference(args):
@@ -167,10 +166,14 @@ def run_reference(args):
     from hodlr3d_gb300.workloads import grid_cell_centres
     pts = grid_cell_centres(args.n)
     threads = os.cpu_count() or 1
-    secs, desc = cpu_sample(pts, args.tol_pow, args.steps, args.warmup, threads, qchoice=args.qchoice,
-                            diag=args.diag)
+    secs, t_aca = cpu_full_product(pts, args.tol_pow, args.steps, args.warmup, threads,
+                                   qchoice=args.qchoice, diag=args.diag)
     s = float(np.mean(secs))
     v = 1.0 / s
+    desc = (f"the whole {args.n}^3 operator: every step one complete FP64 matvec of one right-hand "
+            f"side (all levels, all boxes, near field; entries re-evaluated as the reference does), "
+            f"wall clock; CPU oracle, {threads} threads ({cpu_model()}); assembly {t_aca:.1f} s "
+            f"beforehand, untimed")
     line = {
         "metric": METRIC, "value": v, "unit": "RHS/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": s * 1e3, "higher_is_better": True,
@@ -178,8 +181,10 @@ def run_reference(args):
         "impl": "reference",
         "config": config(args),
         "cpu_baseline": {"value": v, "unit": "RHS/s", "cores": threads, "kind": "port",
-                         "sample": desc},
+                         "sample": desc, "extrapolated": False},
         "e2e": {"value": v, "unit": "RHS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "assembly_seconds": t_aca,
+        "step_seconds": secs,
     }
     print(json.dumps(line), flush=True)
 
@@ -524,21 +529,28 @@ def run_ours(args):
     tune = None
     if not args.no_autotune:
         t = time.perf_counter()
-        rows = H.autotune(reps=3)
+        tune_rows = H.autotune(reps=3)
         ch = H.tuning()
         H.autotune(reps=0)
         counts = (1, 2, 4, 8, 16, 32, 64)
         tune = {"seconds": time.perf_counter() - t,
                 "forward": {n: ch["forward"][n - 1] for n in counts},
                 "transpose": {n: ch["transpose"][n - 1] for n in counts},
-                "ms": {f"{'AT' if tr else 'A'}_{n}_{e}": round(ms, 3) for tr, n, e, ms in rows}}
+                "ms": {f"{'AT' if tr else 'A'}_{n}_{e}": round(ms, 3) for tr, n, e, ms in tune_rows}}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
+        # the whole operator assembled by the CPU oracle, then complete FP64
+        # products timed (after the GPU measurements: the host threads would
+        # perturb their launches)
         threads = os.cpu_count() or 1
-        secs, desc = cpu_sample(pts, args.tol_pow, 1, 0, threads, qchoice=args.qchoice, diag=args.diag)
+        secs, t_aca = cpu_full_product(pts, args.tol_pow, 2, 1, threads, qchoice=args.qchoice,
+                                       diag=args.diag)
         cpu = {"value": 1.0 / float(np.mean(secs)), "unit": "RHS/s", "cores": threads,
-               "kind": "port", "sample": desc}
+               "kind": "port", "extrapolated": False,
+               "sample": f"two complete FP64 matvecs of the whole {args.n}^3 operator (one right-hand "
+                         f"side each, entries re-evaluated as the reference does) after one untimed, "
+                         f"wall clock, {threads} threads ({cpu_model()}); CPU assembly {t_aca:.1f} s"}
 
     if rank == 0:
         line = {
