@@ -99,6 +99,8 @@ def lib() -> ctypes.CDLL:
         "hodlr3d_matvec_host_rows": ([vp, vp, vp, i32, i32], i32),
         "hodlr3d_matvec_transpose": ([vp, vp, vp, i32, i64, i32, vp], i32),
         "hodlr3d_dense_rows": ([vp, vp, i64, vp, vp, i32, i64, vp], i32),
+        "hodlr3d_entries": ([vp, vp, vp, i64, vp], i32),
+        "hodlr3d_quadrature_kii": ([i64, ctypes.POINTER(dbl)], i32),
         "hodlr3d_gmres": ([vp, vp, vp, i32, i64, ctypes.POINTER(GmresParams),
                            ctypes.POINTER(GmresResult), vp, i32, ctypes.POINTER(i32), vp], i32),
         "hodlr3d_get_stats": ([vp, ctypes.POINTER(Stats)], i32),

@@ -236,6 +236,40 @@ int hodlr3d_dense_rows(hodlr3d_t h, const int64_t* rows, int64_t nrows, const do
   return exception_status();
 }
 
+int hodlr3d_quadrature_kii(int64_t n, double* kii) try {
+  if (n < 1 || !kii) return set_error(HODLR3D_ERR_INVALID_ARG, "n must be >= 1 and kii non-null");
+  *kii = quadrature_kii(n);
+  return HODLR3D_OK;
+} catch (...) {
+  return exception_status();
+}
+
+int hodlr3d_entries(hodlr3d_t h, const int64_t* rows, const int64_t* cols, int64_t n,
+                    double* out) try {
+  H3D_TRY(check_handle(h));
+  if (n < 0 || (n > 0 && (!rows || !cols || !out)))
+    return set_error(HODLR3D_ERR_INVALID_ARG, "bad arguments");
+  if (n == 0) return HODLR3D_OK;
+  for (int64_t e = 0; e < n; ++e)
+    if (rows[e] < 0 || rows[e] >= h->N || cols[e] < 0 || cols[e] >= h->N)
+      return set_error(HODLR3D_ERR_INVALID_ARG, "entry %lld: ids (%lld, %lld) outside [0, %lld)",
+                       (long long)e, (long long)rows[e], (long long)cols[e], (long long)h->N);
+  DevBuf rc, v;
+  H3D_CUDA(rc.ensure(sizeof(int64_t) * 2 * n));
+  H3D_CUDA(v.ensure(sizeof(double) * n));
+  cudaStream_t s = h->stream;
+  H3D_CUDA(cudaMemcpyAsync(rc.p, rows, sizeof(int64_t) * n, cudaMemcpyHostToDevice, s));
+  H3D_CUDA(cudaMemcpyAsync(rc.as<int64_t>() + n, cols, sizeof(int64_t) * n, cudaMemcpyHostToDevice, s));
+  h3d::launch_entries(s, h->N, h->xyz.as<double>(), h->kd, rc.as<int64_t>(), n, v.as<double>());
+  ++h->launches;
+  H3D_CUDA(cudaGetLastError());
+  H3D_CUDA(cudaMemcpyAsync(out, v.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  H3D_CUDA(cudaStreamSynchronize(s));
+  return HODLR3D_OK;
+} catch (...) {
+  return exception_status();
+}
+
 int hodlr3d_gmres(hodlr3d_t h, const double* b, double* x, int nrhs, int64_t ld,
                   const hodlr3d_gmres_params* prm, hodlr3d_gmres_result* res, double* hist,
                   int hist_cap, int* n_hist, void* stream) try {

@@ -468,6 +468,29 @@ __global__ void k_dense_rows(int64_t N, const double* __restrict__ xyz, KernelDe
   }
 }
 
+// out[e] = K(rows[e], cols[e]) in FP64 over the original points (the FP64
+// product's entry formula; the diagonal value where the ids are equal); an id
+// outside [0, N) gives NaN.
+__global__ void k_entries(int64_t N, const double* __restrict__ xyz, KernelDesc kd,
+                          const int64_t* __restrict__ rc, int64_t n, double* __restrict__ out) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const int64_t i = rc[e], j = rc[n + e];
+  if (i < 0 || i >= N || j < 0 || j >= N) {
+    out[e] = __longlong_as_double(0x7ff8000000000000LL);
+    return;
+  }
+  out[e] = i == j ? kd.diag
+                  : entry64_offdiag(kd, xyz[3 * i] - xyz[3 * j], xyz[3 * i + 1] - xyz[3 * j + 1],
+                                    xyz[3 * i + 2] - xyz[3 * j + 2]);
+}
+
+void launch_entries(cudaStream_t s, int64_t N, const double* xyz, KernelDesc kd, const int64_t* rc,
+                    int64_t n, double* out) {
+  if (n == 0) return;
+  k_entries<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(N, xyz, kd, rc, n, out);
+}
+
 namespace {
 // 32 x 32 tiles through shared memory (one padding column against bank conflicts)
 __global__ void k_transpose(const double* __restrict__ in, int64_t rows, int64_t cols,

@@ -226,4 +226,8 @@ void launch_dense_rows(cudaStream_t s, int64_t N, const double* xyz, KernelDesc 
                        const int64_t* rows, int64_t nrows, const double* X, int64_t ldx,
                        double* Y, int nrhs);
 
+// out[e] = K(rc[e], rc[n + e]) for e < n (device arrays), FP64
+void launch_entries(cudaStream_t s, int64_t N, const double* xyz, KernelDesc kd, const int64_t* rc,
+                    int64_t n, double* out);
+
 }  // namespace h3d

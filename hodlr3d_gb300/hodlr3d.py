@@ -173,6 +173,18 @@ class HODLR3D:
             check(code)
         return x.T.reshape(shape), info
 
+    def entries(self, rows, cols) -> np.ndarray:
+        """K(rows[e], cols[e]) as the device evaluates it (FP64; the diagonal
+        value where the ids are equal); original point ids."""
+        r = np.ascontiguousarray(np.asarray(rows, np.int64).reshape(-1))
+        c = np.ascontiguousarray(np.asarray(cols, np.int64).reshape(-1))
+        if r.shape != c.shape:
+            raise ValueError("rows and cols differ in length")
+        out = np.empty(len(r), np.float64)
+        check(self._L.hodlr3d_entries(self.handle, r.ctypes.data, c.ctypes.data, len(r),
+                                      out.ctypes.data))
+        return out
+
     def dense_rows(self, rows, x):
         """FP64 direct sum of sampled rows: y[r] = sum_j K(rows[r], j) x[j]."""
         import torch

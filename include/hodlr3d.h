@@ -18,7 +18,7 @@
 extern "C" {
 #endif
 
-#define HODLR3D_ABI_VERSION 2
+#define HODLR3D_ABI_VERSION 3
 
 typedef struct hodlr3d_handle* hodlr3d_t;
 
@@ -177,6 +177,21 @@ int hodlr3d_matvec_transpose(hodlr3d_t h, const double* x, double* y, int nrhs, 
 int hodlr3d_dense_rows(hodlr3d_t h, const int64_t* rows, int64_t nrows, const double* x,
                        double* y, int nrhs, int64_t ldx, void* stream);
 
+/* out[e] = K(rows[e], cols[e]) for e < n: the matrix entries the device
+ * evaluates (the FP64 product's formula for the handle's kernel, its
+ * diagonal value where the ids are equal), original point ids, host arrays;
+ * synchronous.  The batched counterpart of the reference's
+ * userkernel::getMatrixEntry(i, j) (include/kernel.hpp:112; kernel::getRow,
+ * getCol, getMatrix gather it, src/kernel.cpp:7-62); the C++ facade uses it
+ * to check that an application's own getMatrixEntry is the kernel the device
+ * evaluates.  HODLR3D_ERR_INVALID_ARG for an id outside [0, n). */
+int hodlr3d_entries(hodlr3d_t h, const int64_t* rows, const int64_t* cols, int64_t n, double* out);
+/* The diagonal of kernel 16 for n points: 1 + the integral of 1/(4 pi r)
+ * over a point's cell of side h = 1/cbrt(n) (16^3 Gauss-Legendre points on
+ * each octant).  Replaces the Kii computation of the reference's userkernel
+ * constructor (include/kernel.hpp:43-61, src/Integral3D.cpp:9-43); host only,
+ * no device needed. */
+int hodlr3d_quadrature_kii(int64_t n, double* kii);
 /* ---- solve ----------------------------------------------------------- */
 /* GMRES from x0 = 0 for nrhs right-hand sides (device pointers, column-major).
  * Replaces classGMRES::gmres(M, b, maxIterations, threshold, x, error,

@@ -38,7 +38,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_abi_version_and_default_options():
     L = _lib.lib()
-    assert L.hodlr3d_abi_version() == 2
+    assert L.hodlr3d_abi_version() == 3
     o = _lib.Options()
     L.hodlr3d_default_options(ctypes.byref(o))
     assert o.device == 0 and o.keep_fp32 == 1 and math.isnan(o.diag_override)
