@@ -6,11 +6,26 @@
   A^T lambda = g, and grad_b = lambda (``transpose=True`` solves A^T x = b,
   whose backward solves with A).
 
-Both take CUDA float64 tensors of shape (N,) or (N, nrhs).
+Both take CUDA float64 tensors of shape (N,) or (N, nrhs).  A forward or
+adjoint solve that does not reach its tolerance raises
+``SolveNotConverged`` (the gradient of an unconverged solve is not the
+gradient of A^{-1} b); ``ctx.info`` / ``ctx.adjoint_info`` keep the solver's
+report either way.
 """
 from __future__ import annotations
 
 import torch
+
+
+class SolveNotConverged(RuntimeError):
+    """A GMRES solve inside ``solve`` (forward or adjoint) stopped above its tolerance."""
+
+
+def _require_converged(info, what):
+    if not info["converged"]:
+        raise SolveNotConverged(
+            f"{what} GMRES stopped at relative residual {info['rel_residual']:.3e} after "
+            f"{info['iterations']} iterations without reaching its tolerance")
 
 
 class _Matvec(torch.autograd.Function):
@@ -32,6 +47,7 @@ class _Solve(torch.autograd.Function):
         ctx.opts = opts
         x, info = H.gmres(b.detach(), **opts)
         ctx.info = info
+        _require_converged(info, "forward")
         return x
 
     @staticmethod
@@ -39,7 +55,9 @@ class _Solve(torch.autograd.Function):
         # the adjoint of a solve with A is a solve with A^T, and conversely
         opts = dict(ctx.opts)
         opts["transpose"] = not opts.get("transpose", False)
-        lam, _ = ctx.H.gmres(g.contiguous(), **opts)
+        lam, info = ctx.H.gmres(g.contiguous(), **opts)
+        ctx.adjoint_info = info
+        _require_converged(info, "adjoint")
         return lam, None, None
 
 
