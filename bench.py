@@ -134,7 +134,8 @@ def cpu_full_product(pts, tol_pow, steps, warmup, threads, qchoice=16, diag=floa
     Returns (seconds per step for the timed steps, assembly seconds)."""
     from oracle import oracle as orc
     orc.set_threads(threads)
-    o = orc.Oracle(pts, 4, 1.0, tol_pow, qchoice, diag)
+    # lean: pivots and the r x r L, R per pair, as the reference stores them
+    o = orc.Oracle(pts, 4, 1.0, tol_pow, qchoice, diag, lean=True)
     t = time.perf_counter()
     o.assemble()
     t_aca = time.perf_counter() - t

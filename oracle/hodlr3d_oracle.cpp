@@ -92,6 +92,10 @@ struct PairFactors {
   int rank = 0;
   std::vector<int32_t> rows, cols;  // local pivot indices
   std::vector<double> U, V;          // n x rank, m x rank (column-major)
+  // lean storage (the reference's own, include/HODLR3DTree.hpp:20-21): the
+  // r x r factors L(a,b) = U(row_a, b) and R(a,b) = V(col_b, a), row-major,
+  // with U and V dropped after the ACA
+  std::vector<double> Lm, Rm;
 };
 
 }  // namespace
@@ -113,6 +117,7 @@ struct orc_problem {
   std::vector<std::vector<int64_t>> il_ptr;    // il_ptr[j][k] into pair arrays
   std::vector<int32_t> p_level, p_tgt, p_src;  // pair table
   std::vector<PairFactors> fac;
+  bool lean = false;
 };
 
 namespace {
@@ -470,10 +475,29 @@ int orc_assemble(orc_problem* p, const int32_t* sel_level, const int32_t* sel_bo
     const int j = p->p_level[i];
     const int64_t t0 = p->off[j][p->p_tgt[i]], t1 = p->off[j][p->p_tgt[i] + 1];
     const int64_t s0 = p->off[j][p->p_src[i]], s1 = p->off[j][p->p_src[i] + 1];
-    aca(*p, &p->perm[t0], (int)(t1 - t0), &p->perm[s0], (int)(s1 - s0), p->fac[i]);
+    PairFactors& f = p->fac[i];
+    aca(*p, &p->perm[t0], (int)(t1 - t0), &p->perm[s0], (int)(s1 - s0), f);
+    if (p->lean) {
+      const int r = f.rank, n = (int)(t1 - t0), m = (int)(s1 - s0);
+      f.Lm.assign((size_t)r * r, 0.0);
+      f.Rm.assign((size_t)r * r, 0.0);
+      for (int a = 0; a < r; ++a)
+        for (int b = 0; b < r; ++b) {
+          f.Lm[(size_t)a * r + b] = f.U[(size_t)b * n + f.rows[a]];
+          f.Rm[(size_t)a * r + b] = f.V[(size_t)a * m + f.cols[b]];
+        }
+      std::vector<double>().swap(f.U);
+      std::vector<double>().swap(f.V);
+    }
   }
   return 0;
 }
+
+// Lean storage for the assemblies that follow: only pivots and the r x r L, R
+// are kept (the CUR product needs nothing else); the residual-vector forms
+// (orc_pair_factors, orc_matvec_uv, orc_matvec_uv_t) are then unavailable.
+void orc_set_lean(orc_problem* p, int lean) { p->lean = lean != 0; }
+int orc_is_lean(const orc_problem* p) { return p->lean ? 1 : 0; }
 
 void orc_ranks(const orc_problem* p, int32_t* rank) {
   for (size_t i = 0; i < p->fac.size(); ++i) rank[i] = p->fac[i].rank;
@@ -532,15 +556,22 @@ void orc_matvec(const orc_problem* p, const double* xin, double* yout, const int
             for (int64_t c = 0; c < m; ++c) s += entry(*p, gi, p->perm[s0 + c]) * xs[s0 + c];
             t[l] = s;
           }
-          for (int a = 0; a < r; ++a) {  // t1 = L^-1 t0, L(a,b) = U(row_a, b)
+          // L(a,b) = U(row_a, b), R(a,b) = V(col_b, a) (or their lean copies)
+          auto Lab = [&](int a, int b) {
+            return p->lean ? f.Lm[(size_t)a * r + b] : f.U[(size_t)b * n + f.rows[a]];
+          };
+          auto Rab = [&](int a, int b) {
+            return p->lean ? f.Rm[(size_t)a * r + b] : f.V[(size_t)a * m + f.cols[b]];
+          };
+          for (int a = 0; a < r; ++a) {  // t1 = L^-1 t0
             double s = t[a];
-            for (int b = 0; b < a; ++b) s -= f.U[(size_t)b * n + f.rows[a]] * t1[b];
+            for (int b = 0; b < a; ++b) s -= Lab(a, b) * t1[b];
             t1[a] = s / 1.0;
           }
-          for (int a = r - 1; a >= 0; --a) {  // t2 = R^-1 t1, R(a,b) = V(col_b, a)
+          for (int a = r - 1; a >= 0; --a) {  // t2 = R^-1 t1
             double s = t1[a];
-            for (int b = a + 1; b < r; ++b) s -= f.V[(size_t)a * m + f.cols[b]] * t2[b];
-            t2[a] = s / f.V[(size_t)a * m + f.cols[a]];
+            for (int b = a + 1; b < r; ++b) s -= Rab(a, b) * t2[b];
+            t2[a] = s / Rab(a, a);
           }
           for (int64_t c = 0; c < n; ++c) {  // potential += Ac t2
             const int32_t gi = p->perm[t0 + c];

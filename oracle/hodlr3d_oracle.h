@@ -39,9 +39,14 @@ int64_t orc_num_pairs(const orc_problem* p);
 /* pair table in (level, target, source ascending) order: 3 ints per pair */
 void orc_pairs(const orc_problem* p, int32_t* level_tgt_src);
 
+/* Lean storage for later assemblies: pivots and the r x r L, R only (the
+ * reference's storage, include/HODLR3DTree.hpp:20-21); the residual-vector
+ * forms (orc_pair_factors, orc_matvec_uv, orc_matvec_uv_t) then refuse. */
+void orc_set_lean(orc_problem* p, int lean);
+int orc_is_lean(const orc_problem* p);
 /* ACA of every pair (reference HODLR3DTree::getUVtTree, src/HODLR3DTree.cpp:1621-1645).
  * Selection (optional, n_sel > 0): assemble only the pairs whose target box is
- * one of the listed (level, box) targets; used to time a bounded sample. */
+ * one of the listed (level, box) targets. */
 int orc_assemble(orc_problem* p, const int32_t* sel_level, const int32_t* sel_box, int n_sel);
 void orc_ranks(const orc_problem* p, int32_t* rank);
 int64_t orc_total_pivots(const orc_problem* p);

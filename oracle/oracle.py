@@ -53,6 +53,9 @@ def lib():
     L.orc_num_pairs.argtypes = [vp]
     L.orc_num_pairs.restype = ctypes.c_int64
     L.orc_pairs.argtypes = [vp, _i32p]
+    L.orc_set_lean.argtypes = [vp, ctypes.c_int]
+    L.orc_is_lean.argtypes = [vp]
+    L.orc_is_lean.restype = ctypes.c_int
     L.orc_assemble.argtypes = [vp, vp, vp, ctypes.c_int]
     L.orc_assemble.restype = ctypes.c_int
     L.orc_ranks.argtypes = [vp, _i32p]
@@ -82,7 +85,11 @@ def set_threads(n: int) -> None:
 class Oracle:
     """The reference algorithm on the CPU in FP64 (restated; see the C++ file)."""
 
-    def __init__(self, points, nP1D=4, L=1.0, tol_pow=10, kernel=16, diag=float("nan")):
+    def __init__(self, points, nP1D=4, L=1.0, tol_pow=10, kernel=16, diag=float("nan"),
+                 lean=False):
+        """lean: keep only the pivots and the r x r L, R per pair (the
+        reference's own storage; what the CUR product needs) instead of the
+        residual vectors U, V as well -- 62 GB less host memory at 64^3."""
         self._L = lib()
         pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
         self.N = pts.shape[0]
@@ -91,12 +98,17 @@ class Oracle:
                                     int(kernel), float(diag))
         self.levels = self._L.orc_levels(self.h)
         self.assembled = False
+        self._L.orc_set_lean(self.h, 1 if lean else 0)
 
     def __del__(self):
         h = getattr(self, "h", None)
         if h:
             self._L.orc_destroy(h)
             self.h = None
+
+    def _need_vectors(self):
+        if self._L.orc_is_lean(self.h):
+            raise RuntimeError("the residual vectors U, V are not kept in lean mode")
 
     # tree -------------------------------------------------------------
     @property
@@ -150,6 +162,7 @@ class Oracle:
         return r, c
 
     def pair_factors(self, pair: int, n: int, m: int, rank: int):
+        self._need_vectors()
         U = np.empty(n * rank, np.float64)
         V = np.empty(m * rank, np.float64)
         self._L.orc_pair_factors(self.h, int(pair), U, V)
@@ -174,12 +187,14 @@ class Oracle:
         return y
 
     def matvec_uv(self, x) -> np.ndarray:
+        self._need_vectors()
         x = np.ascontiguousarray(x, np.float64)
         y = np.zeros(self.N, np.float64)
         self._L.orc_matvec_uv(self.h, x, y)
         return y
 
     def matvec_uv_t(self, x) -> np.ndarray:
+        self._need_vectors()
         x = np.ascontiguousarray(x, np.float64)
         y = np.zeros(self.N, np.float64)
         self._L.orc_matvec_uv_t(self.h, x, y)

@@ -73,9 +73,11 @@ def test_aca_ranks_and_pivots(big):
         assert np.array_equal(pivot_crc_per_box(H.pairs(), ranks, rows, cols), g["piv_crc_box"])
     else:
         # exp(-r): the device exp may differ from the host's in the last bit,
-        # so a borderline block may stop one step earlier or later
+        # so a borderline block may stop a few steps earlier or later
+        # (measured: 32 of 480,600 blocks, by at most 4); the products are
+        # held to the ACA tolerance below
         diff = np.abs(ranks - ref)
-        assert (diff > 0).mean() <= 0.02 and diff.max() <= 3
+        assert (diff > 0).mean() <= 1e-3 and diff.max() <= 8, ((diff > 0).sum(), diff.max())
 
 
 def _rel(y, ref):
