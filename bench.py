@@ -267,7 +267,7 @@ GEMV_ROWS_T = 256
 
 def engine_of(kernels) -> str:
     """The matvec engine whose kernels a profile report names."""
-    if "leaf_tc" in kernels:
+    if "leaf_rows" in kernels:
         return "tc"
     if "uy" in kernels or "vy" in kernels:
         return "gemv"
@@ -314,12 +314,14 @@ def level_bytes(H, nr_pad, s, engine):
     nbn = np.where((nb >= 0) & ~vertex[None, :], cnt4[np.maximum(nb, 0)], 0).sum(axis=1)
     near = int((cnt * (cnt4 + nbn)).sum()) * 4
     if engine == "tc":
+        # the leaf level as dense FP32 blocks (leaf rows): every leaf-level
+        # pair's n x round4(m) block next to the near-field blocks
+        far_leaf = int((n[leaf] * ((m[leaf] + 3) // 4 * 4)).sum()) * 4
         return {"gather": gather,
                 "ta_slice": v_up + xb + t_up + parts,
                 "tred": parts + t_up,
-                "ta_leaf": v_leaf + xb + t_leaf,
                 "ut_tc": u_up + t_up + ynl,
-                "leaf_tc": u_leaf + near + t_leaf + xb + ynl + y}
+                "leaf_rows": near + far_leaf + xb + ynl + y}
     # few-column engine: chunk partials of the V stacks wider than GEMV_COLS
     # (forward) and of the U blocks taller than GEMV_ROWS_T (transpose), each
     # read once and reduced into the pair's rows of T

@@ -213,7 +213,16 @@ struct hodlr3d_handle {
   bool leaves_aligned = false;  // every leaf population a multiple of 4
   DevBuf knear, near_off;       // FP32 near-field blocks of the tensor-core engine
   DevBuf tct;                   // X and T of the tensor-core engine (split-exact FP32)
-  DevBuf tmaps;                 // tensor maps of the tensor-core engine: U, V, near blocks
+  DevBuf tmaps;                 // tensor maps of the tensor-core engine: U, V, leaf rows
+  // leaf rows of the tensor-core engine (product.cpp ensure_leaf_rows): per
+  // leaf its dense FP32 blocks (near field, then the leaf-level interaction
+  // list) side by side, nk x W_k at krow + h_row_base[k]; built once per handle
+  DevBuf krow, leaf_blocks, block_ptr, row_base, row_ld;
+  std::vector<int64_t> h_row_base;
+  std::vector<int32_t> h_row_ld;
+  int max_blocks = 0;
+  int64_t row_floats = 0;
+  bool rows_built = false;
   bool maps_built = false;
   bool near_built = false;
   std::vector<int32_t> h_nbr_leaf;  // host copy (tensor maps of the near-field blocks)

@@ -87,6 +87,17 @@ __host__ __device__ __forceinline__ int64_t fac_idx(int64_t i, int l, int r, int
   return (int64_t)l * ((n + 3) & ~3) + i;
 }
 
+// One dense block of a leaf row (tensor-core engine): the block of leaf k
+// with source leaf `src` (its near field or its leaf-level interaction list)
+// at column x0 of leaf k's row matrix, nk x round4(len); X of the source
+// starts at tree position src_off.
+struct LeafBlock {
+  int32_t x0;
+  int32_t src_off;
+  int32_t len;
+  int32_t src;
+};
+
 // Work buffers of the tensor-core form (32 right-hand sides, FP32):
 // xt: 32 * N floats, X in tree order, x(t, c) at xt[c N + t]; t: 32 * sum of
 // round4(rank) floats, pair p's T_p (c, l) at t[tc_toff[p] + c tc_tld[p] + l],
@@ -104,30 +115,37 @@ struct TcBuffers {
   const int32_t* upper_pairs;
   int64_t n_upper;
   int max_slice;
-  const float* knear;        // FP32 near-field blocks (launch_near_blocks)
-  const int64_t* near_off;   // 27 per leaf: block offsets, -1 for no neighbour (row
-                             // stride: the leaf's sum of round4(ne))
-  // 2D tensor maps (CUtensorMap, 128 bytes each) of the FP32 operands A, box
-  // 32 x 128, 128-byte swizzle, zero fill; boxes of all levels numbered
-  // together: umaps[b]: the U of the pairs of target box b side by side, as
-  // n x R_b (FarOp::tc_rbox); vmaps[b]: the V of the pairs whose source is box
-  // b, stacked in the order of its reverse list, as (sum of ranks) x
-  // round4(m); nmaps[27 k + s]: near-field block s of leaf k as
-  // nk x round4(ne).
+  // leaf rows: per leaf its dense blocks (near field, then the leaf-level
+  // interaction list) blocks[block_ptr[k] .. block_ptr[k + 1])
+  const LeafBlock* blocks;
+  const int32_t* block_ptr;
+  // 2D tensor maps (CUtensorMap, 128 bytes each) of the FP32 operands A,
+  // 128-byte swizzle, zero fill; boxes of all levels numbered together:
+  // umaps[b]: the U of the pairs of target box b side by side, as n x R_b
+  // (FarOp::tc_rbox), box 32 x 128; vmaps[b]: the V of the pairs whose source
+  // is box b, stacked in the order of its reverse list, as (sum of ranks) x
+  // round4(m), box 32 x 128; rmaps[k]: leaf k's row matrix, nk x W_k, box
+  // 32 x 64.
   const void* umaps;
   const void* vmaps;
-  const void* nmaps;
+  const void* rmaps;
 };
 
 // Tensor-core mixed-precision product A X for 1..32 right-hand sides (zero
-// padded to 32); leaves of at most 128 points whose populations are multiples of 4
+// padded to 32); leaves of at most 64 points whose populations are multiples of 4
 // (16-byte aligned operand rows).  Returns the number of launches.
 int launch_matvec_tc(cudaStream_t s, int64_t N, const int32_t* perm, const FarOp& far,
                      const NearOp& near, const TcBuffers& B, const double* X, int64_t ldx,
                      double* Y, int64_t ldy, int nrhs, MatvecProfiler* prof);
-// Largest number of table entries (pairs of all levels a block multiplies, or
-// a leaf's pairs plus 27 near-field blocks) one tensor-core block takes.
+// Largest number of table entries (pairs of all levels a block multiplies)
+// one tensor-core block takes.
 int tc_max_entries();
+// Evaluates the dense FP32 blocks of the leaf rows (split-exact form): block
+// i of leaf k at column blocks[block_ptr[k] + i].x0 of the nk x row_ld[k]
+// row-major matrix at Krow + row_base[k]; max_blocks = the largest count.
+int launch_row_blocks(cudaStream_t s, int64_t nleaf, int max_blocks, const int32_t* leaf_off,
+                      const NearOp& near, const LeafBlock* blocks, const int32_t* block_ptr,
+                      const int64_t* row_base, const int32_t* row_ld, float* Krow);
 // Evaluates the FP32 near-field blocks of every leaf: block (k, slot) (slots
 // 0..25 the neighbours, 26 the leaf itself) is nk x round4(ne) at
 // near_off[27 k + slot] with row stride near_ld[k] (the blocks of a leaf side

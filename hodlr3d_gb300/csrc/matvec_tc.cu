@@ -1,6 +1,8 @@
 // Tensor-core (tcgen05, kind::tf32, 3xTF32) engine of the mixed-precision
-// matvec for up to 32 right-hand sides (zero padded to 32).  Same operator and same
-// owner writes as the CUDA-core engine in matvec.cu; the products run on the
+// matvec for up to 32 right-hand sides (zero padded to 32).  Same operator
+// and same owner writes as the CUDA-core engine in matvec.cu, except that the
+// leaf-level pairs enter as their dense FP32 blocks (smaller than their
+// low-rank form at the ranks these leaves reach); the products run on the
 // 5th-generation tensor cores with FP32 accumulators in TMEM.
 //
 //   ta_slice  per (level d-1 box "slice", share of its row tiles): T of the
@@ -10,12 +12,11 @@
 //             of 128 rows, K = slice points); level d-1 pairs get T, the pairs
 //             above get slice partials
 //   tred      compensated sum of the slice partials
-//   ta_leaf   per input leaf: the same for the leaf-level pairs
 //   ut_tc     per (slice, 128 rows): long-K GEMM over the pairs of levels < d,
 //             sum of U_p[rows] T_p
-//   leaf_tc   per output leaf: long-K GEMM over its leaf-level pairs (U_p T_p)
-//             and its near-field blocks (K_near X_near), plus the slice sum;
-//             written once in the original order
+//   leaf_rows per output leaf: its dense blocks (near field and leaf-level
+//             interaction list) times the sources' X, two blocks per tile,
+//             plus the level sums; written once in the original order
 //
 // A block streams K = 64 chunks over its M = 128 output tiles.  A T tile (ta)
 // runs over one K range, its input box; the tile of ut / leaf runs over its
@@ -785,98 +786,6 @@ __global__ void __launch_bounds__(THREADS, 1) k_ut_tc(FarOp op, const CUtensorMa
   block_teardown(tmem);
 }
 
-struct SrcLeaf : SrcItems {
-  const double* ynl;
-  const int32_t* perm;
-  double* y;
-  int64_t N, ldy, t0;
-  int nrhs, d;
-  __device__ void finish(int, const float* sum, const float* comp, const float* cross) const {
-    const int row = threadIdx.x & 127, c0 = (threadIdx.x >> 7) * NCOL;
-    if (row >= nrows) return;
-    const int64_t t = t0 + row;
-    const int64_t orig = perm[t];
-#pragma unroll
-    for (int j = 0; j < NCOL; ++j) {
-      const int c = c0 + j;
-      if (c < nrhs) {
-        const double yn = d >= 2 ? ynl[(int64_t)c * N + t] : 0.0;
-        y[(int64_t)c * ldy + orig] = (((double)sum[j] - (double)comp[j]) + (double)cross[j]) + yn;
-      }
-    }
-  }
-};
-
-// Phase B at the leaf level plus the near field: one block per output leaf
-// of at most 128 points.
-__global__ void __launch_bounds__(THREADS, 1) k_leaf_tc(FarOp op, NearOp nr,
-                                                        const CUtensorMap* __restrict__ umaps,
-                                                        const CUtensorMap* __restrict__ nmaps,
-                                                        const float* __restrict__ T,
-                                                        const float* __restrict__ Xt, int64_t N,
-                                                        const double* __restrict__ Ynl,
-                                                        const int32_t* __restrict__ perm, int nrhs,
-                                                        double* __restrict__ Y, int64_t ldy,
-                                                        int* __restrict__ err) {
-  extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ uint64_t bar[NBAR];
-  __shared__ uint32_t tslot;
-  Item* items = reinterpret_cast<Item*>(smem + TAB_OFF);
-  int* cofs = reinterpret_cast<int*>(smem + TAB_OFF + kMaxEntries * ENTRY_BYTES);
-  if (smem_misaligned(smem, err)) return;
-  const int d = op.levels;
-  const int64_t k = blockIdx.x;
-  const int64_t t0 = op.leaf_off[k];
-  const int nk = (int)(op.leaf_off[k + 1] - t0);
-  if (nk <= 0) return;
-  // items: all leaf-level pairs of the leaf (one item), then its 27 near-field
-  // blocks (neighbour slots 0..25, then the leaf itself)
-  const int n = 28;
-  for (int i = threadIdx.x; i < n; i += THREADS) {
-    Item it;
-    if (i == 0) {
-      it = box_item(op, umaps, level_base(d) + k, 0, T);
-    } else {
-      const int sl = i - 1;
-      const int64_t nn = sl < 26 ? (int64_t)nr.nbr_leaf[k * 26 + sl] : k;
-      it.map = nmaps + k * 27 + sl;
-      it.b = Xt;
-      it.y = 0;
-      it.bs = it.blen = it.pad = 0;
-      if (nn >= 0) {
-        const int64_t e0 = op.leaf_off[nn];
-        it.b = Xt + e0;
-        it.bs = (int)N;
-        it.blen = (int)(op.leaf_off[nn + 1] - e0);
-      }
-    }
-    items[i] = it;
-  }
-  __syncthreads();
-  warp0_scan(n, [&](int i) { return (items[i].blen + KC - 1) / KC; }, cofs);
-  const uint32_t tmem = block_setup(bar, &tslot);
-  SrcLeaf src;
-  src.items = items;
-  src.cofs = cofs;
-  src.n = n;
-  src.nrows = nk;
-  src.ntile = 1;
-  src.cpt = cofs[n];
-  src.ynl = Ynl;
-  src.perm = perm;
-  src.y = Y;
-  src.N = N;
-  src.ldy = ldy;
-  src.t0 = t0;
-  src.nrhs = nrhs;
-  src.d = d;
-  if (run_stream(src, smem, bar, tmem, err) == 0 && threadIdx.x < WORKERS) {
-    float z[NCOL] = {};
-    src.finish(0, z, z, z);
-  }
-  block_teardown(tmem);
-}
-
 // X (original order, column-major) -> Xt[c * N + t] in tree order, split-exact FP32
 __global__ void k_gather_xt(int64_t N, int nrhs, const double* __restrict__ X, int64_t ldx,
                             const int32_t* __restrict__ perm, float* __restrict__ Xt) {
@@ -949,6 +858,393 @@ __global__ void k_near_lo(const int32_t* __restrict__ leaf_off, NearOp nr,
   }
 }
 
+// ---------------------------------------------------------------------------
+// Leaf rows: the leaf level as dense blocks, two per tensor-core tile.
+//
+// Leaf k multiplies, at the leaf level, the dense blocks of its near field
+// (itself and its face / edge neighbours) and of its leaf-level interaction
+// list.  The low-rank form of a leaf-level pair is larger than the block
+// itself at these ranks (64-point leaves at tol 1e-10: mean rank 47, so
+// r (n + m) = 6016 entries against n m = 4096), so this engine keeps those
+// blocks dense (FP32, split-exact TF32), side by side in one row-major
+// nk x W_k matrix per leaf (LeafBlock: column x0, width round4(m)); the
+// leaf-level T of the low-rank form is not needed.
+//
+// One block per leaf (nk <= 64).  Chunk c multiplies two blocks at once: rows
+// 0..63 of the 128-row tile hold block 2c, rows 64..127 block 2c + 1, each
+// over its own 64-wide K range, and B = [X_top | X_bottom] (64 columns): the
+// wanted products are the diagonal quarters of D (rows 0..63 x columns 0..31,
+// rows 64..127 x columns 32..63); both halves add to the leaf's rows and are
+// combined at the end.  Per K = 8 step one issuer multiplies A_hi (the loaded
+// FP32 tile itself, read by the tensor core as TF32 from the 128-byte
+// swizzled shared memory) by [B_hi | B_lo] (N = 128), the other A_lo (tensor
+// memory) by B_hi (N = 64).  Accumulation groups are one chunk (8 MMAs per
+// accumulator), read back and summed with compensated FP32 additions: the
+// truncating FP32 accumulation of the tensor core stays below 1e-6 of
+// same-sign sums.
+//
+// Every mbarrier wait is bounded.  A wait that gives up sets the error flag
+// and the block-wide abort flag: no role issues new copies or products after
+// that, the issuers wait (bounded) for their products in flight and the
+// producer for its copies in flight before the block frees its tensor memory
+// and exits.
+namespace lr {
+constexpr int KC = 64;
+constexpr int NB = 2 * NR;                  // B columns: top and bottom right-hand sides
+constexpr int A_HALF = 128 * 32 * 4;        // one K half of A (rows 0..127, 32 K): 16 KB
+constexpr int A_BOX = 64 * 32 * 4;          // one 64-row box: 8 KB
+constexpr int A_BYTES = 2 * A_HALF;
+constexpr int B_PART = NB * KC * 4;         // B_hi (n 0..63) or B_lo (n 64..127): 16 KB
+constexpr int SLOT = A_BYTES + 2 * B_PART;  // 64 KB
+constexpr int kSlots = 3;
+constexpr int kABuf = 2;
+constexpr int kAhead = kSlots - kABuf;
+constexpr int SMEM_BYTES = kSlots * SLOT;
+constexpr uint32_t IDESC_HL = tc::idesc_tf32(128, 2 * NB);  // A_hi [B_hi | B_lo]
+constexpr uint32_t IDESC_LH = tc::idesc_tf32(128, NB);      // A_lo B_hi
+// tensor memory (512 columns): accumulator set b at 256 b -- [HH | X1]
+// (N = 128) then X2 at + 128 (N = 64); A_lo buffer b at 256 b + 192 (64)
+constexpr uint32_t TM_SET = 256;
+constexpr uint32_t TM_X2 = 128;
+constexpr uint32_t TM_ALO = 192;
+constexpr int BAR_FULL = 0, BAR_EMPTY = kSlots, BAR_READY = 2 * kSlots, BAR_MPAR = BAR_READY + kABuf,
+              BAR_ACC = BAR_MPAR + kABuf, BAR_DRAIN = BAR_ACC + 2, NBAR = BAR_DRAIN + 2;
+static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
+static_assert(64 * NR * 8 <= SLOT, "combine buffer fits a slot");
+
+// Shared-memory descriptor of a K-major operand in the 128-byte swizzled
+// layout the tensor copies write (8-row atoms of 1024 bytes; a K = 8 step
+// inside the 128-byte row advances the start address by 32 bytes).
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;             // leading byte offset 16 (unused by this layout)
+  d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset: 8 rows of 128 bytes
+  d |= (uint64_t)1 << 46;             // descriptor version
+  d |= (uint64_t)2 << 61;             // 128-byte swizzle
+  return d;
+}
+
+__device__ __forceinline__ bool aborted(const volatile int* flag) { return *flag != 0; }
+
+__device__ __forceinline__ void give_up(int* err, volatile int* flag) {
+  atomicExch(err, 1);
+  *flag = 1;
+}
+
+// rows of the workers' named barrier (barrier 1, the 512 worker threads)
+__device__ __forceinline__ void workers_sync() { asm volatile("bar.sync 1, %0;\n" ::"n"(WORKERS) : "memory"); }
+
+__device__ __forceinline__ void tmem_ld8x3(uint32_t a0, uint32_t a1, uint32_t a2, float* v0, float* v1,
+                                           float* v2) {
+  uint32_t r[24];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                 "=r"(r[7])
+               : "r"(a0));
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+               : "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                 "=r"(r[14]), "=r"(r[15])
+               : "r"(a1));
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+               : "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+                 "=r"(r[22]), "=r"(r[23])
+               : "r"(a2));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    v0[i] = __uint_as_float(r[i]);
+    v1[i] = __uint_as_float(r[8 + i]);
+    v2[i] = __uint_as_float(r[16 + i]);
+  }
+}
+}  // namespace lr
+
+// Dense FP32 blocks of the leaf rows: block i of leaf k (LeafBlock
+// blocks[block_ptr[k] + i], source leaf src) is nk x round4(m) at column x0 of
+// leaf k's matrix (row_base[k], row stride row_ld[k]), the kernel with the
+// displacement formula of the FP32 near field, in the split-exact form; the
+// columns past m are zero.
+__global__ void k_row_blocks(const int32_t* __restrict__ leaf_off, NearOp nr,
+                             const LeafBlock* __restrict__ blocks, const int32_t* __restrict__ block_ptr,
+                             const int64_t* __restrict__ row_base, const int32_t* __restrict__ row_ld,
+                             float* __restrict__ Krow) {
+  const int64_t k = blockIdx.x;
+  const int i = blockIdx.y;
+  if (block_ptr[k] + i >= block_ptr[k + 1]) return;
+  const LeafBlock b = blocks[block_ptr[k] + i];
+  const int64_t nn = b.src;
+  const int64_t t0 = leaf_off[k], e0 = leaf_off[nn];
+  const int nk = (int)(leaf_off[k + 1] - t0), ne = b.len;
+  const int nep = (ne + 3) & ~3;
+  const int64_t ld = row_ld[k];
+  float* dst = Krow + row_base[k] + b.x0;
+  const float dcx = (float)(nr.centre[3 * k] - nr.centre[3 * nn]);
+  const float dcy = (float)(nr.centre[3 * k + 1] - nr.centre[3 * nn + 1]);
+  const float dcz = (float)(nr.centre[3 * k + 2] - nr.centre[3 * nn + 2]);
+  for (int e = threadIdx.x; e < nk * nep; e += blockDim.x) {
+    const int ii = e / nep, j = e - ii * nep;
+    float v = 0.f;
+    if (j < ne) {
+      const int64_t ti = t0 + ii, ej = e0 + j;
+      v = (nn == k && ii == j) ? (float)nr.kd.diag
+                               : entry32_offdiag(nr.kd, (nr.xl[ti] - nr.xl[ej]) + dcx,
+                                                 (nr.yl[ti] - nr.yl[ej]) + dcy,
+                                                 (nr.zl[ti] - nr.zl[ej]) + dcz);
+    }
+    dst[(int64_t)ii * ld + j] = tf32_split_value((double)v);
+  }
+}
+
+// The leaf level and the near field of leaf k = blockIdx.x, plus the level
+// sums of the levels above (Ynl, d >= 2); owner write of the leaf's rows in
+// the original order.
+__global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
+    const int32_t* __restrict__ leaf_off, const LeafBlock* __restrict__ blocks,
+    const int32_t* __restrict__ block_ptr, const CUtensorMap* __restrict__ rmaps,
+    const float* __restrict__ Xt, int64_t N, const double* __restrict__ Ynl, int levels,
+    const int32_t* __restrict__ perm, int nrhs, double* __restrict__ Y, int64_t ldy,
+    int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ uint64_t bar[lr::NBAR];
+  __shared__ uint32_t tslot;
+  __shared__ int abort_flag;
+  if (smem_misaligned(smem, err)) return;
+  const int64_t k = blockIdx.x;
+  const int64_t t0 = leaf_off[k];
+  const int nk = (int)(leaf_off[k + 1] - t0);
+  if (nk <= 0) return;
+  if (nk > 64) {
+    if (threadIdx.x == 0) atomicExch(err, 2);
+    return;
+  }
+  const LeafBlock* it = blocks + block_ptr[k];
+  const int nit = block_ptr[k + 1] - block_ptr[k];
+  const int nch = (nit + 1) / 2;
+  const CUtensorMap* map = rmaps + k;
+  const int tid = threadIdx.x;
+  volatile int* abortp = &abort_flag;
+  if (tid < 32) tc::tmem_alloc(&tslot, kTmemCols);
+  if (tid == 0) {
+    abort_flag = 0;
+    for (int i = 0; i < lr::kSlots; ++i) {
+      tc::mbar_init(&bar[lr::BAR_FULL + i], 1);
+      tc::mbar_init(&bar[lr::BAR_EMPTY + i], 2);
+    }
+    for (int i = 0; i < lr::kABuf; ++i) {
+      tc::mbar_init(&bar[lr::BAR_READY + i], WORKERS / 32);
+      tc::mbar_init(&bar[lr::BAR_MPAR + i], 2);
+    }
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&bar[lr::BAR_ACC + i], 2);
+      tc::mbar_init(&bar[lr::BAR_DRAIN + i], 1);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tslot;
+
+  if (tid >= PRODUCER) {
+    // producer warp (lane 0): four 32 x 64 boxes per chunk (K halves of the
+    // top and bottom blocks); a missing bottom block reads rows 64..127 of
+    // the leaf's matrix, all outside it: zeros
+    if ((tid & 31) == 0) {
+      int issued = 0;
+      for (int c = 0; c < nch; ++c) {
+        const int s = c % lr::kSlots;
+        if (c >= lr::kSlots && !tc::mbar_wait_sleep(&bar[lr::BAR_EMPTY + s], (uint32_t)(((c / lr::kSlots) - 1) & 1),
+                                                kWaitLimit, kWaitHintNs))
+          lr::give_up(err, abortp);
+        if (lr::aborted(abortp)) break;
+        unsigned char* a = smem + s * lr::SLOT;
+        const LeafBlock bt = it[2 * c];
+        const bool hb = 2 * c + 1 < nit;
+        const int xb = hb ? it[2 * c + 1].x0 : 0, yb = hb ? 0 : 64;
+        expect_tx(&bar[lr::BAR_FULL + s], (uint32_t)lr::A_BYTES);
+        tma_load_2d(a, map, bt.x0, 0, &bar[lr::BAR_FULL + s]);
+        tma_load_2d(a + lr::A_HALF, map, bt.x0 + 32, 0, &bar[lr::BAR_FULL + s]);
+        tma_load_2d(a + lr::A_BOX, map, xb, yb, &bar[lr::BAR_FULL + s]);
+        tma_load_2d(a + lr::A_HALF + lr::A_BOX, map, xb + 32, yb, &bar[lr::BAR_FULL + s]);
+        ++issued;
+      }
+      // copies in flight land before the block exits (bounded)
+      for (int c = issued > lr::kSlots ? issued - lr::kSlots : 0; c < issued; ++c)
+        if (!tc::mbar_wait_sleep(&bar[lr::BAR_FULL + c % lr::kSlots], (uint32_t)((c / lr::kSlots) & 1), kWaitLimit,
+                                 kWaitHintNs))
+          lr::give_up(err, abortp);
+    }
+  } else if (tid >= ISSUER0) {
+    // issuers (lane 0 of warps 16 and 17): A_hi [B_hi | B_lo] -> [HH | X1],
+    // A_lo B_hi -> X2
+    if ((tid & 31) == 0) {
+      const bool second = tid >= ISSUER0 + 32;
+      int c = 0;
+      for (; c < nch; ++c) {
+        if (!tc::mbar_wait_sleep(&bar[lr::BAR_READY + c % lr::kABuf], (uint32_t)((c / lr::kABuf) & 1), kWaitLimit,
+                                 kWaitHintNs))
+          lr::give_up(err, abortp);
+        if (lr::aborted(abortp)) break;
+        tc::fence_after_sync();
+        const uint32_t set = tmem + lr::TM_SET * (uint32_t)(c & 1);
+        unsigned char* slot = smem + (c % lr::kSlots) * lr::SLOT;
+        const uint64_t bd = tc::make_desc(tc::smem_addr(slot + lr::A_BYTES), 128, lr::KC * 32);
+        if (!second) {
+          const uint32_t a0 = tc::smem_addr(slot);
+#pragma unroll
+          for (int ks = 0; ks < lr::KC / 8; ++ks)
+            tc::mma_tf32(set, lr::desc_sw128(a0 + (uint32_t)((ks >> 2) * lr::A_HALF + (ks & 3) * 32)),
+                         bd + (uint64_t)((ks * 256) >> 4), lr::IDESC_HL, ks > 0 ? 1u : 0u);
+        } else {
+          const uint32_t alo = tmem + lr::TM_SET * (uint32_t)(c % lr::kABuf) + lr::TM_ALO;
+#pragma unroll
+          for (int ks = 0; ks < lr::KC / 8; ++ks)
+            tc::mma_tf32_ta(set + lr::TM_X2, alo + 8u * ks, bd + (uint64_t)((ks * 256) >> 4), lr::IDESC_LH,
+                            ks > 0 ? 1u : 0u);
+        }
+        tc::mma_commit(&bar[lr::BAR_MPAR + c % lr::kABuf]);
+        tc::mma_commit(&bar[lr::BAR_EMPTY + c % lr::kSlots]);
+        tc::mma_commit(&bar[lr::BAR_ACC + (c & 1)]);
+      }
+      // the products issued so far complete before the block frees tensor memory
+      tc::mma_commit(&bar[lr::BAR_DRAIN + (second ? 1 : 0)]);
+      if (!tc::mbar_wait_sleep(&bar[lr::BAR_DRAIN + (second ? 1 : 0)], 0u, kWaitLimit, kWaitHintNs))
+        lr::give_up(err, abortp);
+    }
+  } else {
+    // workers.  Thread (row R = tid % 128, K quarter kq = warp / 4): splits
+    // 16 K values of row R of A into tensor memory, copies B's k quad
+    // (tid % 16) of column tid / 16 for the top block and the bottom block,
+    // and reads back accumulator columns 8 kq .. 8 kq + 7 of its half.
+    const int w = tid >> 5, kq = w >> 2, R = tid & 127;
+    const bool bottom = (w & 3) >= 2;  // rows 64..127: warp-uniform
+    const uint32_t lane_base = ((uint32_t)(w & 3) * 32u) << 16;
+    const int bcol = tid >> 4, bk = 4 * (tid & 15);
+    const uint32_t boff_top = lr::A_BYTES + tc::kmajor_off(bcol, bk, lr::KC);
+    const uint32_t boff_bot = lr::A_BYTES + tc::kmajor_off(bcol + NR, bk, lr::KC);
+    float sum[NCOL], comp[NCOL], cross[NCOL];
+#pragma unroll
+    for (int j = 0; j < NCOL; ++j) sum[j] = comp[j] = cross[j] = 0.f;
+
+    auto load_b = [&](int c) {
+      unsigned char* slot = smem + (c % lr::kSlots) * lr::SLOT;
+      const LeafBlock bt = it[2 * c];
+      const bool okt = bk < bt.len;
+      cp_async16(slot + boff_top, okt ? Xt + (int64_t)bcol * N + bt.src_off + bk : Xt, okt);
+      bool okb = false;
+      const float* srcb = Xt;
+      if (2 * c + 1 < nit) {
+        const LeafBlock bb = it[2 * c + 1];
+        okb = bk < bb.len;
+        if (okb) srcb = Xt + (int64_t)bcol * N + bb.src_off + bk;
+      }
+      cp_async16(slot + boff_bot, srcb, okb);
+    };
+    auto read = [&](int c) {
+      const uint32_t set = tmem + lr::TM_SET * (uint32_t)(c & 1) + (bottom ? (uint32_t)NR : 0u) +
+                           (uint32_t)(NCOL * kq) + lane_base;
+      if (!tc::mbar_wait_sleep(&bar[lr::BAR_ACC + (c & 1)], (uint32_t)((c >> 1) & 1), kWaitLimit, kWaitHintNs))
+        lr::give_up(err, abortp);
+      tc::fence_after_sync();
+      float hh[NCOL], x1[NCOL], x2[NCOL];
+      lr::tmem_ld8x3(set, set + (uint32_t)lr::NB, set + lr::TM_X2, hh, x1, x2);
+      tc::fence_before_sync();
+#pragma unroll
+      for (int j = 0; j < NCOL; ++j) {
+        kahan_add(sum[j], comp[j], hh[j]);
+        cross[j] += x1[j] + x2[j];
+      }
+    };
+
+    int nload = 0;
+    for (; nload < lr::kAhead && nload < nch; ++nload) load_b(nload);
+    cp_async_commit();
+    int c = 0;
+    for (; c < nch; ++c) {
+      const int s = c % lr::kSlots;
+      // chunk c - lr::kABuf multiplied: its tensor-memory A_lo buffer (this
+      // chunk's) and its slot (refilled with B below) are free
+      if (c >= lr::kABuf && !tc::mbar_wait_sleep(&bar[lr::BAR_MPAR + c % lr::kABuf], (uint32_t)(((c / lr::kABuf) - 1) & 1),
+                                            kWaitLimit, kWaitHintNs))
+        lr::give_up(err, abortp);
+      if (lr::aborted(abortp)) break;
+      if (nload < nch) {
+        load_b(nload);
+        ++nload;
+      }
+      cp_async_commit();
+      cp_async_wait<lr::kAhead>();
+      if (!tc::mbar_wait_sleep(&bar[lr::BAR_FULL + s], (uint32_t)((c / lr::kSlots) & 1), kWaitLimit, kWaitHintNs))
+        lr::give_up(err, abortp);
+      if (lr::aborted(abortp)) break;
+      unsigned char* slot = smem + s * lr::SLOT;
+      {
+        // A_lo of 16 K values of row R, from the swizzled tile of its K half
+        const unsigned char* sa = slot + (kq >> 1) * lr::A_HALF + (uint32_t)R * 128u;
+        float lo[16];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int qq = 4 * (kq & 1) + j;
+          const float4 x = *reinterpret_cast<const float4*>(sa + ((uint32_t)(qq ^ (R & 7)) << 4));
+          lo[4 * j] = x.x - tf32_rz(x.x);
+          lo[4 * j + 1] = x.y - tf32_rz(x.y);
+          lo[4 * j + 2] = x.z - tf32_rz(x.z);
+          lo[4 * j + 3] = x.w - tf32_rz(x.w);
+        }
+        tc::tmem_st16(tmem + lr::TM_SET * (uint32_t)(c % lr::kABuf) + lr::TM_ALO + 16u * kq + lane_base, lo);
+        // low parts of this thread's two B segments, next to B_hi
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          unsigned char* sb = slot + (h ? boff_bot : boff_top);
+          const float4 xb = *reinterpret_cast<const float4*>(sb);
+          float4 lb;
+          lb.x = xb.x - tf32_rz(xb.x);
+          lb.y = xb.y - tf32_rz(xb.y);
+          lb.z = xb.z - tf32_rz(xb.z);
+          lb.w = xb.w - tf32_rz(xb.w);
+          *reinterpret_cast<float4*>(sb + lr::B_PART) = lb;
+        }
+        tc::tmem_wait_st();
+      }
+      tc::fence_async_smem();
+      tc::fence_before_sync();
+      __syncwarp();
+      if ((tid & 31) == 0) tc::mbar_arrive(&bar[lr::BAR_READY + c % lr::kABuf]);
+      if (c >= 1) read(c - 1);
+    }
+    if (c == nch && nch > 0) read(nch - 1);
+    cp_async_wait<0>();
+    // combine the halves: the bottom rows' sums go through shared memory
+    // (slot 0, free once every worker is past its last chunk)
+    lr::workers_sync();
+    double v[NCOL];
+#pragma unroll
+    for (int j = 0; j < NCOL; ++j) v[j] = ((double)sum[j] - (double)comp[j]) + (double)cross[j];
+    double* comb = reinterpret_cast<double*>(smem);
+    if (bottom) {
+#pragma unroll
+      for (int j = 0; j < NCOL; ++j) comb[(R - 64) * NR + NCOL * kq + j] = v[j];
+    }
+    lr::workers_sync();
+    if (!bottom && R < nk && !lr::aborted(abortp)) {
+      const int64_t t = t0 + R;
+      const int64_t orig = perm[t];
+#pragma unroll
+      for (int j = 0; j < NCOL; ++j) {
+        const int cc = NCOL * kq + j;
+        if (cc < nrhs) {
+          const double yn = levels >= 2 ? Ynl[(int64_t)cc * N + t] : 0.0;
+          Y[(int64_t)cc * ldy + orig] = (v[j] + comb[R * NR + cc]) + yn;
+        }
+      }
+    }
+  }
+  // teardown: every role is past its last use of tensor memory and shared memory
+  tc::fence_before_sync();
+  __syncthreads();
+  if (tid < 32) tc::tmem_dealloc(tmem, kTmemCols);
+}
+
 }  // namespace
 
 int launch_near_lo(cudaStream_t s, int64_t nleaf, const int32_t* leaf_off, const NearOp& near,
@@ -960,6 +1256,15 @@ int launch_near_lo(cudaStream_t s, int64_t nleaf, const int32_t* leaf_off, const
 
 int tc_max_entries() { return kMaxEntries; }
 
+int launch_row_blocks(cudaStream_t s, int64_t nleaf, int max_blocks, const int32_t* leaf_off,
+                      const NearOp& near, const LeafBlock* blocks, const int32_t* block_ptr,
+                      const int64_t* row_base, const int32_t* row_ld, float* Krow) {
+  if (nleaf == 0 || max_blocks == 0) return 0;
+  k_row_blocks<<<dim3((unsigned)nleaf, (unsigned)max_blocks), 256, 0, s>>>(
+      leaf_off, near, blocks, block_ptr, row_base, row_ld, Krow);
+  return 1;
+}
+
 int launch_near_blocks(cudaStream_t s, int64_t nleaf, const int32_t* leaf_off, const NearOp& near,
                        const int64_t* near_off, const int32_t* near_ld, float* Knear) {
   k_near_blocks<<<dim3((unsigned)nleaf, 27), 256, 0, s>>>(leaf_off, near, near_off, near_ld, Knear);
@@ -969,18 +1274,18 @@ int launch_near_blocks(cudaStream_t s, int64_t nleaf, const int32_t* leaf_off, c
 int launch_matvec_tc(cudaStream_t s, int64_t N, const int32_t* perm, const FarOp& far,
                      const NearOp& near, const TcBuffers& B, const double* X, int64_t ldx,
                      double* Y, int64_t ldy, int nrhs, MatvecProfiler* prof) {
+  (void)near;
   static bool attr[kMaxDevices] = {};  // kernel attributes are per device
   const int dev = current_device();
   if (!attr[dev]) {
-    cudaFuncSetAttribute(k_ta_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     cudaFuncSetAttribute(k_ta_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     cudaFuncSetAttribute(k_ut_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-    cudaFuncSetAttribute(k_leaf_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    cudaFuncSetAttribute(k_leaf_rows_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, lr::SMEM_BYTES);
     attr[dev] = true;
   }
   const CUtensorMap* umaps = static_cast<const CUtensorMap*>(B.umaps);
   const CUtensorMap* vmaps = static_cast<const CUtensorMap*>(B.vmaps);
-  const CUtensorMap* nmaps = static_cast<const CUtensorMap*>(B.nmaps);
+  const CUtensorMap* rmaps = static_cast<const CUtensorMap*>(B.rmaps);
   int launches = 0;
   if (prof) prof->begin(s);
   k_gather_xt<<<(unsigned)((N * NR + 255) / 256), 256, 0, s>>>(N, nrhs, X, ldx, perm, B.xt);
@@ -988,6 +1293,7 @@ int launch_matvec_tc(cudaStream_t s, int64_t N, const int32_t* perm, const FarOp
   if (prof) prof->mark(s, "gather");
   const int d = far.levels;
   if (d >= 2) {
+    // T of the pairs above the leaves, then their U T: level sums in Ynl
     const int64_t nslice = int64_t(1) << (3 * (d - 1));
     // several blocks share a slice's row tiles when slices are few
     const int split = (int)std::max<int64_t>(1, std::min<int64_t>(32, (16 * 152) / nslice));
@@ -1000,23 +1306,17 @@ int launch_matvec_tc(cudaStream_t s, int64_t N, const int32_t* perm, const FarOp
       ++launches;
       if (prof) prof->mark(s, "tred");
     }
-  }
-  k_ta_tc<false><<<dim3((unsigned)far.nleaf, 1), THREADS, SMEM_BYTES, s>>>(far, vmaps, B.xt, N, B.t,
-                                                                           B.p, B.err);
-  ++launches;
-  if (prof) prof->mark(s, "ta_leaf");
-  if (d >= 2) {
-    const int64_t nslice = int64_t(1) << (3 * (d - 1));
     const int tiles = (B.max_slice + 127) / 128;
     k_ut_tc<<<dim3((unsigned)nslice, (unsigned)std::max(1, tiles)), THREADS, SMEM_BYTES, s>>>(
         far, umaps, B.t, N, B.ynl, B.err);
     ++launches;
     if (prof) prof->mark(s, "ut_tc");
   }
-  k_leaf_tc<<<(unsigned)far.nleaf, THREADS, SMEM_BYTES, s>>>(far, near, umaps, nmaps, B.t, B.xt, N,
-                                                             B.ynl, perm, nrhs, Y, ldy, B.err);
+  // the leaf level (dense blocks) and the near field, plus the level sums
+  k_leaf_rows_tc<<<(unsigned)far.nleaf, THREADS, lr::SMEM_BYTES, s>>>(
+      far.leaf_off, B.blocks, B.block_ptr, rmaps, B.xt, N, B.ynl, d, perm, nrhs, Y, ldy, B.err);
   ++launches;
-  if (prof) prof->mark(s, "leaf_tc");
+  if (prof) prof->mark(s, "leaf_rows");
   return launches;
 }
 

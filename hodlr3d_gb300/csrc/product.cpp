@@ -19,11 +19,11 @@ int ensure_matvec_buffers(hodlr3d_t h, int nrhs) {
 }
 
 // Tensor maps (2D tiled, FP32, 128-byte swizzle, zero fill outside) of the
-// tensor-core engine's A operands, box 32 x 128: per target box the U of its
-// pairs side by side (n x R_b), per source box the V of its pairs (sum of
-// ranks x round4(m)), per leaf and neighbour slot the near-field block
-// (nk x round4(ne)).  Maps of empty operands stay zero and are never used.
-int build_tensor_maps(hodlr3d_t h, const std::vector<int64_t>& near_off) {
+// tensor-core engine's A operands: per target box the U of its pairs side by
+// side (n x R_b) and per source box the V of its pairs (sum of ranks x
+// round4(m)), box 32 x 128; per leaf its row matrix (nk x W_k), box 32 x 64.
+// Maps of empty operands stay zero and are never used.
+int build_tensor_maps(hodlr3d_t h) {
   static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
   if (!encode) {
     cudaDriverEntryPointQueryResult q;
@@ -33,7 +33,7 @@ int build_tensor_maps(hodlr3d_t h, const std::vector<int64_t>& near_off) {
       return set_error(HODLR3D_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
   }
   const int64_t nbox = (int64_t)h->h_vbox_rows.size();
-  const int64_t nm = 2 * nbox + 27 * h->nleaf;
+  const int64_t nm = 2 * nbox + h->nleaf;
   std::vector<CUtensorMap> maps((size_t)std::max<int64_t>(nm, 1));
   std::memset(maps.data(), 0, sizeof(CUtensorMap) * maps.size());
   std::atomic<int> bad{0};
@@ -54,7 +54,7 @@ int build_tensor_maps(hodlr3d_t h, const std::vector<int64_t>& near_off) {
                     (int)r, (long long)rows, (long long)inner, (const void*)base, box_rows, (void*)m);
     }
   };
-  const float* knear = h->knear.as<float>();
+  const float* krow = h->krow.as<float>();
   const int nthr = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
   std::vector<std::thread> th;
   for (int t = 0; t < nthr; ++t)
@@ -74,14 +74,7 @@ int build_tensor_maps(hodlr3d_t h, const std::vector<int64_t>& near_off) {
       }
       for (int64_t k = t; k < h->nleaf; k += nthr) {
         const int64_t nk = h->h_leaf_off[k + 1] - h->h_leaf_off[k];
-        for (int sl = 0; sl < 27; ++sl) {
-          const int64_t off = near_off[27 * k + sl];
-          if (off < 0) continue;
-          const int64_t nn = sl < 26 ? h->h_nbr_leaf[26 * k + sl] : k;
-          const int64_t ne = h->h_leaf_off[nn + 1] - h->h_leaf_off[nn];
-          enc(&maps[2 * nbox + 27 * k + sl], knear + off, (ne + 3) & ~int64_t(3), nk, 128,
-              h->h_near_ld[k]);
-        }
+        enc(&maps[2 * nbox + k], krow + h->h_row_base[k], h->h_row_ld[k], nk, 64, h->h_row_ld[k]);
       }
     });
   for (auto& x : th) x.join();
@@ -142,6 +135,72 @@ int ensure_near_blocks(hodlr3d_t h, const h3d::NearOp& nr, cudaStream_t s) {
   H3D_CUDA(cudaGetLastError());
   h->near_floats = tot;
   h->near_built = true;
+  return HODLR3D_OK;
+}
+
+// Leaf rows of the tensor-core engine: for every leaf (at most 64 points) its
+// blocks -- near field (neighbour slots 0..25 with a leaf, then itself), then
+// its leaf-level interaction list in pair order -- each nk x round4(m), side
+// by side in one row-major nk x W_k FP32 matrix, evaluated once per handle
+// (they depend on the points only).
+int ensure_leaf_rows(hodlr3d_t h, const h3d::NearOp& nr, cudaStream_t s) {
+  if (h->rows_built) return HODLR3D_OK;
+  if ((int64_t)h->h_nbr_leaf.size() != 26 * h->nleaf) {
+    h->h_nbr_leaf.resize(26 * h->nleaf);
+    H3D_CUDA(cudaMemcpy(h->h_nbr_leaf.data(), h->nbr_leaf.p, sizeof(int32_t) * 26 * h->nleaf,
+                        cudaMemcpyDeviceToHost));
+  }
+  const int d = h->levels;
+  const int64_t lb = h3d::level_base(d);
+  std::vector<h3d::LeafBlock> blocks;
+  std::vector<int32_t> ptr(h->nleaf + 1, 0);
+  h->h_row_base.assign(h->nleaf, 0);
+  h->h_row_ld.assign(h->nleaf, 0);
+  int64_t tot = 0;
+  int maxb = 0;
+  for (int64_t k = 0; k < h->nleaf; ++k) {
+    const int64_t nk = h->h_leaf_off[k + 1] - h->h_leaf_off[k];
+    int64_t col = 0;
+    auto add = [&](int64_t src) {
+      const int64_t m = h->h_leaf_off[src + 1] - h->h_leaf_off[src];
+      if (m <= 0) return;
+      blocks.push_back({(int32_t)col, h->h_leaf_off[src], (int32_t)m, (int32_t)src});
+      col += (m + 3) & ~int64_t(3);
+    };
+    for (int sl = 0; sl < 27; ++sl) {
+      const int64_t nn = sl < 26 ? h->h_nbr_leaf[26 * k + sl] : k;
+      if (nn >= 0) add(nn);
+    }
+    if (d >= 1)
+      for (int64_t p = h->h_il_ptr[lb + k]; p < h->h_il_ptr[lb + k + 1]; ++p) add(h->h_pair_src[p] - lb);
+    ptr[k + 1] = (int32_t)blocks.size();
+    maxb = std::max(maxb, ptr[k + 1] - ptr[k]);
+    if (col >= INT32_MAX) return set_error(HODLR3D_ERR_UNSUPPORTED, "leaf row wider than 2^31 - 1");
+    h->h_row_base[k] = tot;
+    h->h_row_ld[k] = (int32_t)col;
+    tot += nk * col;
+  }
+  H3D_CUDA(h->krow.ensure(sizeof(float) * std::max<int64_t>(tot, 4)));
+  H3D_CUDA(h->leaf_blocks.ensure(sizeof(h3d::LeafBlock) * std::max<size_t>(blocks.size(), 1)));
+  H3D_CUDA(h->block_ptr.ensure(sizeof(int32_t) * ptr.size()));
+  H3D_CUDA(h->row_base.ensure(sizeof(int64_t) * std::max<int64_t>(h->nleaf, 1)));
+  H3D_CUDA(h->row_ld.ensure(sizeof(int32_t) * std::max<int64_t>(h->nleaf, 1)));
+  if (!blocks.empty())
+    H3D_CUDA(cudaMemcpy(h->leaf_blocks.p, blocks.data(), sizeof(h3d::LeafBlock) * blocks.size(),
+                        cudaMemcpyHostToDevice));
+  H3D_CUDA(cudaMemcpy(h->block_ptr.p, ptr.data(), sizeof(int32_t) * ptr.size(), cudaMemcpyHostToDevice));
+  H3D_CUDA(cudaMemcpy(h->row_base.p, h->h_row_base.data(), sizeof(int64_t) * h->nleaf,
+                      cudaMemcpyHostToDevice));
+  H3D_CUDA(cudaMemcpy(h->row_ld.p, h->h_row_ld.data(), sizeof(int32_t) * h->nleaf,
+                      cudaMemcpyHostToDevice));
+  h->launches += h3d::launch_row_blocks(s, h->nleaf, maxb, h->leaf_off.as<int32_t>(), nr,
+                                        h->leaf_blocks.as<h3d::LeafBlock>(), h->block_ptr.as<int32_t>(),
+                                        h->row_base.as<int64_t>(), h->row_ld.as<int32_t>(),
+                                        h->krow.as<float>());
+  H3D_CUDA(cudaGetLastError());
+  h->max_blocks = maxb;
+  h->row_floats = tot;
+  h->rows_built = true;
   h->maps_built = false;
   return HODLR3D_OK;
 }
@@ -374,7 +433,7 @@ int run_gemv(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld, cuda
 }
 
 // The tensor-core engine (matvec_tc.cu) in batches of 32 columns; builds its
-// near-field blocks and tensor maps on first use.
+// leaf rows and tensor maps on first use.
 int run_tc(hodlr3d_t h, const h3d::FarOp& far, const h3d::NearOp& nr, const double* x, double* y,
            int nrhs, int64_t ld, cudaStream_t s) {
   H3D_TRY(ensure_matvec_buffers(h, 32));  // slice partials and level sums of 32 columns
@@ -382,8 +441,8 @@ int run_tc(hodlr3d_t h, const h3d::FarOp& far, const h3d::NearOp& nr, const doub
     H3D_CUDA(h->dev_err.ensure(sizeof(int)));
     H3D_CUDA(cudaMemsetAsync(h->dev_err.p, 0, sizeof(int), s));
   }
-  H3D_TRY(ensure_near_blocks(h, nr, s));
-  if (!h->maps_built) H3D_TRY(build_tensor_maps(h, h->h_near_off));
+  H3D_TRY(ensure_leaf_rows(h, nr, s));
+  if (!h->maps_built) H3D_TRY(build_tensor_maps(h));
   // [X | T], the B operands in the split-exact form
   H3D_CUDA(h->tct.ensure(sizeof(float) * 32 * (h->N + std::max<int64_t>(h->sum_rank4, 1))));
   h3d::TcBuffers T{};
@@ -395,13 +454,13 @@ int run_tc(hodlr3d_t h, const h3d::FarOp& far, const h3d::NearOp& nr, const doub
   T.upper_pairs = h->upper.as<int32_t>();
   T.n_upper = h->n_upper;
   T.max_slice = h->max_slice;
-  T.knear = h->knear.as<float>();
-  T.near_off = h->near_off.as<int64_t>();
+  T.blocks = h->leaf_blocks.as<h3d::LeafBlock>();
+  T.block_ptr = h->block_ptr.as<int32_t>();
   const CUtensorMap* tm = h->tmaps.as<CUtensorMap>();
   const int64_t nbox = (int64_t)h->h_vbox_rows.size();
   T.umaps = tm;
   T.vmaps = tm + nbox;
-  T.nmaps = tm + 2 * nbox;
+  T.rmaps = tm + 2 * nbox;
   for (int c0 = 0; c0 < nrhs; c0 += 32)
     h->launches += h3d::launch_matvec_tc(s, h->N, h->perm.as<int32_t>(), far, nr, T, x + c0 * ld,
                                          ld, y + c0 * ld, ld, std::min(32, nrhs - c0),
@@ -498,8 +557,9 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
   // the engine of this call: forced, tuned (automatic choice after
   // hodlr3d_autotune, mixed form) or 0 for the rules below
   const int engine = h->engine == 0 && mixed ? h->tuned[trans ? 1 : 0][nrhs] : h->engine;
-  // trees the tensor-core engine takes (16-byte aligned leaf rows, bounded tables)
-  const bool tc_tree = h->max_leaf <= 128 && h->leaves_aligned && h->tc_entries <= h3d::tc_max_entries();
+  // trees the tensor-core engine takes (leaves of at most 64 points, 16-byte
+  // aligned leaf rows, bounded tables)
+  const bool tc_tree = h->max_leaf <= 64 && h->leaves_aligned && h->tc_entries <= h3d::tc_max_entries();
   const int gemv_max = trans ? kGemvTransposeMax : (tc_tree ? kGemvForwardMax : kGemvForwardNoTcMax);
   bool use_gemv = false;
   // fp64x: the few-column kernels (automatic or forced); forcing the CUDA-core
@@ -542,7 +602,7 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
   if (engine == 2 && !tc_ok)
     return set_error(HODLR3D_ERR_UNSUPPORTED,
                      "the tensor-core engine needs A x (not the transpose) in the mixed form, "
-                     "leaves of at most 128 points, each a multiple of 4, and at most %d pairs per "
+                     "leaves of at most 64 points, each a multiple of 4, and at most %d pairs per "
                      "block (this tree: %d)", h3d::tc_max_entries(), h->tc_entries);
   if (tc_ok && engine != 1) return run_tc(h, far, nr, x, y, nrhs, ld, s);
   // the CUDA-core engine (matvec.cu)

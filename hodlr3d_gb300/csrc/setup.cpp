@@ -595,9 +595,9 @@ int finish_assembly(hodlr3d_t h, double t_start) {
     for (int64_t b = 0; b < (int64_t(1) << (3 * (d - 1))); ++b)
       h->max_slice = std::max(h->max_slice, h->h_leaf_off[(b + 1) << 3] - h->h_leaf_off[b << 3]);
   }
-  // table sizes of the tensor-core blocks: per level d - 1 box the pairs of
+  // table sizes of the tensor-core T blocks: per level d - 1 box the pairs of
   // its ancestors (interaction lists are symmetric, so as many by source as
-  // by target), per leaf its pairs plus 27 near-field blocks
+  // by target); the leaf kernel reads its block list from global memory
   h->tc_entries = 0;
   {
     auto cnt = [&](int j, int64_t b) {
@@ -610,7 +610,6 @@ int finish_assembly(hodlr3d_t h, double t_start) {
         for (int j = 1; j <= d - 1; ++j) n += cnt(j, b >> (3 * (d - 1 - j)));
         h->tc_entries = std::max(h->tc_entries, n);
       }
-    for (int64_t k = 0; k < h->nleaf; ++k) h->tc_entries = std::max(h->tc_entries, cnt(d, k) + 27);
   }
   h->sum_rank = acc;
   h->sum_rank4 = acc4;

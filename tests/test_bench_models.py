@@ -105,6 +105,17 @@ def test_factor_bytes_add_up_on_the_golden_tree(grid16):
     fac_simt = (sm["vtx"] - xb - t_up - parts) + (sm["ut"] - t_up - ynl) + (sm["leaf"] - xb - ynl - y)
     assert fac_simt == ent * s
     tc = bench.level_bytes(H, nr, s, "tc")
-    fac_tc = (tc["ta_slice"] - xb - t_up - parts) + (tc["ta_leaf"] - xb - t_leaf) + \
-        (tc["ut_tc"] - t_up - ynl) + (tc["leaf_tc"] - (fac_uy - fac_ut) - t_leaf - xb - ynl - y)
-    assert fac_tc == ent * s
+    # the tensor cores stream the factors above the leaves and, at the leaf
+    # level, the dense blocks of the leaf-level pairs next to the near field
+    dense_leaf = 0
+    up_ent = 0
+    for (j, a, b), r in zip(g["pairs"].tolist(), g["rank"].tolist()):
+        w = 8 ** (d - j)
+        na, mb = off[(a + 1) * w] - off[a * w], off[(b + 1) * w] - off[b * w]
+        if j == d:
+            dense_leaf += na * ((mb + 3) // 4 * 4)
+        else:
+            up_ent += r * (na + mb)
+    fac_tc = (tc["ta_slice"] - xb - t_up - parts) + (tc["ut_tc"] - t_up - ynl)
+    assert fac_tc == up_ent * s
+    assert tc["leaf_rows"] - (fac_uy - fac_ut) - xb - ynl - y == dense_leaf * s

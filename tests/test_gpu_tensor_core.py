@@ -2,7 +2,7 @@
 matvec against the CUDA-core engine and the reference's FP64 matvec.
 
 The engine takes A x in batches of up to 32 right-hand sides on trees whose
-leaf populations are multiples of 4 (16-byte aligned FP32 operand rows); the
+leaf populations are multiples of 4 (16-byte aligned FP32 operand rows) and at most 64; the
 automatic choice gives it A x with more than 4 columns (fewer go to the
 few-column kernels).  Other cases are refused with HODLR3D_ERR_UNSUPPORTED
 when it is forced, and the automatic choice routes them to the CUDA-core
@@ -28,7 +28,7 @@ def case(request):
 
 
 def tc_eligible(H):
-    return bool((np.diff(H.leaf_offsets()) % 4 == 0).all()) and int(np.diff(H.leaf_offsets()).max()) <= 128
+    return bool((np.diff(H.leaf_offsets()) % 4 == 0).all()) and int(np.diff(H.leaf_offsets()).max()) <= 64
 
 
 @pytest.mark.parametrize("nrhs", [32, 20])
