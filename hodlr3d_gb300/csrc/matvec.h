@@ -140,6 +140,8 @@ int launch_matvec_tc(cudaStream_t s, int64_t N, const int32_t* perm, const FarOp
 // Largest number of table entries (pairs of all levels a block multiplies)
 // one tensor-core block takes.
 int tc_max_entries();
+// Largest number of dense blocks in one leaf row of the tensor-core engine.
+int tc_max_row_blocks();
 // Evaluates the dense FP32 blocks of the leaf rows (split-exact form): block
 // i of leaf k at column blocks[block_ptr[k] + i].x0 of the nk x row_ld[k]
 // row-major matrix at Krow + row_base[k]; max_blocks = the largest count.

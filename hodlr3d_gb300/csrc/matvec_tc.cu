@@ -899,7 +899,9 @@ constexpr int SLOT = A_BYTES + 2 * B_PART;  // 64 KB
 constexpr int kSlots = 3;
 constexpr int kABuf = 2;
 constexpr int kAhead = kSlots - kABuf;
-constexpr int SMEM_BYTES = kSlots * SLOT;
+constexpr int kMaxBlocks = 512;             // blocks of one leaf row (table in shared memory)
+constexpr int TAB_OFF = kSlots * SLOT;
+constexpr int SMEM_BYTES = TAB_OFF + kMaxBlocks * (int)sizeof(LeafBlock);
 constexpr uint32_t IDESC_HL = tc::idesc_tf32(128, 2 * NB);  // A_hi [B_hi | B_lo]
 constexpr uint32_t IDESC_LH = tc::idesc_tf32(128, NB);      // A_lo B_hi
 // tensor memory (512 columns): accumulator set b at 256 b -- [HH | X1]
@@ -1017,9 +1019,15 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
     if (threadIdx.x == 0) atomicExch(err, 2);
     return;
   }
-  const LeafBlock* it = blocks + block_ptr[k];
   const int nit = block_ptr[k + 1] - block_ptr[k];
+  if (nit > lr::kMaxBlocks) {
+    if (threadIdx.x == 0) atomicExch(err, 2);
+    return;
+  }
   const int nch = (nit + 1) / 2;
+  // the leaf's block list, staged in shared memory
+  LeafBlock* it = reinterpret_cast<LeafBlock*>(smem + lr::TAB_OFF);
+  for (int i = threadIdx.x; i < nit; i += THREADS) it[i] = blocks[block_ptr[k] + i];
   const CUtensorMap* map = rmaps + k;
   const int tid = threadIdx.x;
   volatile int* abortp = &abort_flag;
@@ -1255,6 +1263,7 @@ int launch_near_lo(cudaStream_t s, int64_t nleaf, const int32_t* leaf_off, const
 }
 
 int tc_max_entries() { return kMaxEntries; }
+int tc_max_row_blocks() { return lr::kMaxBlocks; }
 
 int launch_row_blocks(cudaStream_t s, int64_t nleaf, int max_blocks, const int32_t* leaf_off,
                       const NearOp& near, const LeafBlock* blocks, const int32_t* block_ptr,

@@ -175,6 +175,9 @@ int ensure_leaf_rows(hodlr3d_t h, const h3d::NearOp& nr, cudaStream_t s) {
       for (int64_t p = h->h_il_ptr[lb + k]; p < h->h_il_ptr[lb + k + 1]; ++p) add(h->h_pair_src[p] - lb);
     ptr[k + 1] = (int32_t)blocks.size();
     maxb = std::max(maxb, ptr[k + 1] - ptr[k]);
+    if (maxb > h3d::tc_max_row_blocks())
+      return set_error(HODLR3D_ERR_UNSUPPORTED, "a leaf row has %d blocks; the tensor-core engine takes %d",
+                       maxb, h3d::tc_max_row_blocks());
     if (col >= INT32_MAX) return set_error(HODLR3D_ERR_UNSUPPORTED, "leaf row wider than 2^31 - 1");
     h->h_row_base[k] = tot;
     h->h_row_ld[k] = (int32_t)col;
