@@ -893,38 +893,26 @@ constexpr int KC = 64;
 constexpr int NB = 2 * NR;                  // B columns: top and bottom right-hand sides
 constexpr int A_HALF = 128 * 32 * 4;        // one K half of A (rows 0..127, 32 K): 16 KB
 constexpr int A_BOX = 64 * 32 * 4;          // one 64-row box: 8 KB
-constexpr int A_BYTES = 2 * A_HALF;
+constexpr int A_BYTES = 2 * A_HALF;         // an A slot: 32 KB
 constexpr int B_PART = NB * KC * 4;         // B_hi (n 0..63) or B_lo (n 64..127): 16 KB
-constexpr int SLOT = A_BYTES + 2 * B_PART;  // 64 KB
-constexpr int kSlots = 3;
-constexpr int kABuf = 2;
-constexpr int kAhead = kSlots - kABuf;
+constexpr int B_BYTES = 2 * B_PART;         // a B slot: 32 KB
+constexpr int kASlots = 4;                  // A tiles in flight (freed once split)
+constexpr int kBSlots = 2;                  // B tiles (freed once multiplied)
+constexpr int B_OFF = kASlots * A_BYTES;
 constexpr int kMaxBlocks = 512;             // blocks of one leaf row (table in shared memory)
-constexpr int TAB_OFF = kSlots * SLOT;
+constexpr int TAB_OFF = B_OFF + kBSlots * B_BYTES;
 constexpr int SMEM_BYTES = TAB_OFF + kMaxBlocks * (int)sizeof(LeafBlock);
 constexpr uint32_t IDESC_HL = tc::idesc_tf32(128, 2 * NB);  // A_hi [B_hi | B_lo]
 constexpr uint32_t IDESC_LH = tc::idesc_tf32(128, NB);      // A_lo B_hi
-// tensor memory (512 columns): accumulator set b at 256 b -- [HH | X1]
-// (N = 128) then X2 at + 128 (N = 64); A_lo buffer b at 256 b + 192 (64)
-constexpr uint32_t TM_SET = 256;
+// tensor memory (512 columns): the accumulators [HH | X1] (N = 128) at 0 and
+// X2 (N = 64) at 128; A buffer b (hi 64, lo 64 columns) at 256 + 128 b
 constexpr uint32_t TM_X2 = 128;
-constexpr uint32_t TM_ALO = 192;
-constexpr int BAR_FULL = 0, BAR_EMPTY = kSlots, BAR_READY = 2 * kSlots, BAR_MPAR = BAR_READY + kABuf,
-              BAR_ACC = BAR_MPAR + kABuf, BAR_DRAIN = BAR_ACC + 2, NBAR = BAR_DRAIN + 2;
+constexpr uint32_t TM_A = 256;
+constexpr uint32_t TM_ASTRIDE = 128;
+constexpr int BAR_FULL = 0, BAR_EMPTY = kASlots, BAR_READY = 2 * kASlots, BAR_ACC = BAR_READY + 1,
+              BAR_DRAIN = BAR_ACC + 1, NBAR = BAR_DRAIN + 2;
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
-static_assert(64 * NR * 8 <= SLOT, "combine buffer fits a slot");
-
-// Shared-memory descriptor of a K-major operand in the 128-byte swizzled
-// layout the tensor copies write (8-row atoms of 1024 bytes; a K = 8 step
-// inside the 128-byte row advances the start address by 32 bytes).
-__device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr) {
-  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
-  d |= (uint64_t)1 << 16;             // leading byte offset 16 (unused by this layout)
-  d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset: 8 rows of 128 bytes
-  d |= (uint64_t)1 << 46;             // descriptor version
-  d |= (uint64_t)2 << 61;             // 128-byte swizzle
-  return d;
-}
+static_assert(64 * NR * 8 <= A_BYTES, "combine buffer fits an A slot");
 
 __device__ __forceinline__ bool aborted(const volatile int* flag) { return *flag != 0; }
 
@@ -1000,6 +988,14 @@ __global__ void k_row_blocks(const int32_t* __restrict__ leaf_off, NearOp nr,
 // The leaf level and the near field of leaf k = blockIdx.x, plus the level
 // sums of the levels above (Ynl, d >= 2); owner write of the leaf's rows in
 // the original order.
+//
+// Pipeline: the producer keeps up to kASlots A tiles in flight; the workers
+// split tile c into tensor memory (hi = the value itself, which the tensor
+// core reads as TF32, and lo = its remainder; A buffer c % 2), which frees
+// its shared-memory slot at once, write the low part of B, read back the
+// accumulators of chunk c - 1, copy B of chunk c + 1 into the B slot chunk
+// c - 1 used, and signal "ready"; the issuers multiply chunk c into the one
+// accumulator set.
 __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
     const int32_t* __restrict__ leaf_off, const LeafBlock* __restrict__ blocks,
     const int32_t* __restrict__ block_ptr, const CUtensorMap* __restrict__ rmaps,
@@ -1034,18 +1030,14 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
   if (tid < 32) tc::tmem_alloc(&tslot, kTmemCols);
   if (tid == 0) {
     abort_flag = 0;
-    for (int i = 0; i < lr::kSlots; ++i) {
+    for (int i = 0; i < lr::kASlots; ++i) {
       tc::mbar_init(&bar[lr::BAR_FULL + i], 1);
-      tc::mbar_init(&bar[lr::BAR_EMPTY + i], 2);
+      tc::mbar_init(&bar[lr::BAR_EMPTY + i], WORKERS / 32);
     }
-    for (int i = 0; i < lr::kABuf; ++i) {
-      tc::mbar_init(&bar[lr::BAR_READY + i], WORKERS / 32);
-      tc::mbar_init(&bar[lr::BAR_MPAR + i], 2);
-    }
-    for (int i = 0; i < 2; ++i) {
-      tc::mbar_init(&bar[lr::BAR_ACC + i], 2);
-      tc::mbar_init(&bar[lr::BAR_DRAIN + i], 1);
-    }
+    tc::mbar_init(&bar[lr::BAR_READY], WORKERS / 32);
+    tc::mbar_init(&bar[lr::BAR_ACC], 2);
+    tc::mbar_init(&bar[lr::BAR_DRAIN], 1);
+    tc::mbar_init(&bar[lr::BAR_DRAIN + 1], 1);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   tc::fence_before_sync();
@@ -1060,12 +1052,13 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
     if ((tid & 31) == 0) {
       int issued = 0;
       for (int c = 0; c < nch; ++c) {
-        const int s = c % lr::kSlots;
-        if (c >= lr::kSlots && !tc::mbar_wait_sleep(&bar[lr::BAR_EMPTY + s], (uint32_t)(((c / lr::kSlots) - 1) & 1),
-                                                kWaitLimit, kWaitHintNs))
+        const int s = c % lr::kASlots;
+        if (c >= lr::kASlots &&
+            !tc::mbar_wait_sleep(&bar[lr::BAR_EMPTY + s], (uint32_t)(((c / lr::kASlots) - 1) & 1),
+                                 kWaitLimit, kWaitHintNs))
           lr::give_up(err, abortp);
         if (lr::aborted(abortp)) break;
-        unsigned char* a = smem + s * lr::SLOT;
+        unsigned char* a = smem + s * lr::A_BYTES;
         const LeafBlock bt = it[2 * c];
         const bool hb = 2 * c + 1 < nit;
         const int xb = hb ? it[2 * c + 1].x0 : 0, yb = hb ? 0 : 64;
@@ -1077,42 +1070,29 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
         ++issued;
       }
       // copies in flight land before the block exits (bounded)
-      for (int c = issued > lr::kSlots ? issued - lr::kSlots : 0; c < issued; ++c)
-        if (!tc::mbar_wait_sleep(&bar[lr::BAR_FULL + c % lr::kSlots], (uint32_t)((c / lr::kSlots) & 1), kWaitLimit,
-                                 kWaitHintNs))
+      for (int c = issued > lr::kASlots ? issued - lr::kASlots : 0; c < issued; ++c)
+        if (!tc::mbar_wait_sleep(&bar[lr::BAR_FULL + c % lr::kASlots], (uint32_t)((c / lr::kASlots) & 1),
+                                 kWaitLimit, kWaitHintNs))
           lr::give_up(err, abortp);
     }
   } else if (tid >= ISSUER0) {
     // issuers (lane 0 of warps 16 and 17): A_hi [B_hi | B_lo] -> [HH | X1],
-    // A_lo B_hi -> X2
+    // A_lo B_hi -> X2, A from tensor memory
     if ((tid & 31) == 0) {
       const bool second = tid >= ISSUER0 + 32;
-      int c = 0;
-      for (; c < nch; ++c) {
-        if (!tc::mbar_wait_sleep(&bar[lr::BAR_READY + c % lr::kABuf], (uint32_t)((c / lr::kABuf) & 1), kWaitLimit,
-                                 kWaitHintNs))
+      for (int c = 0; c < nch; ++c) {
+        if (!tc::mbar_wait_sleep(&bar[lr::BAR_READY], (uint32_t)(c & 1), kWaitLimit, kWaitHintNs))
           lr::give_up(err, abortp);
         if (lr::aborted(abortp)) break;
         tc::fence_after_sync();
-        const uint32_t set = tmem + lr::TM_SET * (uint32_t)(c & 1);
-        unsigned char* slot = smem + (c % lr::kSlots) * lr::SLOT;
-        const uint64_t bd = tc::make_desc(tc::smem_addr(slot + lr::A_BYTES), 128, lr::KC * 32);
-        if (!second) {
-          const uint32_t a0 = tc::smem_addr(slot);
+        const uint64_t bd =
+            tc::make_desc(tc::smem_addr(smem + lr::B_OFF + (c % lr::kBSlots) * lr::B_BYTES), 128, lr::KC * 32);
+        const uint32_t ab = tmem + lr::TM_A + lr::TM_ASTRIDE * (uint32_t)(c & 1) + (second ? 64u : 0u);
 #pragma unroll
-          for (int ks = 0; ks < lr::KC / 8; ++ks)
-            tc::mma_tf32(set, lr::desc_sw128(a0 + (uint32_t)((ks >> 2) * lr::A_HALF + (ks & 3) * 32)),
-                         bd + (uint64_t)((ks * 256) >> 4), lr::IDESC_HL, ks > 0 ? 1u : 0u);
-        } else {
-          const uint32_t alo = tmem + lr::TM_SET * (uint32_t)(c % lr::kABuf) + lr::TM_ALO;
-#pragma unroll
-          for (int ks = 0; ks < lr::KC / 8; ++ks)
-            tc::mma_tf32_ta(set + lr::TM_X2, alo + 8u * ks, bd + (uint64_t)((ks * 256) >> 4), lr::IDESC_LH,
-                            ks > 0 ? 1u : 0u);
-        }
-        tc::mma_commit(&bar[lr::BAR_MPAR + c % lr::kABuf]);
-        tc::mma_commit(&bar[lr::BAR_EMPTY + c % lr::kSlots]);
-        tc::mma_commit(&bar[lr::BAR_ACC + (c & 1)]);
+        for (int ks = 0; ks < lr::KC / 8; ++ks)
+          tc::mma_tf32_ta(tmem + (second ? lr::TM_X2 : 0u), ab + 8u * ks, bd + (uint64_t)((ks * 256) >> 4),
+                          second ? lr::IDESC_LH : lr::IDESC_HL, ks > 0 ? 1u : 0u);
+        tc::mma_commit(&bar[lr::BAR_ACC]);
       }
       // the products issued so far complete before the block frees tensor memory
       tc::mma_commit(&bar[lr::BAR_DRAIN + (second ? 1 : 0)]);
@@ -1128,17 +1108,17 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
     const bool bottom = (w & 3) >= 2;  // rows 64..127: warp-uniform
     const uint32_t lane_base = ((uint32_t)(w & 3) * 32u) << 16;
     const int bcol = tid >> 4, bk = 4 * (tid & 15);
-    const uint32_t boff_top = lr::A_BYTES + tc::kmajor_off(bcol, bk, lr::KC);
-    const uint32_t boff_bot = lr::A_BYTES + tc::kmajor_off(bcol + NR, bk, lr::KC);
+    const uint32_t boff_top = tc::kmajor_off(bcol, bk, lr::KC);
+    const uint32_t boff_bot = tc::kmajor_off(bcol + NR, bk, lr::KC);
     float sum[NCOL], comp[NCOL], cross[NCOL];
 #pragma unroll
     for (int j = 0; j < NCOL; ++j) sum[j] = comp[j] = cross[j] = 0.f;
 
     auto load_b = [&](int c) {
-      unsigned char* slot = smem + (c % lr::kSlots) * lr::SLOT;
+      unsigned char* bs = smem + lr::B_OFF + (c % lr::kBSlots) * lr::B_BYTES;
       const LeafBlock bt = it[2 * c];
       const bool okt = bk < bt.len;
-      cp_async16(slot + boff_top, okt ? Xt + (int64_t)bcol * N + bt.src_off + bk : Xt, okt);
+      cp_async16(bs + boff_top, okt ? Xt + (int64_t)bcol * N + bt.src_off + bk : Xt, okt);
       bool okb = false;
       const float* srcb = Xt;
       if (2 * c + 1 < nit) {
@@ -1146,16 +1126,16 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
         okb = bk < bb.len;
         if (okb) srcb = Xt + (int64_t)bcol * N + bb.src_off + bk;
       }
-      cp_async16(slot + boff_bot, srcb, okb);
+      cp_async16(bs + boff_bot, srcb, okb);
+      cp_async_commit();
     };
     auto read = [&](int c) {
-      const uint32_t set = tmem + lr::TM_SET * (uint32_t)(c & 1) + (bottom ? (uint32_t)NR : 0u) +
-                           (uint32_t)(NCOL * kq) + lane_base;
-      if (!tc::mbar_wait_sleep(&bar[lr::BAR_ACC + (c & 1)], (uint32_t)((c >> 1) & 1), kWaitLimit, kWaitHintNs))
+      const uint32_t acc = tmem + (bottom ? (uint32_t)NR : 0u) + (uint32_t)(NCOL * kq) + lane_base;
+      if (!tc::mbar_wait_sleep(&bar[lr::BAR_ACC], (uint32_t)(c & 1), kWaitLimit, kWaitHintNs))
         lr::give_up(err, abortp);
       tc::fence_after_sync();
       float hh[NCOL], x1[NCOL], x2[NCOL];
-      lr::tmem_ld8x3(set, set + (uint32_t)lr::NB, set + lr::TM_X2, hh, x1, x2);
+      lr::tmem_ld8x3(acc, acc + (uint32_t)lr::NB, acc + lr::TM_X2, hh, x1, x2);
       tc::fence_before_sync();
 #pragma unroll
       for (int j = 0; j < NCOL; ++j) {
@@ -1164,46 +1144,47 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
       }
     };
 
-    int nload = 0;
-    for (; nload < lr::kAhead && nload < nch; ++nload) load_b(nload);
-    cp_async_commit();
+    if (nch > 0) load_b(0);
     int c = 0;
     for (; c < nch; ++c) {
-      const int s = c % lr::kSlots;
-      // chunk c - lr::kABuf multiplied: its tensor-memory A_lo buffer (this
-      // chunk's) and its slot (refilled with B below) are free
-      if (c >= lr::kABuf && !tc::mbar_wait_sleep(&bar[lr::BAR_MPAR + c % lr::kABuf], (uint32_t)(((c / lr::kABuf) - 1) & 1),
-                                            kWaitLimit, kWaitHintNs))
+      const int s = c % lr::kASlots;
+      if (!tc::mbar_wait_sleep(&bar[lr::BAR_FULL + s], (uint32_t)((c / lr::kASlots) & 1), kWaitLimit,
+                               kWaitHintNs))
         lr::give_up(err, abortp);
       if (lr::aborted(abortp)) break;
-      if (nload < nch) {
-        load_b(nload);
-        ++nload;
-      }
-      cp_async_commit();
-      cp_async_wait<lr::kAhead>();
-      if (!tc::mbar_wait_sleep(&bar[lr::BAR_FULL + s], (uint32_t)((c / lr::kSlots) & 1), kWaitLimit, kWaitHintNs))
-        lr::give_up(err, abortp);
-      if (lr::aborted(abortp)) break;
-      unsigned char* slot = smem + s * lr::SLOT;
       {
-        // A_lo of 16 K values of row R, from the swizzled tile of its K half
-        const unsigned char* sa = slot + (kq >> 1) * lr::A_HALF + (uint32_t)R * 128u;
-        float lo[16];
+        // row R, 16 K values, from the swizzled tile of its K half: hi (the
+        // value itself) and lo into A buffer c % 2, whose last reader (chunk
+        // c - 2) is complete (its accumulators were read back)
+        const unsigned char* sa = smem + s * lr::A_BYTES + (kq >> 1) * lr::A_HALF + (uint32_t)R * 128u;
+        float hi[16], lo[16];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           const int qq = 4 * (kq & 1) + j;
           const float4 x = *reinterpret_cast<const float4*>(sa + ((uint32_t)(qq ^ (R & 7)) << 4));
+          hi[4 * j] = x.x;
+          hi[4 * j + 1] = x.y;
+          hi[4 * j + 2] = x.z;
+          hi[4 * j + 3] = x.w;
           lo[4 * j] = x.x - tf32_rz(x.x);
           lo[4 * j + 1] = x.y - tf32_rz(x.y);
           lo[4 * j + 2] = x.z - tf32_rz(x.z);
           lo[4 * j + 3] = x.w - tf32_rz(x.w);
         }
-        tc::tmem_st16(tmem + lr::TM_SET * (uint32_t)(c % lr::kABuf) + lr::TM_ALO + 16u * kq + lane_base, lo);
-        // low parts of this thread's two B segments, next to B_hi
+        const uint32_t ta = tmem + lr::TM_A + lr::TM_ASTRIDE * (uint32_t)(c & 1) + 16u * kq + lane_base;
+        tc::tmem_st16(ta, hi);
+        tc::tmem_st16(ta + 64u, lo);
+      }
+      // the A slot is free once every worker warp has read its rows
+      __syncwarp();
+      if ((tid & 31) == 0) tc::mbar_arrive(&bar[lr::BAR_EMPTY + s]);
+      {
+        // low parts of this thread's two B segments of chunk c, next to B_hi
+        cp_async_wait<0>();
+        unsigned char* bs = smem + lr::B_OFF + (c % lr::kBSlots) * lr::B_BYTES;
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-          unsigned char* sb = slot + (h ? boff_bot : boff_top);
+          unsigned char* sb = bs + (h ? boff_bot : boff_top);
           const float4 xb = *reinterpret_cast<const float4*>(sb);
           float4 lb;
           lb.x = xb.x - tf32_rz(xb.x);
@@ -1212,18 +1193,21 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
           lb.w = xb.w - tf32_rz(xb.w);
           *reinterpret_cast<float4*>(sb + lr::B_PART) = lb;
         }
-        tc::tmem_wait_st();
       }
+      tc::tmem_wait_st();
+      // chunk c - 1's accumulators back (the products of chunk c overwrite
+      // them), then B of chunk c + 1 into the slot chunk c - 1 read
+      if (c >= 1) read(c - 1);
+      if (c + 1 < nch) load_b(c + 1);
       tc::fence_async_smem();
       tc::fence_before_sync();
       __syncwarp();
-      if ((tid & 31) == 0) tc::mbar_arrive(&bar[lr::BAR_READY + c % lr::kABuf]);
-      if (c >= 1) read(c - 1);
+      if ((tid & 31) == 0) tc::mbar_arrive(&bar[lr::BAR_READY]);
     }
     if (c == nch && nch > 0) read(nch - 1);
     cp_async_wait<0>();
     // combine the halves: the bottom rows' sums go through shared memory
-    // (slot 0, free once every worker is past its last chunk)
+    // (A slot 0, free once every worker is past its last chunk)
     lr::workers_sync();
     double v[NCOL];
 #pragma unroll
