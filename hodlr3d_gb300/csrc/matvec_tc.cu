@@ -53,7 +53,9 @@
 // matches an FP64 sum here at a fraction of the cost of GB300's FP64 units)
 // and its cross parts with plain FP32 additions.
 //
-// Every mbarrier wait is bounded; a wait that gives up sets the error flag.
+// Every mbarrier wait is bounded; a wait that gives up sets the error flag and
+// the block's abort flag, after which no role issues new copies or products
+// and the block drains those in flight (bounded) before it exits.
 #include <cuda.h>
 
 #include <algorithm>
@@ -101,7 +103,8 @@ constexpr int BAR_EMPTY = kSlots;          // [kSlots] slot no longer read (issu
 constexpr int BAR_READY = 2 * kSlots;      // [kABuf] chunk c % kABuf split (one arrival per worker warp)
 constexpr int BAR_MPAR = BAR_READY + kABuf;  // [kABuf] chunk c % kABuf multiplied (issuer commits)
 constexpr int BAR_ACC = BAR_MPAR + kABuf;  // [2] accumulator set complete (issuer commits)
-constexpr int NBAR = BAR_ACC + 2;
+constexpr int BAR_DRAIN = BAR_ACC + 2;     // [2] an issuer's products in flight completed
+constexpr int NBAR = BAR_DRAIN + 2;
 
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
 static_assert(TM_A + TM_ASTRIDE * kABuf <= kTmemCols, "tensor memory");
@@ -181,8 +184,19 @@ static_assert(sizeof(PairRow) == ENTRY_BYTES, "entry");
 // every worker calls src.finish(tile, sum, comp, cross) once a tile's
 // products are summed (the tile's value is (sum - comp) + cross).  Returns the
 // number of chunks.
+//
+// A bounded wait that gives up sets the error flag and *abortp: every role
+// then stops issuing copies and products, the issuers wait (bounded) for
+// their products in flight and the producer for its copies in flight, and
+// no tile is finished, before the block frees its tensor memory.
+__device__ __forceinline__ void stream_give_up(int* err, volatile int* abortp) {
+  atomicExch(err, 1);
+  *abortp = 1;
+}
+
 template <class Src>
-__device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t tmem, int* err) {
+__device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t tmem, int* err,
+                          volatile int* abortp) {
   const int tid = threadIdx.x;
   const int cpt = src.cpt, nch = src.ntile * src.cpt;
   if (nch <= 0) return 0;
@@ -190,14 +204,23 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
   if (tid >= PRODUCER) {
     // producer warp: lane 0 waits for the slot; the lanes issue the copies
     const int lane = tid & 31;
+    int issued = 0;
     for (int c = 0; c < nch; ++c) {
       const int s = c % kSlots;
       if (lane == 0 && c >= kSlots &&
           !tc::mbar_wait_sleep(&bar[BAR_EMPTY + s], (uint32_t)(((c / kSlots) - 1) & 1), kWaitLimit, kWaitHintNs))
-        atomicExch(err, 1);
+        stream_give_up(err, abortp);
       __syncwarp();
+      if (*abortp) break;
       src.produce(c, smem + s * SLOT_BYTES, &bar[BAR_FULL + s], lane);
+      ++issued;
     }
+    // copies in flight land before the block exits (bounded)
+    if (lane == 0)
+      for (int c = issued > kSlots ? issued - kSlots : 0; c < issued; ++c)
+        if (!tc::mbar_wait_sleep(&bar[BAR_FULL + c % kSlots], (uint32_t)((c / kSlots) & 1), kWaitLimit,
+                                 kWaitHintNs))
+          stream_give_up(err, abortp);
     return nch;
   }
 
@@ -210,7 +233,8 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
       const bool close = ct == cpt - 1 || gk == kGroupChunks - 1;
       const int buf = g & 1;
       if (!tc::mbar_wait_sleep(&bar[BAR_READY + c % kABuf], (uint32_t)((c / kABuf) & 1), kWaitLimit, kWaitHintNs))
-        atomicExch(err, 1);
+        stream_give_up(err, abortp);
+      if (*abortp) break;
       tc::fence_after_sync();
       const uint32_t ab = tmem + TM_A + TM_ASTRIDE * (uint32_t)(c % kABuf) + (second ? (uint32_t)KC : 0u);
       const uint32_t d = tmem + TM_ACC * (uint32_t)buf + (second ? 64u : 0u);
@@ -231,6 +255,10 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
       }
       ct = ct == cpt - 1 ? 0 : ct + 1;
     }
+    // the products issued so far complete before the block frees tensor memory
+    tc::mma_commit(&bar[BAR_DRAIN + (second ? 1 : 0)]);
+    if (!tc::mbar_wait_sleep(&bar[BAR_DRAIN + (second ? 1 : 0)], 0u, kWaitLimit, kWaitHintNs))
+      stream_give_up(err, abortp);
     return nch;
   }
 
@@ -266,7 +294,7 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
   auto read = [&](int g) {
     const uint32_t base = tmem + TM_ACC * (uint32_t)(g & 1) + (uint32_t)(NCOL * kq) + lane_base;
     if (!tc::mbar_wait_sleep(&bar[BAR_ACC + (g & 1)], (uint32_t)((g >> 1) & 1), kWaitLimit, kWaitHintNs))
-      atomicExch(err, 1);
+      stream_give_up(err, abortp);
     tc::fence_after_sync();
     float hh[NCOL], x1[NCOL], x2[NCOL];
     tc::tmem_ld8(base, hh);
@@ -288,7 +316,8 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
     // tensor-memory A buffer (this chunk's) are free
     if (c >= kABuf && !tc::mbar_wait_sleep(&bar[BAR_MPAR + c % kABuf],
                                      (uint32_t)(((c / kABuf) - 1) & 1), kWaitLimit, kWaitHintNs))
-      atomicExch(err, 1);
+      stream_give_up(err, abortp);
+    if (*abortp) break;
     if (nload < nch) {
       src.load_b(nload, smem + (nload % kSlots) * SLOT_BYTES, m);
       ++nload;
@@ -296,7 +325,8 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
     cp_async_commit();
     cp_async_wait<kAhead>();
     if (!tc::mbar_wait_sleep(&bar[BAR_FULL + s], (uint32_t)((c / kSlots) & 1), kWaitLimit, kWaitHintNs))
-      atomicExch(err, 1);
+      stream_give_up(err, abortp);
+    if (*abortp) break;
 
     unsigned char* slot = smem + s * SLOT_BYTES;
     {
@@ -344,6 +374,7 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
     if (close) {
       if (pend) {
         read(g - 1);
+        if (*abortp) break;
         if (pend_tile != tile) {
           src.finish(pend_tile, sum, comp, cross);
 #pragma unroll
@@ -364,8 +395,10 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
       ++ct;
     }
   }
-  read(g - 1);
-  src.finish(pend_tile, sum, comp, cross);
+  if (!*abortp) {
+    read(g - 1);
+    if (!*abortp) src.finish(pend_tile, sum, comp, cross);
+  }
   cp_async_wait<0>();
   return nch;
 }
@@ -377,9 +410,12 @@ __device__ __forceinline__ bool smem_misaligned(const unsigned char* smem, int* 
   return true;
 }
 
-__device__ __forceinline__ uint32_t block_setup(uint64_t* bar, uint32_t* tslot) {
+__device__ __forceinline__ uint32_t block_setup(uint64_t* bar, uint32_t* tslot, int* abort_flag) {
   if (threadIdx.x < 32) tc::tmem_alloc(tslot, kTmemCols);
   if (threadIdx.x == 0) {
+    *abort_flag = 0;
+    tc::mbar_init(&bar[BAR_DRAIN], 1);
+    tc::mbar_init(&bar[BAR_DRAIN + 1], 1);
     for (int i = 0; i < kSlots; ++i) {
       tc::mbar_init(&bar[BAR_FULL + i], 1);
       tc::mbar_init(&bar[BAR_EMPTY + i], 2);
@@ -619,7 +655,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_ta_tc(FarOp op, const CUtensorMa
   __syncthreads();
   const int ntiles_all = lv[1][nlev];
   if ((int)blockIdx.y >= ntiles_all) return;
-  const uint32_t tmem = block_setup(bar, &tslot);
+  __shared__ int abort_flag;
+  const uint32_t tmem = block_setup(bar, &tslot, &abort_flag);
   SrcTa src;
   src.tab = tab;
   src.cum = cum;
@@ -634,7 +671,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_ta_tc(FarOp op, const CUtensorMa
   src.cpt = (kin + KC - 1) / KC;
   src.b = Xt + i0;
   src.bs = N;
-  run_stream(src, smem, bar, tmem, err);
+  run_stream(src, smem, bar, tmem, err, &abort_flag);
   block_teardown(tmem);
 }
 
@@ -768,7 +805,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_ut_tc(FarOp op, const CUtensorMa
   }
   __syncthreads();
   warp0_scan(n, [&](int i) { return (items[i].blen + KC - 1) / KC; }, cofs);
-  const uint32_t tmem = block_setup(bar, &tslot);
+  __shared__ int abort_flag;
+  const uint32_t tmem = block_setup(bar, &tslot, &abort_flag);
   SrcUt src;
   src.items = items;
   src.cofs = cofs;
@@ -779,7 +817,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_ut_tc(FarOp op, const CUtensorMa
   src.ynl = Ynl;
   src.N = N;
   src.r0 = r0;
-  if (run_stream(src, smem, bar, tmem, err) == 0 && threadIdx.x < WORKERS) {
+  if (run_stream(src, smem, bar, tmem, err, &abort_flag) == 0 && threadIdx.x < WORKERS) {
     float z[NCOL] = {};
     src.finish(0, z, z, z);
   }
