@@ -932,8 +932,11 @@ constexpr int NB = 2 * NR;                  // B columns: top and bottom right-h
 constexpr int A_HALF = 128 * 32 * 4;        // one K half of A (rows 0..127, 32 K): 16 KB
 constexpr int A_BOX = 64 * 32 * 4;          // one 64-row box: 8 KB
 constexpr int A_BYTES = 2 * A_HALF;         // an A slot: 32 KB
-constexpr int B_PART = NB * KC * 4;         // B_hi (n 0..63) or B_lo (n 64..127): 16 KB
-constexpr int B_BYTES = 2 * B_PART;         // a B slot: 32 KB
+// B in the 128-byte swizzled K-major layout, per K half 128 rows (n 0..63
+// B_hi, 64..127 B_lo) of 128 bytes: 16 KB; its low part 64 rows below
+constexpr int B_HALF = 2 * NB * 32 * 4;
+constexpr int B_LO = NB * 128;
+constexpr int B_BYTES = 2 * B_HALF;         // a B slot: 32 KB
 constexpr int kASlots = 4;                  // A tiles in flight (freed once split)
 constexpr int kBSlots = 2;                  // B tiles (freed once multiplied)
 constexpr int B_OFF = kASlots * A_BYTES;
@@ -951,6 +954,24 @@ constexpr int BAR_FULL = 0, BAR_EMPTY = kASlots, BAR_READY = 2 * kASlots, BAR_AC
               BAR_DRAIN = BAR_ACC + 1, NBAR = BAR_DRAIN + 2;
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
 static_assert(64 * NR * 8 <= A_BYTES, "combine buffer fits an A slot");
+
+// Shared-memory descriptor of a K-major operand in the 128-byte swizzled
+// layout (8-row atoms of 1024 bytes; a K = 8 step inside the 128-byte row
+// advances the start address by 32 bytes).
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;             // leading byte offset 16 (unused by this layout)
+  d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset: 8 rows of 128 bytes
+  d |= (uint64_t)1 << 46;             // descriptor version
+  d |= (uint64_t)2 << 61;             // 128-byte swizzle
+  return d;
+}
+
+// byte offset of the 16-byte chunk (row n, K values 4 kc .. 4 kc + 3) in a
+// 128-byte swizzled K-major tile whose K halves (32 values) are half apart
+__device__ __forceinline__ uint32_t sw128_off(int n, int kc, int half) {
+  return (uint32_t)((kc >> 3) * half + n * 128 + (((kc & 7) ^ (n & 7)) << 4));
+}
 
 __device__ __forceinline__ bool aborted(const volatile int* flag) { return *flag != 0; }
 
@@ -1123,12 +1144,12 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
           lr::give_up(err, abortp);
         if (lr::aborted(abortp)) break;
         tc::fence_after_sync();
-        const uint64_t bd =
-            tc::make_desc(tc::smem_addr(smem + lr::B_OFF + (c % lr::kBSlots) * lr::B_BYTES), 128, lr::KC * 32);
+        const uint32_t b0 = tc::smem_addr(smem + lr::B_OFF + (c % lr::kBSlots) * lr::B_BYTES);
         const uint32_t ab = tmem + lr::TM_A + lr::TM_ASTRIDE * (uint32_t)(c & 1) + (second ? 64u : 0u);
 #pragma unroll
         for (int ks = 0; ks < lr::KC / 8; ++ks)
-          tc::mma_tf32_ta(tmem + (second ? lr::TM_X2 : 0u), ab + 8u * ks, bd + (uint64_t)((ks * 256) >> 4),
+          tc::mma_tf32_ta(tmem + (second ? lr::TM_X2 : 0u), ab + 8u * ks,
+                          lr::desc_sw128(b0 + (uint32_t)((ks >> 2) * lr::B_HALF + (ks & 3) * 32)),
                           second ? lr::IDESC_LH : lr::IDESC_HL, ks > 0 ? 1u : 0u);
         tc::mma_commit(&bar[lr::BAR_ACC]);
       }
@@ -1145,9 +1166,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
     const int w = tid >> 5, kq = w >> 2, R = tid & 127;
     const bool bottom = (w & 3) >= 2;  // rows 64..127: warp-uniform
     const uint32_t lane_base = ((uint32_t)(w & 3) * 32u) << 16;
+    // B copies: 16 consecutive threads read 256 contiguous bytes of one
+    // column; 8 of them write one 128-byte swizzled row (no bank conflicts)
     const int bcol = tid >> 4, bk = 4 * (tid & 15);
-    const uint32_t boff_top = tc::kmajor_off(bcol, bk, lr::KC);
-    const uint32_t boff_bot = tc::kmajor_off(bcol + NR, bk, lr::KC);
+    const uint32_t boff_top = lr::sw128_off(bcol, tid & 15, lr::B_HALF);
+    const uint32_t boff_bot = lr::sw128_off(bcol + NR, tid & 15, lr::B_HALF);
     float sum[NCOL], comp[NCOL], cross[NCOL];
 #pragma unroll
     for (int j = 0; j < NCOL; ++j) sum[j] = comp[j] = cross[j] = 0.f;
@@ -1229,7 +1252,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
           lb.y = xb.y - tf32_rz(xb.y);
           lb.z = xb.z - tf32_rz(xb.z);
           lb.w = xb.w - tf32_rz(xb.w);
-          *reinterpret_cast<float4*>(sb + lr::B_PART) = lb;
+          *reinterpret_cast<float4*>(sb + lr::B_LO) = lb;
         }
       }
       tc::tmem_wait_st();
