@@ -77,6 +77,8 @@ constexpr int THREADS = WORKERS + 96;
 constexpr int A_HALF = 128 * 32 * 4;       // one 32-wide box of A (16 KB)
 constexpr int A_BYTES = 2 * A_HALF;        // A chunk (32 KB)
 constexpr int B_BYTES = NR * KC * 4;       // one TF32 part of a B chunk (8 KB)
+constexpr int B_HALF = 2 * NR * 128;       // B hi and lo rows of one K half (8 KB)
+constexpr int B_LO = NR * 128;             // B_lo rows below B_hi in each K half
 constexpr int SLOT_BYTES = A_BYTES + 2 * B_BYTES;  // slot: A, B hi, B lo
 constexpr int kSlots = 4;
 constexpr int kABuf = 2;                   // tensor-memory A buffers (chunks multiplied ahead)
@@ -145,8 +147,30 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
-// This worker's B copy: k quad qb of column cb to offB of the slot (its low
-// part goes to offB + B_BYTES).
+// Shared-memory descriptor of a K-major operand in the 128-byte swizzled
+// layout (8-row atoms of 1024 bytes, each row 32 K values of 128 bytes whose
+// 16-byte chunk j sits at chunk j ^ (row % 8)); a K = 8 step inside the row
+// advances the start address by 32 bytes.  The tensor copies of A write this
+// layout; the workers write B in it, which keeps their 16-byte shared-memory
+// accesses free of bank conflicts.
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;             // leading byte offset 16 (unused by this layout)
+  d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset: 8 rows of 128 bytes
+  d |= (uint64_t)1 << 46;             // descriptor version
+  d |= (uint64_t)2 << 61;             // 128-byte swizzle
+  return d;
+}
+
+// byte offset of the 16-byte chunk (row n, K values 4 kc .. 4 kc + 3) in a
+// 128-byte swizzled K-major tile whose K halves (32 values) are `half` apart
+__device__ __forceinline__ uint32_t sw128_off(int n, int kc, int half) {
+  return (uint32_t)((kc >> 3) * half + n * 128 + (((kc & 7) ^ (n & 7)) << 4));
+}
+
+// This worker's B copy: k quad qb of column cb to offB of the slot, in the
+// 128-byte swizzled layout (B_hi rows 0..31, B_lo rows 32..63 of each K half);
+// its low part goes to offB + B_LO.
 struct CopyMap {
   int cb, qb;
   uint32_t offB;
@@ -238,12 +262,11 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
       tc::fence_after_sync();
       const uint32_t ab = tmem + TM_A + TM_ASTRIDE * (uint32_t)(c % kABuf) + (second ? (uint32_t)KC : 0u);
       const uint32_t d = tmem + TM_ACC * (uint32_t)buf + (second ? 64u : 0u);
-      const uint64_t bd =
-          tc::make_desc(tc::smem_addr(smem + (c % kSlots) * SLOT_BYTES + A_BYTES), 128, KC * 32);
+      const uint32_t b0 = tc::smem_addr(smem + (c % kSlots) * SLOT_BYTES + A_BYTES);
 #pragma unroll
       for (int ks = 0; ks < KC / 8; ++ks)
-        tc::mma_tf32_ta(d, ab + 8u * ks, bd + (uint64_t)((ks * 256) >> 4), second ? IDESC32 : IDESC64,
-                        (gk > 0 || ks > 0) ? 1u : 0u);
+        tc::mma_tf32_ta(d, ab + 8u * ks, desc_sw128(b0 + (uint32_t)((ks >> 2) * B_HALF + (ks & 3) * 32)),
+                        second ? IDESC32 : IDESC64, (gk > 0 || ks > 0) ? 1u : 0u);
       tc::mma_commit(&bar[BAR_MPAR + c % kABuf]);
       tc::mma_commit(&bar[BAR_EMPTY + c % kSlots]);
       if (close) {
@@ -267,9 +290,11 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
   // kq = w / 4; each copies B's k quad qb of column cb.
   const int w = tid >> 5, lane = tid & 31, kq = w >> 2;
   CopyMap m;
-  m.cb = 8 * (tid >> 7) + ((tid >> 2) & 7);
-  m.qb = 4 * ((tid >> 5) & 3) + (tid & 3);
-  m.offB = A_BYTES + tc::kmajor_off(m.cb, 4 * m.qb, KC);
+  // 16 consecutive threads copy one column's 64 K values (256 contiguous
+  // bytes); 8 of them write one 128-byte swizzled row without bank conflicts
+  m.cb = tid >> 4;
+  m.qb = tid & 15;
+  m.offB = A_BYTES + sw128_off(m.cb, m.qb, B_HALF);
   const int R = tid & 127;
   const uint32_t lane_base = ((uint32_t)((tid >> 5) & 3) * 32u) << 16;
   // a warp whose 32 rows all lie at or past the tile's live rows (a 64-point
@@ -360,7 +385,7 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
         lb.y = xb.y - tf32_rz(xb.y);
         lb.z = xb.z - tf32_rz(xb.z);
         lb.w = xb.w - tf32_rz(xb.w);
-        *reinterpret_cast<float4*>(sb + B_BYTES) = lb;
+        *reinterpret_cast<float4*>(sb + B_LO) = lb;
       }
       tc::tmem_wait_st();
     }
@@ -955,24 +980,6 @@ constexpr int BAR_FULL = 0, BAR_EMPTY = kASlots, BAR_READY = 2 * kASlots, BAR_AC
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
 static_assert(64 * NR * 8 <= A_BYTES, "combine buffer fits an A slot");
 
-// Shared-memory descriptor of a K-major operand in the 128-byte swizzled
-// layout (8-row atoms of 1024 bytes; a K = 8 step inside the 128-byte row
-// advances the start address by 32 bytes).
-__device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr) {
-  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
-  d |= (uint64_t)1 << 16;             // leading byte offset 16 (unused by this layout)
-  d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset: 8 rows of 128 bytes
-  d |= (uint64_t)1 << 46;             // descriptor version
-  d |= (uint64_t)2 << 61;             // 128-byte swizzle
-  return d;
-}
-
-// byte offset of the 16-byte chunk (row n, K values 4 kc .. 4 kc + 3) in a
-// 128-byte swizzled K-major tile whose K halves (32 values) are half apart
-__device__ __forceinline__ uint32_t sw128_off(int n, int kc, int half) {
-  return (uint32_t)((kc >> 3) * half + n * 128 + (((kc & 7) ^ (n & 7)) << 4));
-}
-
 __device__ __forceinline__ bool aborted(const volatile int* flag) { return *flag != 0; }
 
 __device__ __forceinline__ void give_up(int* err, volatile int* flag) {
@@ -1149,7 +1156,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
 #pragma unroll
         for (int ks = 0; ks < lr::KC / 8; ++ks)
           tc::mma_tf32_ta(tmem + (second ? lr::TM_X2 : 0u), ab + 8u * ks,
-                          lr::desc_sw128(b0 + (uint32_t)((ks >> 2) * lr::B_HALF + (ks & 3) * 32)),
+                          desc_sw128(b0 + (uint32_t)((ks >> 2) * lr::B_HALF + (ks & 3) * 32)),
                           second ? lr::IDESC_LH : lr::IDESC_HL, ks > 0 ? 1u : 0u);
         tc::mma_commit(&bar[lr::BAR_ACC]);
       }
@@ -1169,8 +1176,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
     // B copies: 16 consecutive threads read 256 contiguous bytes of one
     // column; 8 of them write one 128-byte swizzled row (no bank conflicts)
     const int bcol = tid >> 4, bk = 4 * (tid & 15);
-    const uint32_t boff_top = lr::sw128_off(bcol, tid & 15, lr::B_HALF);
-    const uint32_t boff_bot = lr::sw128_off(bcol + NR, tid & 15, lr::B_HALF);
+    const uint32_t boff_top = sw128_off(bcol, tid & 15, lr::B_HALF);
+    const uint32_t boff_bot = sw128_off(bcol + NR, tid & 15, lr::B_HALF);
     float sum[NCOL], comp[NCOL], cross[NCOL];
 #pragma unroll
     for (int j = 0; j < NCOL; ++j) sum[j] = comp[j] = cross[j] = 0.f;
