@@ -75,15 +75,16 @@ constexpr int ISSUER0 = WORKERS;           // warps 16, 17: MMA issuers
 constexpr int PRODUCER = WORKERS + 64;     // warp 18: A copies
 constexpr int THREADS = WORKERS + 96;
 constexpr int A_HALF = 128 * 32 * 4;       // one 32-wide box of A (16 KB)
-constexpr int A_BYTES = 2 * A_HALF;        // A chunk (32 KB)
-constexpr int B_BYTES = NR * KC * 4;       // one TF32 part of a B chunk (8 KB)
+constexpr int A_BYTES = 2 * A_HALF;        // an A slot: one chunk (32 KB)
 constexpr int B_HALF = 2 * NR * 128;       // B hi and lo rows of one K half (8 KB)
 constexpr int B_LO = NR * 128;             // B_lo rows below B_hi in each K half
-constexpr int SLOT_BYTES = A_BYTES + 2 * B_BYTES;  // slot: A, B hi, B lo
-constexpr int kSlots = 4;
+constexpr int B_SLOT = 2 * B_HALF;         // a B slot: one chunk, hi and lo (16 KB)
+constexpr int kSlots = 4;                  // A ring: tiles in flight, freed once split
+constexpr int kBSlots = 4;                 // B ring: freed once multiplied
 constexpr int kABuf = 2;                   // tensor-memory A buffers (chunks multiplied ahead)
-constexpr int kAhead = kSlots - kABuf;     // B chunks in flight ahead of the split one
-constexpr int TAB_OFF = kSlots * SLOT_BYTES;
+constexpr int kAhead = kBSlots - kABuf;    // B chunks in flight ahead of the split one
+constexpr int B_RING = kSlots * A_BYTES;
+constexpr int TAB_OFF = B_RING + kBSlots * B_SLOT;
 constexpr int kMaxEntries = 768;           // table entries (pairs, near blocks) of one block
 constexpr int ENTRY_BYTES = 32;
 constexpr int SMEM_BYTES = TAB_OFF + kMaxEntries * ENTRY_BYTES + (kMaxEntries + 1) * 4;
@@ -101,7 +102,7 @@ constexpr uint32_t TM_ASTRIDE = 2 * KC;
 constexpr int kGroupChunks = 2;            // chunks per accumulation group (K = 128)
 // barriers
 constexpr int BAR_FULL = 0;                // [kSlots] A of the slot landed (producer, tx)
-constexpr int BAR_EMPTY = kSlots;          // [kSlots] slot no longer read (issuer commits)
+constexpr int BAR_EMPTY = kSlots;          // [kSlots] A slot split (one arrival per worker warp)
 constexpr int BAR_READY = 2 * kSlots;      // [kABuf] chunk c % kABuf split (one arrival per worker warp)
 constexpr int BAR_MPAR = BAR_READY + kABuf;  // [kABuf] chunk c % kABuf multiplied (issuer commits)
 constexpr int BAR_ACC = BAR_MPAR + kABuf;  // [2] accumulator set complete (issuer commits)
@@ -110,7 +111,8 @@ constexpr int NBAR = BAR_DRAIN + 2;
 
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
 static_assert(TM_A + TM_ASTRIDE * kABuf <= kTmemCols, "tensor memory");
-static_assert(SLOT_BYTES % 1024 == 0, "128-byte swizzled tiles start on 1024 bytes");
+static_assert(A_BYTES % 1024 == 0 && B_SLOT % 1024 == 0 && B_RING % 1024 == 0,
+              "128-byte swizzled tiles start on 1024 bytes");
 
 __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
   const float y = x - c;
@@ -236,7 +238,7 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
         stream_give_up(err, abortp);
       __syncwarp();
       if (*abortp) break;
-      src.produce(c, smem + s * SLOT_BYTES, &bar[BAR_FULL + s], lane);
+      src.produce(c, smem + s * A_BYTES, &bar[BAR_FULL + s], lane);
       ++issued;
     }
     // copies in flight land before the block exits (bounded)
@@ -262,13 +264,12 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
       tc::fence_after_sync();
       const uint32_t ab = tmem + TM_A + TM_ASTRIDE * (uint32_t)(c % kABuf) + (second ? (uint32_t)KC : 0u);
       const uint32_t d = tmem + TM_ACC * (uint32_t)buf + (second ? 64u : 0u);
-      const uint32_t b0 = tc::smem_addr(smem + (c % kSlots) * SLOT_BYTES + A_BYTES);
+      const uint32_t b0 = tc::smem_addr(smem + B_RING + (c % kBSlots) * B_SLOT);
 #pragma unroll
       for (int ks = 0; ks < KC / 8; ++ks)
         tc::mma_tf32_ta(d, ab + 8u * ks, desc_sw128(b0 + (uint32_t)((ks >> 2) * B_HALF + (ks & 3) * 32)),
                         second ? IDESC32 : IDESC64, (gk > 0 || ks > 0) ? 1u : 0u);
       tc::mma_commit(&bar[BAR_MPAR + c % kABuf]);
-      tc::mma_commit(&bar[BAR_EMPTY + c % kSlots]);
       if (close) {
         tc::mma_commit(&bar[BAR_ACC + buf]);
         ++g;
@@ -294,7 +295,7 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
   // bytes); 8 of them write one 128-byte swizzled row without bank conflicts
   m.cb = tid >> 4;
   m.qb = tid & 15;
-  m.offB = A_BYTES + sw128_off(m.cb, m.qb, B_HALF);
+  m.offB = sw128_off(m.cb, m.qb, B_HALF);
   const int R = tid & 127;
   const uint32_t lane_base = ((uint32_t)((tid >> 5) & 3) * 32u) << 16;
   // a warp whose 32 rows all lie at or past the tile's live rows (a 64-point
@@ -310,7 +311,7 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
   int nload = 0;
   for (int i = 0; i < kAhead; ++i) {
     if (nload < nch) {
-      src.load_b(nload, smem + (nload % kSlots) * SLOT_BYTES, m);
+      src.load_b(nload, smem + B_RING + (nload % kBSlots) * B_SLOT, m);
       ++nload;
     }
     cp_async_commit();
@@ -337,14 +338,14 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
   bool pend = false;
   for (int c = 0; c < nch; ++c) {
     const int s = c % kSlots;
-    // chunk c - kABuf multiplied: its slot (refilled with B below) and its
+    // chunk c - kABuf multiplied: its B slot (refilled with B below) and its
     // tensor-memory A buffer (this chunk's) are free
     if (c >= kABuf && !tc::mbar_wait_sleep(&bar[BAR_MPAR + c % kABuf],
                                      (uint32_t)(((c / kABuf) - 1) & 1), kWaitLimit, kWaitHintNs))
       stream_give_up(err, abortp);
     if (*abortp) break;
     if (nload < nch) {
-      src.load_b(nload, smem + (nload % kSlots) * SLOT_BYTES, m);
+      src.load_b(nload, smem + B_RING + (nload % kBSlots) * B_SLOT, m);
       ++nload;
     }
     cp_async_commit();
@@ -353,7 +354,8 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
       stream_give_up(err, abortp);
     if (*abortp) break;
 
-    unsigned char* slot = smem + s * SLOT_BYTES;
+    unsigned char* slot = smem + s * A_BYTES;
+    unsigned char* bslot = smem + B_RING + (c % kBSlots) * B_SLOT;
     {
       // the row this thread owns, from the 128-byte swizzled A box of its K half
       if (warp_live) {
@@ -376,9 +378,12 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
         tc::tmem_st16(ta, hi);
         tc::tmem_st16(ta + (uint32_t)KC, lo);
       }
+      // the A slot is free once every worker warp has read its rows
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&bar[BAR_EMPTY + s]);
       if (src.fresh_b(c)) {
         // the B segment this thread copied: low part next to it
-        unsigned char* sb = slot + m.offB;
+        unsigned char* sb = bslot + m.offB;
         const float4 xb = *reinterpret_cast<const float4*>(sb);
         float4 lb;
         lb.x = xb.x - tf32_rz(xb.x);
@@ -443,7 +448,7 @@ __device__ __forceinline__ uint32_t block_setup(uint64_t* bar, uint32_t* tslot, 
     tc::mbar_init(&bar[BAR_DRAIN + 1], 1);
     for (int i = 0; i < kSlots; ++i) {
       tc::mbar_init(&bar[BAR_FULL + i], 1);
-      tc::mbar_init(&bar[BAR_EMPTY + i], 2);
+      tc::mbar_init(&bar[BAR_EMPTY + i], WORKERS / 32);
     }
     for (int i = 0; i < kABuf; ++i) {
       tc::mbar_init(&bar[BAR_READY + i], WORKERS / 32);
@@ -523,10 +528,10 @@ struct SrcTa {
   // this thread's row in the last finished tile (rows only move forward)
   int wk = 0, flev = -1, fidx = 0;
 
-  // B is X over the input box: when kSlots is a multiple of cpt, slot s always
-  // holds K range s % cpt, so B is copied and split in the first kSlots chunks
-  // only and read from the slot afterwards
-  __device__ bool fresh_b(int c) const { return c < kSlots || kSlots % cpt != 0; }
+  // B is X over the input box: when kBSlots is a multiple of cpt, B slot s
+  // always holds K range s % cpt, so B is copied and split in the first
+  // kBSlots chunks only and read from the slot afterwards
+  __device__ bool fresh_b(int c) const { return c < kBSlots || kBSlots % cpt != 0; }
   // tiles of V-stack rows: every row of a tile can be live
   __device__ int live_rows() const { return 128; }
   __device__ int level_of(int tg) const {
