@@ -241,6 +241,8 @@ def pair_sizes(H):
 
 # FP64 arithmetic rate for the assembly's fraction: GB300's nominal dense FP64
 ASSEMBLY_PEAK_GFLOPS = 1250.0
+# FP64 FMAs per second at that nominal rate
+FP64_FMA_PEAK = ASSEMBLY_PEAK_GFLOPS * 1e9 / 2
 
 
 def aca_work(H):
@@ -267,6 +269,8 @@ GEMV_ROWS_T = 256
 
 def engine_of(kernels) -> str:
     """The matvec engine whose kernels a profile report names."""
+    if "uy64" in kernels or "vy64" in kernels:
+        return "f64"
     if "leaf_rows" in kernels:
         return "tc"
     if "uy" in kernels or "vy" in kernels:
@@ -275,6 +279,16 @@ def engine_of(kernels) -> str:
 
 
 def level_bytes(H, nr_pad, s, engine):
+    """Algorithmic bytes per launch of each kernel (see level_bytes_engine);
+    the FP64 streaming engine ("f64") is the few-column engine's stages on
+    8-byte factors and near-field blocks, one column."""
+    if engine == "f64":
+        gv = level_bytes_engine(H, 1, 8, "gemv", near_bytes=8)
+        return {k + "64": v for k, v in gv.items()}
+    return level_bytes_engine(H, nr_pad, s, engine)
+
+
+def level_bytes_engine(H, nr_pad, s, engine, near_bytes=4):
     """Algorithmic bytes per launch of each kernel of one matvec engine
     ("simt", "tc" or "gemv"), keyed by the names its profiler spans carry: the
     factor entries it streams (s bytes each), plus its right-hand-side,
@@ -312,7 +326,7 @@ def level_bytes(H, nr_pad, s, engine):
     vertex = np.array([abs(dx) + abs(dy) + abs(dz) == 3 for dz in (-1, 0, 1) for dy in (-1, 0, 1)
                        for dx in (-1, 0, 1) if (dx, dy, dz) != (0, 0, 0)])
     nbn = np.where((nb >= 0) & ~vertex[None, :], cnt4[np.maximum(nb, 0)], 0).sum(axis=1)
-    near = int((cnt * (cnt4 + nbn)).sum()) * 4
+    near = int((cnt * (cnt4 + nbn)).sum()) * near_bytes
     if engine == "tc":
         # the leaf level as dense FP32 blocks (leaf rows): every leaf-level
         # pair's n x round4(m) block next to the near-field blocks
@@ -403,8 +417,12 @@ def run_ours(args):
     ms_max = max_over_ranks(ws, ms)
     value = ws * nrhs / (ms_max * 1e-3)
 
-    # ---- FP64 form, one right-hand side ----------------------------------
+    # ---- FP64 form, one right-hand side: the FP64 streaming engine (the
+    # automatic choice), and the CUDA-core FP64 kernels beside it -----------
     ms64 = timed(lambda: H.matvec(x1, "fp64"), max(3, args.steps // 2), 2)
+    H.set_engine("simt")
+    ms64_simt = timed(lambda: H.matvec(x1, "fp64"), max(3, args.steps // 4), 2)
+    H.set_engine("auto")
 
     # ---- per-kernel times (events between launches) -> roofline ----------
     H.set_profiling(True)
@@ -451,6 +469,16 @@ def run_ours(args):
     y1 = H.matvec(x1, "mixed")[ridx]
     one["forward"]["error_vs_dense_fp64"] = float((torch.linalg.norm(y1 - d1) / torch.linalg.norm(d1)).item())
     one["speedup_vs_fp64_1rhs"] = ms64 / one["forward"]["ms"]
+
+    # FP64 streaming engine: bytes against HBM, FMAs against GB300's FP64 rate
+    k64 = kernel_split(lambda: H.matvec(x1, "fp64"))
+    a64 = level_bytes(H, 1, 8, engine_of(k64))
+    fp64_entries = st["factor_entries"] + st["near_entries"]
+    fp64 = {"rhs_per_s": 1e3 / ms64, "ms": ms64, "engine": engine_of(k64), "kernel_ms": k64,
+            "whole_GBps": sum(a64[k] for k in k64 if k in a64) / (ms64 * 1e-3) / 1e9,
+            "fma_per_s": fp64_entries / (ms64 * 1e-3),
+            "fma_peak_nominal": FP64_FMA_PEAK, "fma_frac_nominal": fp64_entries / (ms64 * 1e-3) / FP64_FMA_PEAK,
+            "cuda_core_fp64_ms": ms64_simt, "speedup_vs_cuda_core_fp64": ms64_simt / ms64}
 
     # ---- FP64-accurate products in FP32-pair arithmetic (fp64x) ----------
     msx = timed(lambda: H.matvec(x1, "fp64x"), max(3, args.steps // 2), 3)
@@ -563,7 +591,7 @@ def run_ours(args):
             "config": config(args), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(launches), "gpu_launches_per_step": int(launches_step),
             "clocks": clocks,
-            "fp64_1rhs": {"rhs_per_s": 1e3 / ms64, "ms": ms64},
+            "fp64_1rhs": fp64,
             "cuda_graph": graph,
             "autotune": tune,
             "mixed_1rhs": one,

@@ -21,7 +21,7 @@ LIB_DIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIB_DIR, "libhodlr3d_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["tree.cu", "aca.cu", "matvec.cu", "matvec_tc.cu", "matvec_gemv.cu", "gmres.cu", "noalloc.cu",
+SOURCES = ["tree.cu", "aca.cu", "matvec.cu", "matvec_tc.cu", "matvec_gemv.cu", "matvec_f64.cu", "gmres.cu", "noalloc.cu",
            "setup.cpp", "factors.cpp", "product.cpp", "solve.cpp", "capi.cpp"]
 
 

@@ -239,6 +239,14 @@ struct hodlr3d_handle {
       gv_upofs, gv_vt_items, gv_vt_upper, gv_ut_items, gv_ut_upper, gv_x, gv_t, gv_tt, gv_p, gv_pt,
       gv_xl, gv_tl, gv_ttl, gv_pd, gv_ptd;
   int64_t gv_n_vt_items = 0, gv_n_vt_upper = 0, gv_n_ut_items = 0, gv_n_ut_upper = 0;
+  int64_t gv_trows = 0, gv_vrows = 0, gv_pv = 0, gv_pu = 0;  // T rows, V-stack rows, partial rows
+  // FP64 streaming engine (matvec_f64.cu): FP64 factors grouped like the FP32
+  // copies, FP64 near-field blocks, FP64 work buffers; built on first use
+  // after each assembly, left out (the CUDA-core FP64 kernels serve) when
+  // they do not fit in device memory
+  DevBuf u64g_pool, v64g_pool, knear64, f64_x, f64_t, f64_tt, f64_p, f64_pt;
+  bool f64_built = false;
+  bool f64_unavailable = false;
   // GMRES work buffers
   DevBuf g_Q, g_w, g_r, g_x, g_b, g_H, g_cs, g_sn, g_beta, g_hk, g_bnorm, g_err, g_part, g_y,
       g_kcol, g_brk, g_scal, g_d, g_coef;

@@ -226,6 +226,43 @@ size_t gemv_smem_bytes(int max_leaf4, int nr, bool fp64x);
 int launch_matvec_gemv(cudaStream_t s, const GemvOp& op, const GemvBuffers& B, const double* X,
                        int64_t ldx, double* Y, int64_t ldy, int nrhs, bool trans, bool fp64x,
                        MatvecProfiler* prof);
+// The FP64 form streamed (matvec_f64.cu): one right-hand side per pass over
+// FP64 copies of the factors grouped exactly like the FP32 ones (the same
+// element offsets, so GemvOp's tables serve; its float pointers are unused)
+// and FP64 near-field blocks in the near-field layout.  Work buffers: xg N,
+// t the rows of T (zeroed once: padding rows are never written), tt the
+// V-stack rows, p / pt the chunk partials, all FP64.
+struct F64Buffers {
+  const double* u64;
+  const double* v64;
+  const double* knear64;
+  double* xg;
+  double* t;
+  double* tt;
+  double* p;
+  double* pt;
+  const int4* vt_items;
+  int64_t n_vt_items;
+  const int32_t* vt_upper;
+  int64_t n_vt_upper;
+  const int2* ut_items;
+  int64_t n_ut_items;
+  const int32_t* ut_upper;
+  int64_t n_ut_upper;
+};
+size_t f64_smem_bytes(int max_leaf4);
+// y = A x (trans: A^T x) for one column, device pointers; returns the launches.
+int launch_matvec_f64(cudaStream_t s, const GemvOp& op, const F64Buffers& B, const double* x,
+                      double* y, bool trans, MatvecProfiler* prof);
+// FP64 grouped copies of every pair's U (row stride us[p], zeros up to
+// round4(r)) and V (leading dimension round4(m)) at ug[p], vg[p].
+int launch_group_f64(cudaStream_t s, int64_t npairs, const double* const* u64, double* const* ug,
+                     const int32_t* nsize, const int32_t* us, const double* const* v64,
+                     double* const* vg, const int32_t* msize, const int32_t* rank);
+// FP64 near-field blocks (the FP64 form's entries) in the near-field layout.
+int launch_near64(cudaStream_t s, int64_t nleaf, const int32_t* leaf_off, const NearOp& near,
+                  const int64_t* near_off, const int32_t* near_ld, double* Knear64);
+
 // fp64x: lo parts of the near-field blocks, knearlo = K (FP64, as the FP64
 // near field evaluates it) - Knear, same layout.
 int launch_near_lo(cudaStream_t s, int64_t nleaf, const int32_t* leaf_off, const NearOp& near,

@@ -298,6 +298,10 @@ int ensure_gemv(hodlr3d_t h, cudaStream_t s) {
   H3D_CUDA(put(h->gv_vt_upper, vt_upper.data(), sizeof(int32_t) * vt_upper.size()));
   H3D_CUDA(put(h->gv_ut_items, ut_items.data(), sizeof(int32_t) * ut_items.size()));
   H3D_CUDA(put(h->gv_ut_upper, ut_upper.data(), sizeof(int32_t) * ut_upper.size()));
+  h->gv_trows = trows;
+  h->gv_vrows = vrows;
+  h->gv_pv = pv;
+  h->gv_pu = pu;
   h->gv_n_vt_items = (int64_t)vt_items.size() / 4;
   h->gv_n_vt_upper = (int64_t)vt_upper.size();
   h->gv_n_ut_items = (int64_t)ut_items.size() / 2;
@@ -371,10 +375,113 @@ int ensure_lo(hodlr3d_t h, const h3d::NearOp& nr, cudaStream_t s) {
   return HODLR3D_OK;
 }
 
+// The FP64 streaming engine's grouped FP64 factors, FP64 near-field blocks
+// and work buffers, built on first use after each assembly (the few-column
+// tables exist).  When they do not fit in device memory the engine is left
+// out for this assembly and the CUDA-core FP64 kernels serve.
+int ensure_f64(hodlr3d_t h, const h3d::NearOp& nr, cudaStream_t s) {
+  if (h->f64_built || h->f64_unavailable) return HODLR3D_OK;
+  const int64_t np = h->npairs;
+  auto release = [&] {
+    cudaGetLastError();
+    for (DevBuf* b : {&h->u64g_pool, &h->v64g_pool, &h->knear64, &h->f64_x, &h->f64_t, &h->f64_tt,
+                      &h->f64_p, &h->f64_pt})
+      b->release();
+    h->f64_unavailable = true;
+  };
+  auto get = [&](DevBuf& b, size_t bytes) {
+    const cudaError_t e = b.ensure(std::max<size_t>(bytes, 16));
+    return e;
+  };
+  const size_t ub = h->u32_pool->bytes / sizeof(float) * sizeof(double);
+  const size_t vb = h->v32_pool->bytes / sizeof(float) * sizeof(double);
+  for (auto& req : std::vector<std::pair<DevBuf*, size_t>>{
+           {&h->u64g_pool, ub},
+           {&h->v64g_pool, vb},
+           {&h->knear64, sizeof(double) * (size_t)std::max<int64_t>(h->near_floats, 4)},
+           {&h->f64_x, sizeof(double) * (size_t)h->N},
+           {&h->f64_t, sizeof(double) * (size_t)std::max<int64_t>(h->gv_trows, 1)},
+           {&h->f64_tt, sizeof(double) * (size_t)std::max<int64_t>(h->gv_vrows, 1)},
+           {&h->f64_p, sizeof(double) * (size_t)std::max<int64_t>(h->gv_pv, 1)},
+           {&h->f64_pt, sizeof(double) * (size_t)std::max<int64_t>(h->gv_pu, 1)}}) {
+    const cudaError_t e = get(*req.first, req.second);
+    if (e == cudaErrorMemoryAllocation) {
+      release();
+      return HODLR3D_OK;
+    }
+    H3D_CUDA(e);
+  }
+  H3D_CUDA(cudaMemsetAsync(h->f64_t.p, 0, h->f64_t.bytes, s));
+  if (np) {
+    const float* ubase = h->u32_pool->as<float>();
+    const float* vbase = h->v32_pool->as<float>();
+    std::vector<double*> ug(np), vg(np);
+    for (int64_t p = 0; p < np; ++p) {
+      ug[p] = h->u64g_pool.as<double>() + (h->h_u32[p] - ubase);
+      vg[p] = h->v64g_pool.as<double>() + (h->h_v32[p] - vbase);
+    }
+    DevBuf du, dv, dug, dvg, dn, dm, dus, dr;
+    H3D_CUDA(du.ensure(sizeof(void*) * np));
+    H3D_CUDA(dv.ensure(sizeof(void*) * np));
+    H3D_CUDA(dug.ensure(sizeof(void*) * np));
+    H3D_CUDA(dvg.ensure(sizeof(void*) * np));
+    H3D_CUDA(dn.ensure(sizeof(int32_t) * np));
+    H3D_CUDA(dm.ensure(sizeof(int32_t) * np));
+    H3D_CUDA(dus.ensure(sizeof(int32_t) * np));
+    H3D_CUDA(dr.ensure(sizeof(int32_t) * np));
+    H3D_CUDA(cudaMemcpy(du.p, h->h_u64.data(), sizeof(void*) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(cudaMemcpy(dv.p, h->h_v64.data(), sizeof(void*) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(cudaMemcpy(dug.p, ug.data(), sizeof(void*) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(cudaMemcpy(dvg.p, vg.data(), sizeof(void*) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(cudaMemcpy(dn.p, h->h_pair_n.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(cudaMemcpy(dm.p, h->h_pair_m.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(cudaMemcpy(dus.p, h->h_ustride.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice));
+    H3D_CUDA(cudaMemcpy(dr.p, h->h_rank.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice));
+    h->launches += h3d::launch_group_f64(s, np, du.as<const double* const>(), dug.as<double* const>(),
+                                         dn.as<int32_t>(), dus.as<int32_t>(), dv.as<const double* const>(),
+                                         dvg.as<double* const>(), dm.as<int32_t>(), dr.as<int32_t>());
+    H3D_CUDA(cudaGetLastError());
+    H3D_CUDA(cudaStreamSynchronize(s));
+  }
+  h->launches += h3d::launch_near64(s, h->nleaf, h->leaf_off.as<int32_t>(), nr, h->near_off.as<int64_t>(),
+                                    h->near_ld.as<int32_t>(), h->knear64.as<double>());
+  H3D_CUDA(cudaGetLastError());
+  h->f64_built = true;
+  return HODLR3D_OK;
+}
+
+h3d::GemvOp gemv_op(hodlr3d_t h, bool fp64x);
+
+// The FP64 streaming engine (matvec_f64.cu), one column per pass.
+int run_f64(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld, cudaStream_t s, bool trans) {
+  const h3d::GemvOp g = gemv_op(h, false);
+  h3d::F64Buffers B{};
+  B.u64 = h->u64g_pool.as<double>();
+  B.v64 = h->v64g_pool.as<double>();
+  B.knear64 = h->knear64.as<double>();
+  B.xg = h->f64_x.as<double>();
+  B.t = h->f64_t.as<double>();
+  B.tt = h->f64_tt.as<double>();
+  B.p = h->f64_p.as<double>();
+  B.pt = h->f64_pt.as<double>();
+  B.vt_items = h->gv_vt_items.as<int4>();
+  B.n_vt_items = h->gv_n_vt_items;
+  B.vt_upper = h->gv_vt_upper.as<int32_t>();
+  B.n_vt_upper = h->gv_n_vt_upper;
+  B.ut_items = h->gv_ut_items.as<int2>();
+  B.n_ut_items = h->gv_n_ut_items;
+  B.ut_upper = h->gv_ut_upper.as<int32_t>();
+  B.n_ut_upper = h->gv_n_ut_upper;
+  for (int c = 0; c < nrhs; ++c)
+    h->launches += h3d::launch_matvec_f64(s, g, B, x + c * ld, y + c * ld, trans,
+                                          h->profiling ? &h->prof : nullptr);
+  H3D_CUDA(cudaGetLastError());
+  return HODLR3D_OK;
+}
+
 // The few-column engine (matvec_gemv.cu) over this handle's tables, in passes
 // of 4 (or 8) columns; its tables and, for fp64x, the lo parts exist.
-int run_gemv(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld, cudaStream_t s,
-             bool trans, bool fp64x) {
+h3d::GemvOp gemv_op(hodlr3d_t h, bool fp64x) {
   h3d::GemvOp g{};
   g.levels = h->levels;
   g.max_leaf4 = (h->max_leaf + 3) & ~3;
@@ -402,6 +509,12 @@ int run_gemv(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld, cuda
   g.near_base = h->near_base.as<int64_t>();
   g.near_ld = h->near_ld.as<int32_t>();
   g.near_off = h->near_off.as<int64_t>();
+  return g;
+}
+
+int run_gemv(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld, cudaStream_t s,
+             bool trans, bool fp64x) {
+  const h3d::GemvOp g = gemv_op(h, fp64x);
   h3d::GemvBuffers gb{};
   gb.xg = h->gv_x.as<float>();
   gb.t = h->gv_t.as<float>();
@@ -596,10 +709,25 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
     precision = HODLR3D_FP64;
     far = far_op(h, false);
   }
+  // the FP64 form: streamed from FP64 copies grouped like the FP32 ones
+  // (automatic or forced few-column engine); else the CUDA-core kernels
+  if (precision == HODLR3D_FP64 && !use_gemv && (engine == 0 || engine == 3)) {
+    H3D_TRY(ensure_near_blocks(h, nr, s));
+    H3D_TRY(ensure_gemv(h, s));
+    if (h->gemv_ok) {
+      H3D_TRY(ensure_f64(h, nr, s));
+      if (h->f64_built) return run_f64(h, x, y, nrhs, ld, s, trans);
+    }
+    if (engine == 3)
+      return set_error(HODLR3D_ERR_UNSUPPORTED,
+                       "the few-column engine's FP64 form needs leaves whose near-field inputs fit "
+                       "its shared memory, fewer than 2^31 rows of T and device memory for the FP64 "
+                       "factors grouped by box");
+  }
   if (engine == 3 && !use_gemv && !fp64x)
     return set_error(HODLR3D_ERR_UNSUPPORTED,
-                     "the few-column engine needs the mixed form, leaves whose near-field inputs "
-                     "fit its shared memory and fewer than 2^31 rows of T");
+                     "the few-column engine needs the mixed or FP64 form, leaves whose near-field "
+                     "inputs fit its shared memory and fewer than 2^31 rows of T");
   if (use_gemv) return run_gemv(h, x, y, nrhs, ld, s, trans, fp64x);
   const bool tc_ok = mixed && !trans && tc_tree;
   if (engine == 2 && !tc_ok)

@@ -655,6 +655,8 @@ int finish_assembly(hodlr3d_t h, double t_start) {
   h->near_built = false;
   h->maps_built = false;
   h->gemv_built = false;
+  h->f64_built = false;
+  h->f64_unavailable = false;
   h->assembled = true;
   h->finish_seconds = now_s() - t_finish;
   h->assemble_seconds = now_s() - t_start;

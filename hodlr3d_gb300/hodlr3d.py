@@ -254,7 +254,9 @@ class HODLR3D:
 
     def set_engine(self, engine: str) -> None:
         """'auto', 'simt' (CUDA cores, every form), 'tc' (tcgen05 tensor cores,
-        mixed A x) or 'gemv' (few-column FP32 kernels, mixed A x and A^T x)."""
+        mixed A x) or 'gemv' (few-column streaming kernels: mixed and fp64x
+        A x and A^T x from the FP32 copies, the FP64 form from FP64 copies
+        grouped the same way)."""
         check(self._L.hodlr3d_set_engine(self.handle, {"auto": 0, "simt": 1, "tc": 2, "gemv": 3}[engine]))
 
     ENGINES = ("auto", "simt", "tc", "gemv")

@@ -226,10 +226,13 @@ int64_t hodlr3d_launch_count(hodlr3d_t h);
 /* Matvec engine: 0 = automatic (mixed form: the few-column FP32 kernels for
  * A x with 1..4 right-hand sides (1..32 on trees the tensor cores do not
  * take) and A^T x with 1..32, the tensor cores, tcgen05 3xTF32, for A x with
- * more; HODLR3D_FP64X: the few-column kernels; otherwise CUDA-core kernels),
- * 1 = CUDA-core kernels only (HODLR3D_FP64X becomes HODLR3D_FP64), 2 = tensor
- * cores only, 3 = few-column kernels only (HODLR3D_ERR_UNSUPPORTED where the
- * chosen engine does not apply).  After hodlr3d_autotune the automatic
+ * more; HODLR3D_FP64X: the few-column kernels; HODLR3D_FP64: the few-column
+ * FP64 streaming kernels, one column per pass, over FP64 factors grouped by
+ * box (built on first use; where they do not fit in device memory, and
+ * otherwise, the CUDA-core kernels), 1 = CUDA-core kernels only
+ * (HODLR3D_FP64X becomes HODLR3D_FP64), 2 = tensor cores only, 3 =
+ * few-column kernels only (HODLR3D_ERR_UNSUPPORTED where the chosen engine
+ * does not apply).  After hodlr3d_autotune the automatic
  * choice of the mixed form follows its timings instead of these rules. */
 int hodlr3d_set_engine(hodlr3d_t h, int engine);
 /* Autotuner of the automatic engine choice over this operator's own rank

@@ -15,7 +15,7 @@ sys.path.insert(0, ROOT)
 import bench  # noqa: E402
 import golden_util as gu  # noqa: E402
 
-SOURCES = {"simt": "matvec.cu", "tc": "matvec_tc.cu", "gemv": "matvec_gemv.cu"}
+SOURCES = {"simt": "matvec.cu", "tc": "matvec_tc.cu", "gemv": "matvec_gemv.cu", "f64": "matvec_f64.cu"}
 
 
 class FakeOperator:

@@ -94,9 +94,13 @@ def test_gemv_adjoint_identity(case):
     assert ((lhs - rhs).abs() <= 2e-6 * scale).all(), (lhs, rhs, scale)
 
 
-def test_gemv_refuses_fp64(case):
+def test_gemv_takes_fp64_as_the_fp64_stream(case):
+    """Forced few-column engine with the FP64 form: the FP64 streaming kernels
+    (FP64 factors grouped by box), the same product as the automatic choice."""
     g, H, _ = case
+    x = torch.ones(H.N, 1, dtype=torch.float64, device="cuda")
+    ya = H.matvec(x, "fp64")
     H.set_engine("gemv")
-    with pytest.raises(RuntimeError, match="few-column engine"):
-        H.matvec(torch.ones(H.N, 1, dtype=torch.float64, device="cuda"), "fp64")
+    yg = H.matvec(x, "fp64")
     H.set_engine("auto")
+    assert torch.equal(ya, yg)
