@@ -711,7 +711,8 @@ int matvec_device(hodlr3d_t h, const double* x, double* y, int nrhs, int64_t ld,
   }
   // the FP64 form: streamed from FP64 copies grouped like the FP32 ones
   // (automatic or forced few-column engine); else the CUDA-core kernels
-  if (precision == HODLR3D_FP64 && !use_gemv && (engine == 0 || engine == 3)) {
+  // (its grouped layout is the FP32 copies' one: with keep_fp32 = 0 there is none)
+  if (precision == HODLR3D_FP64 && !use_gemv && h->opt.keep_fp32 && (engine == 0 || engine == 3)) {
     H3D_TRY(ensure_near_blocks(h, nr, s));
     H3D_TRY(ensure_gemv(h, s));
     if (h->gemv_ok) {
