@@ -92,6 +92,19 @@ __global__ void k64_gather(int64_t N, const double* __restrict__ X, const int32_
   if (t < N) xg[t] = X[perm[t]];
 }
 
+// nr rows of a V stack window (row stride m4, len2 groups) times xs, LW
+// lanes per row, 4 rows per lane, the warps taking row blocks in turn; row R's
+// sum goes to put(R, sum)
+template <int LW, class Put>
+__device__ __forceinline__ void vt_pass(const double* __restrict__ V, int64_t m4, int nr, int len2,
+                                        const double* xs, Put&& put) {
+  constexpr int P = 4, RB = P * (32 / LW);
+  const int w = threadIdx.x >> 5;
+  for (int b0 = w * RB; b0 < nr; b0 += WARPS * RB)
+    rows_dot<LW, P>(V + (int64_t)b0 * m4, m4, min(RB, nr - b0), len2, xs,
+                    [&](int q, double s) { put(b0 + q, s); });
+}
+
 // Forward far field, input side: item (a, ci, r0, nr): rows r0 .. r0 + nr of
 // source box a's V stack over columns [ci CW, + CW) times x of those points;
 // row R goes to its T row (vrow_t) or, for boxes wider than one chunk, to
@@ -119,17 +132,24 @@ __global__ void __launch_bounds__(THREADS) k64_vt(GemvOp op, const double* __res
   const int32_t* vr = op.vrow_t + op.vrow0[a] + r0;
   const double* V = v64 + op.vbox_off[a] + (int64_t)r0 * m4 + col0;
   double* dst = pofs < 0 ? t : part + pofs + (int64_t)ci * rows_a + r0;
-  const int w = threadIdx.x >> 5;
   const int len2 = cl / 2;
-  constexpr int RB = 8;  // rows per warp pass
-  for (int b0 = w * RB; b0 < nr; b0 += WARPS * RB)
-    rows_dot_any<RB>(V + (int64_t)b0 * m4, m4, min(RB, nr - b0), len2, xs, [&](int q, double s) {
-      const int R = b0 + q;
-      if (pofs < 0)
-        dst[vr[R]] = s;
-      else
-        dst[R] = s;
-    });
+  auto put = [&](int R, double s) {
+    if (pofs < 0)
+      dst[vr[R]] = s;
+    else
+      dst[R] = s;
+  };
+  // lanes per row from the row length: at least 4 groups (8 FMAs) per lane,
+  // so that the FP64 additions of the lane reduction stay a small share of
+  // the FP64 pipe's work (leaf-level stacks: 64 entries per row)
+  if (len2 >= 128)
+    vt_pass<32>(V, m4, nr, len2, xs, put);
+  else if (len2 >= 32)
+    vt_pass<8>(V, m4, nr, len2, xs, put);
+  else if (len2 >= 16)
+    vt_pass<4>(V, m4, nr, len2, xs, put);
+  else
+    vt_pass<2>(V, m4, nr, len2, xs, put);
 }
 
 // T rows of the source boxes wider than one chunk: sum of their chunk partials
