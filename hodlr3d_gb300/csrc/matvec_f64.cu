@@ -139,14 +139,16 @@ __global__ void __launch_bounds__(THREADS) k64_vt(GemvOp op, const double* __res
     else
       dst[R] = s;
   };
-  // lanes per row from the row length: at least 4 groups (8 FMAs) per lane,
-  // so that the FP64 additions of the lane reduction stay a small share of
-  // the FP64 pipe's work (leaf-level stacks: 64 entries per row)
-  if (len2 >= 128)
+  // lanes per row from the row length: about 8 groups (16 FMAs) per lane, so
+  // that the FP64 additions of the lane reduction (log2 of the lanes) stay a
+  // small share of the FP64 pipe's work (leaf-level stacks: 64 entries per row)
+  if (len2 >= 256)
     vt_pass<32>(V, m4, nr, len2, xs, put);
-  else if (len2 >= 32)
+  else if (len2 >= 128)
+    vt_pass<16>(V, m4, nr, len2, xs, put);
+  else if (len2 >= 64)
     vt_pass<8>(V, m4, nr, len2, xs, put);
-  else if (len2 >= 16)
+  else if (len2 >= 32)
     vt_pass<4>(V, m4, nr, len2, xs, put);
   else
     vt_pass<2>(V, m4, nr, len2, xs, put);
