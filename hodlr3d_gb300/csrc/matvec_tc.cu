@@ -21,37 +21,40 @@
 // A block streams K = 64 chunks over its M = 128 output tiles.  A T tile (ta)
 // runs over one K range, its input box; the tile of ut / leaf runs over its
 // items (operand pairs: a factor A and its right-hand sides B, summed into
-// the tile) one after the other.  Three roles, synchronised by mbarriers only:
+// the tile) one after the other.  In ta / ut three roles share the chunks,
+// synchronised by mbarriers only:
 //
 //   producer (one warp)    copies A global -> shared with the tensor memory
 //                          accelerator: 2D tiled loads from one tensor map per
-//                          factor (boxes of 32 K x 128 rows, or 32 x 8 for the
-//                          V of the T kernels, two K halves per chunk),
-//                          128-byte swizzle, zero fill outside the factor; up
-//                          to kSlots chunks ahead
-//   workers (16 warps)     copy B (X or T, 32 columns) with 16-byte cp.async
-//                          into the canonical K-major layout; split A and B
-//                          into TF32 parts (below); read the accumulators back
-//   issuers (2 threads)    issue, per K = 8 step,
-//                            A_hi [B_hi | B_lo] -> D  (N = 64: hi*hi, hi*lo)
-//                            A_lo B_hi          -> D2 (N = 32: lo*hi)
-//                          with A read from tensor memory, so the tensor core
-//                          reads only B from shared memory
+//                          factor (boxes of 32 K x 128 rows, two K halves per
+//                          chunk), 128-byte swizzle, zero fill outside the
+//                          factor; up to kSlots chunks ahead
+//   workers (8 warps)      copy B (X or T, 32 columns) with 16-byte cp.async
+//                          into the 128-byte swizzled K-major layout, kAhead
+//                          chunks ahead; split A and B into TF32 parts
+//                          (below); read the accumulators back
+//   issuer (one thread)    issues, per K = 8 step,
+//                            A_hi [B_hi | B_lo] -> D cols 0..63 (hi*hi, hi*lo)
+//                            A_lo B_hi          -> D cols 32..63 (+= lo*hi)
+//                          with A read from tensor memory (the tensor core
+//                          reads only B from shared memory); in order from
+//                          one thread, so the second accumulates onto the first
 //
 // The factors, X and T are held in the split-exact FP32 form (common.cuh): v =
 // hi + lo with hi = v with the 13 low mantissa bits cleared and lo = v - hi,
-// both exact TF32.  The workers owning a row (four per row, 16 K values each)
+// both exact TF32.  The workers owning a row (two per row, 32 K values each)
 // read it from the swizzled tile, store hi and lo to tensor memory; the
 // thread that copied a B segment writes its low part next to it (the tensor
 // core reads B_hi from the copy itself).  The lo*lo term, below 2^-22 of the
-// product, is left out.  Groups of kGroupChunks chunks alternate between two
-// accumulator sets (16 hi*hi MMAs per group, so that the truncating FP32
-// accumulation of the tensor core sees few additions: its bias stays below
-// 1e-6 of the product for all-positive data); a group is read back
-// while the next one is multiplied, its
-// hi*hi part summed with compensated (Kahan) FP32 additions (whose error
-// matches an FP64 sum here at a fraction of the cost of GB300's FP64 units)
-// and its cross parts with plain FP32 additions.
+// product, is left out.  Every chunk has its own accumulator (8 hi*hi MMAs,
+// so that the truncating FP32 accumulation of the tensor core sees few
+// additions: its bias stays well below 1e-6 of the product for all-positive
+// data), one of kAcc in tensor memory, read back kLag chunks later while the
+// next chunks are split and multiplied; its hi*hi part is summed with
+// compensated (Kahan) FP32 additions (whose error matches an FP64 sum here at
+// a fraction of the cost of GB300's FP64 units), its cross part with plain
+// FP32 additions.  The waits of this pipeline poll without suspending the
+// warp: a suspended warp resumes hundreds of cycles after the phase completes.
 //
 // Every mbarrier wait is bounded; a wait that gives up sets the error flag and
 // the block's abort flag, after which no role issues new copies or products
@@ -69,11 +72,11 @@ namespace {
 
 constexpr int NR = 32;                     // right-hand sides (MMA N)
 constexpr int KC = 64;                     // K per chunk (two 32-wide boxes of A)
-constexpr int WORKERS = 512;               // copy B, split and read back: four threads per row
-constexpr int NCOL = 8;                    // accumulator columns (right-hand sides) per worker
-constexpr int ISSUER0 = WORKERS;           // warps 16, 17: MMA issuers
-constexpr int PRODUCER = WORKERS + 64;     // warp 18: A copies
-constexpr int THREADS = WORKERS + 96;
+constexpr int WORKERS = 256;               // copy B, split and read back: two threads per row
+constexpr int NCOL = 16;                   // accumulator columns (right-hand sides) per worker
+constexpr int ISSUER0 = WORKERS;           // warp 8: MMA issuer
+constexpr int PRODUCER = WORKERS + 32;     // warp 9: A copies
+constexpr int THREADS = PRODUCER + 32;
 constexpr int A_HALF = 128 * 32 * 4;       // one 32-wide box of A (16 KB)
 constexpr int A_BYTES = 2 * A_HALF;        // an A slot: one chunk (32 KB)
 constexpr int B_HALF = 2 * NR * 128;       // B hi and lo rows of one K half (8 KB)
@@ -81,8 +84,10 @@ constexpr int B_LO = NR * 128;             // B_lo rows below B_hi in each K hal
 constexpr int B_SLOT = 2 * B_HALF;         // a B slot: one chunk, hi and lo (16 KB)
 constexpr int kSlots = 4;                  // A ring: tiles in flight, freed once split
 constexpr int kBSlots = 4;                 // B ring: freed once multiplied
-constexpr int kABuf = 2;                   // tensor-memory A buffers (chunks multiplied ahead)
-constexpr int kAhead = kBSlots - kABuf;    // B chunks in flight ahead of the split one
+constexpr int kABuf = 2;                   // tensor-memory A buffers
+constexpr int kAcc = 3;                    // accumulators: one per chunk, read back kLag chunks later
+constexpr int kLag = 2;
+constexpr int kAhead = 2;                  // B chunks copied ahead of the one split into hi/lo
 constexpr int B_RING = kSlots * A_BYTES;
 constexpr int TAB_OFF = B_RING + kBSlots * B_SLOT;
 constexpr int kMaxEntries = 768;           // table entries (pairs, near blocks) of one block
@@ -92,22 +97,21 @@ constexpr uint32_t kWaitLimit = 1u << 17;   // polls of up to kWaitHintNs each: 
 constexpr uint32_t kWaitHintNs = 8192;
 constexpr uint32_t IDESC64 = tc::idesc_tf32(128, 2 * NR);
 constexpr uint32_t IDESC32 = tc::idesc_tf32(128, NR);
-// tensor memory: accumulator set b at column 96 b (D: hi*hi 0..31, hi*lo
-// 32..63; D2: lo*hi 64..95); A of chunk c at 192 + 128 (c % kABuf) (hi
+// tensor memory: the accumulator of chunk c at column 64 (c % kAcc) (hi*hi
+// 0..31; hi*lo + lo*hi 32..63); A of chunk c at 192 + 128 (c % kABuf) (hi
 // 0..63, lo 64..127)
 constexpr uint32_t kTmemCols = 512;
-constexpr uint32_t TM_ACC = 96;
-constexpr uint32_t TM_A = 192;
+constexpr uint32_t TM_ACC = 64;
+constexpr uint32_t TM_A = TM_ACC * kAcc;
 constexpr uint32_t TM_ASTRIDE = 2 * KC;
-constexpr int kGroupChunks = 2;            // chunks per accumulation group (K = 128)
 // barriers
 constexpr int BAR_FULL = 0;                // [kSlots] A of the slot landed (producer, tx)
 constexpr int BAR_EMPTY = kSlots;          // [kSlots] A slot split (one arrival per worker warp)
 constexpr int BAR_READY = 2 * kSlots;      // [kABuf] chunk c % kABuf split (one arrival per worker warp)
-constexpr int BAR_MPAR = BAR_READY + kABuf;  // [kABuf] chunk c % kABuf multiplied (issuer commits)
-constexpr int BAR_ACC = BAR_MPAR + kABuf;  // [2] accumulator set complete (issuer commits)
-constexpr int BAR_DRAIN = BAR_ACC + 2;     // [2] an issuer's products in flight completed
-constexpr int NBAR = BAR_DRAIN + 2;
+constexpr int BAR_DONE = BAR_READY + kABuf;  // [kAcc] chunk c % kAcc multiplied (issuer commits)
+constexpr int BAR_DRAIN = BAR_DONE + kAcc;   // the issuer's products in flight completed
+constexpr int NBAR = BAR_DRAIN + 1;
+static_assert(kLag >= kABuf && kAcc > kLag && kAhead >= 1 && kAhead + kLag <= kBSlots, "chunk pipeline");
 
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
 static_assert(TM_A + TM_ASTRIDE * kABuf <= kTmemCols, "tensor memory");
@@ -170,13 +174,17 @@ __device__ __forceinline__ uint32_t sw128_off(int n, int kc, int half) {
   return (uint32_t)((kc >> 3) * half + n * 128 + (((kc & 7) ^ (n & 7)) << 4));
 }
 
-// This worker's B copy: k quad qb of column cb to offB of the slot, in the
-// 128-byte swizzled layout (B_hi rows 0..31, B_lo rows 32..63 of each K half);
-// its low part goes to offB + B_LO.
-struct CopyMap {
-  int cb, qb;
-  uint32_t offB;
-};
+// The B copies of one chunk: lane l of worker warp v copies k quad qb =
+// l % 16 of the columns cb = 2 i + l / 16, i = 2 v, 2 v + 1, to
+// bslot_off(i, l) of the slot, in the 128-byte swizzled layout (B_hi rows
+// 0..31, B_lo rows 32..63 of each K half); their low parts go B_LO further.
+// 16 consecutive lanes copy one column's 64 K values (256 contiguous bytes);
+// a warp's 16-byte accesses fill four 128-byte rows, free of bank conflicts.
+constexpr int BCOPIES = 16 / (WORKERS / 32);  // column pairs per worker warp
+__device__ __forceinline__ int bslot_col(int i, int lane) { return 2 * i + (lane >> 4); }
+__device__ __forceinline__ uint32_t bslot_off(int i, int lane) {
+  return sw128_off(bslot_col(i, lane), lane & 15, B_HALF);
+}
 
 // A table entry of the long-K kernels: A is the box at (k, y) of map, B column
 // c at b + c bs; blen values of K (a multiple of 4).
@@ -234,7 +242,7 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
     for (int c = 0; c < nch; ++c) {
       const int s = c % kSlots;
       if (lane == 0 && c >= kSlots &&
-          !tc::mbar_wait_sleep(&bar[BAR_EMPTY + s], (uint32_t)(((c / kSlots) - 1) & 1), kWaitLimit, kWaitHintNs))
+          !tc::mbar_wait_spin(&bar[BAR_EMPTY + s], (uint32_t)(((c / kSlots) - 1) & 1)))
         stream_give_up(err, abortp);
       __syncwarp();
       if (*abortp) break;
@@ -251,51 +259,39 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
   }
 
   if (tid >= ISSUER0) {
-    // issuer warps (lane 0): warp 8 A_hi [B_hi | B_lo] -> D, warp 9 A_lo B_hi -> D2
-    if ((tid & 31) != 0) return nch;
-    const bool second = tid >= ISSUER0 + 32;
-    int g = 0, gk = 0, ct = 0;
+    // the issuer (warp 8, lane 0), per K step of 8: A_hi [B_hi | B_lo] -> D
+    // columns 0..63, then A_lo B_hi -> D columns 32..63 (issued in order by
+    // one thread, so the second always accumulates onto the first)
+    if (tid != ISSUER0) return nch;
     for (int c = 0; c < nch; ++c) {
-      const bool close = ct == cpt - 1 || gk == kGroupChunks - 1;
-      const int buf = g & 1;
-      if (!tc::mbar_wait_sleep(&bar[BAR_READY + c % kABuf], (uint32_t)((c / kABuf) & 1), kWaitLimit, kWaitHintNs))
+      if (!tc::mbar_wait_spin(&bar[BAR_READY + c % kABuf], (uint32_t)((c / kABuf) & 1)))
         stream_give_up(err, abortp);
       if (*abortp) break;
       tc::fence_after_sync();
-      const uint32_t ab = tmem + TM_A + TM_ASTRIDE * (uint32_t)(c % kABuf) + (second ? (uint32_t)KC : 0u);
-      const uint32_t d = tmem + TM_ACC * (uint32_t)buf + (second ? 64u : 0u);
+      const uint32_t ab = tmem + TM_A + TM_ASTRIDE * (uint32_t)(c % kABuf);
+      const uint32_t d = tmem + TM_ACC * (uint32_t)(c % kAcc);
       const uint32_t b0 = tc::smem_addr(smem + B_RING + (c % kBSlots) * B_SLOT);
 #pragma unroll
-      for (int ks = 0; ks < KC / 8; ++ks)
-        tc::mma_tf32_ta(d, ab + 8u * ks, desc_sw128(b0 + (uint32_t)((ks >> 2) * B_HALF + (ks & 3) * 32)),
-                        second ? IDESC32 : IDESC64, (gk > 0 || ks > 0) ? 1u : 0u);
-      tc::mma_commit(&bar[BAR_MPAR + c % kABuf]);
-      if (close) {
-        tc::mma_commit(&bar[BAR_ACC + buf]);
-        ++g;
-        gk = 0;
-      } else {
-        ++gk;
+      for (int ks = 0; ks < KC / 8; ++ks) {
+        const uint64_t bd = desc_sw128(b0 + (uint32_t)((ks >> 2) * B_HALF + (ks & 3) * 32));
+        tc::mma_tf32_ta(d, ab + 8u * ks, bd, IDESC64, ks > 0 ? 1u : 0u);
+        tc::mma_tf32_ta(d + 32u, ab + (uint32_t)KC + 8u * ks, bd, IDESC32, 1u);
       }
-      ct = ct == cpt - 1 ? 0 : ct + 1;
+      // chunk c multiplied: its accumulator is complete, its A buffer and B slot free
+      tc::mma_commit(&bar[BAR_DONE + c % kAcc]);
     }
     // the products issued so far complete before the block frees tensor memory
-    tc::mma_commit(&bar[BAR_DRAIN + (second ? 1 : 0)]);
-    if (!tc::mbar_wait_sleep(&bar[BAR_DRAIN + (second ? 1 : 0)], 0u, kWaitLimit, kWaitHintNs))
+    tc::mma_commit(&bar[BAR_DRAIN]);
+    if (!tc::mbar_wait_sleep(&bar[BAR_DRAIN], 0u, kWaitLimit, kWaitHintNs))
       stream_give_up(err, abortp);
     return nch;
   }
 
-  // workers.  Warp w owns rows 32 (w % 4) .. + 31 (its TMEM lanes), K quads
-  // 4 kq .. 4 kq + 3 of every chunk and accumulator columns 8 kq .. 8 kq + 7,
-  // kq = w / 4; each copies B's k quad qb of column cb.
-  const int w = tid >> 5, lane = tid & 31, kq = w >> 2;
-  CopyMap m;
-  // 16 consecutive threads copy one column's 64 K values (256 contiguous
-  // bytes); 8 of them write one 128-byte swizzled row without bank conflicts
-  m.cb = tid >> 4;
-  m.qb = tid & 15;
-  m.offB = sw128_off(m.cb, m.qb, B_HALF);
+  // workers.  Warp w owns rows 32 (w % 4) .. + 31 (its TMEM lanes), the K
+  // half kq = w / 4 of every chunk (32 values, one 128-byte swizzled box of
+  // A) and accumulator columns 16 kq .. 16 kq + 15; it copies the column
+  // pairs i0, i0 + 1 of B.
+  const int w = tid >> 5, lane = tid & 31, kq = w >> 2, i0 = BCOPIES * w;
   const int R = tid & 127;
   const uint32_t lane_base = ((uint32_t)((tid >> 5) & 3) * 32u) << 16;
   // a warp whose 32 rows all lie at or past the tile's live rows (a 64-point
@@ -308,126 +304,109 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
 #pragma unroll
   for (int j = 0; j < NCOL; ++j) sum[j] = comp[j] = cross[j] = 0.f;
 
-  int nload = 0;
-  for (int i = 0; i < kAhead; ++i) {
-    if (nload < nch) {
-      src.load_b(nload, smem + B_RING + (nload % kBSlots) * B_SLOT, m);
-      ++nload;
-    }
-    cp_async_commit();
-  }
-
-  auto read = [&](int g) {
-    const uint32_t base = tmem + TM_ACC * (uint32_t)(g & 1) + (uint32_t)(NCOL * kq) + lane_base;
-    if (!tc::mbar_wait_sleep(&bar[BAR_ACC + (g & 1)], (uint32_t)((g >> 1) & 1), kWaitLimit, kWaitHintNs))
-      stream_give_up(err, abortp);
+  // the accumulator of chunk r (multiplied: waited for by the caller) into
+  // this thread's compensated sums
+  auto read = [&](int r) {
+    const uint32_t base = tmem + TM_ACC * (uint32_t)(r % kAcc) + (uint32_t)(NCOL * kq) + lane_base;
     tc::fence_after_sync();
-    float hh[NCOL], x1[NCOL], x2[NCOL];
-    tc::tmem_ld8(base, hh);
-    tc::tmem_ld8(base + 32u, x1);
-    tc::tmem_ld8(base + 64u, x2);
+    float hh[NCOL], xx[NCOL];
+    tc::tmem_ld16x2(base, base + 32u, hh, xx);
     tc::fence_before_sync();
 #pragma unroll
     for (int j = 0; j < NCOL; ++j) {
       kahan_add(sum[j], comp[j], hh[j]);
-      cross[j] += x1[j] + x2[j];
+      cross[j] += xx[j];
     }
   };
 
-  int g = 0, gk = 0, ct = 0, tile = 0, pend_tile = 0;
-  bool pend = false;
-  for (int c = 0; c < nch; ++c) {
-    const int s = c % kSlots;
-    // chunk c - kABuf multiplied: its B slot (refilled with B below) and its
-    // tensor-memory A buffer (this chunk's) are free
-    if (c >= kABuf && !tc::mbar_wait_sleep(&bar[BAR_MPAR + c % kABuf],
-                                     (uint32_t)(((c / kABuf) - 1) & 1), kWaitLimit, kWaitHintNs))
-      stream_give_up(err, abortp);
-    if (*abortp) break;
-    if (nload < nch) {
-      src.load_b(nload, smem + B_RING + (nload % kBSlots) * B_SLOT, m);
-      ++nload;
-    }
+  // B of the first kAhead chunks, one copy group per chunk (empty past the end)
+  for (int c = 0; c < kAhead; ++c) {
+    if (c < nch) src.load_b(c, smem + B_RING + (c % kBSlots) * B_SLOT, lane, i0);
     cp_async_commit();
-    cp_async_wait<kAhead>();
-    if (!tc::mbar_wait_sleep(&bar[BAR_FULL + s], (uint32_t)((c / kSlots) & 1), kWaitLimit, kWaitHintNs))
-      stream_give_up(err, abortp);
-    if (*abortp) break;
-
-    unsigned char* slot = smem + s * A_BYTES;
-    unsigned char* bslot = smem + B_RING + (c % kBSlots) * B_SLOT;
-    {
-      // the row this thread owns, from the 128-byte swizzled A box of its K half
-      if (warp_live) {
-        const unsigned char* sa = slot + (kq >> 1) * A_HALF + (uint32_t)R * 128u;
-        float hi[16], lo[16];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int qq = 4 * (kq & 1) + j;
-          const float4 x = *reinterpret_cast<const float4*>(sa + ((uint32_t)(qq ^ (R & 7)) << 4));
-          hi[4 * j] = tf32_rz(x.x);
-          hi[4 * j + 1] = tf32_rz(x.y);
-          hi[4 * j + 2] = tf32_rz(x.z);
-          hi[4 * j + 3] = tf32_rz(x.w);
-          lo[4 * j] = x.x - hi[4 * j];
-          lo[4 * j + 1] = x.y - hi[4 * j + 1];
-          lo[4 * j + 2] = x.z - hi[4 * j + 2];
-          lo[4 * j + 3] = x.w - hi[4 * j + 3];
-        }
-        const uint32_t ta = tmem + TM_A + TM_ASTRIDE * (uint32_t)(c % kABuf) + 16u * kq + lane_base;
-        tc::tmem_st16(ta, hi);
-        tc::tmem_st16(ta + (uint32_t)KC, lo);
-      }
-      // the A slot is free once every worker warp has read its rows
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&bar[BAR_EMPTY + s]);
-      if (src.fresh_b(c)) {
-        // the B segment this thread copied: low part next to it
-        unsigned char* sb = bslot + m.offB;
-        const float4 xb = *reinterpret_cast<const float4*>(sb);
-        float4 lb;
-        lb.x = xb.x - tf32_rz(xb.x);
-        lb.y = xb.y - tf32_rz(xb.y);
-        lb.z = xb.z - tf32_rz(xb.z);
-        lb.w = xb.w - tf32_rz(xb.w);
-        *reinterpret_cast<float4*>(sb + B_LO) = lb;
-      }
-      tc::tmem_wait_st();
-    }
-    // B (cp.async copies and low parts) to the tensor core's proxy; A stored
-    tc::fence_async_smem();
-    tc::fence_before_sync();
-    __syncwarp();
-    if (lane == 0) tc::mbar_arrive(&bar[BAR_READY + c % kABuf]);
-    const bool tile_end = ct == cpt - 1;
-    const bool close = tile_end || gk == kGroupChunks - 1;
-    if (close) {
-      if (pend) {
-        read(g - 1);
-        if (*abortp) break;
-        if (pend_tile != tile) {
-          src.finish(pend_tile, sum, comp, cross);
-#pragma unroll
-          for (int j = 0; j < NCOL; ++j) sum[j] = comp[j] = cross[j] = 0.f;
-        }
-      }
-      pend = true;
-      pend_tile = tile;
-      ++g;
-      gk = 0;
-    } else {
-      ++gk;
-    }
-    if (tile_end) {
-      ++tile;
-      ct = 0;
-    } else {
-      ++ct;
-    }
   }
-  if (!*abortp) {
-    read(g - 1);
-    if (!*abortp) src.finish(pend_tile, sum, comp, cross);
+
+  // iteration c waits for the products of chunk c - kLag (which frees chunk
+  // c's tensor-memory A buffer and the B slot of chunk c + kAhead), copies B
+  // of chunk c + kAhead, splits chunk c and hands it to the issuer, then
+  // reads chunk c - kLag back while chunk c is multiplied; kLag more
+  // iterations read the last chunks.  The accumulator of chunk c - kLag is
+  // next written by chunk c + 1, handed over in the next iteration.
+  for (int c = 0; c < nch + kLag; ++c) {
+    if (c >= kLag) {
+      const int r = c - kLag;
+      if (!tc::mbar_wait_spin(&bar[BAR_DONE + r % kAcc], (uint32_t)((r / kAcc) & 1)))
+        stream_give_up(err, abortp);
+      if (*abortp) break;
+    }
+    if (c < nch) {
+      const int s = c % kSlots;
+      if (c + kAhead < nch) src.load_b(c + kAhead, smem + B_RING + ((c + kAhead) % kBSlots) * B_SLOT, lane, i0);
+      cp_async_commit();
+      cp_async_wait<kAhead>();
+      if (!tc::mbar_wait_spin(&bar[BAR_FULL + s], (uint32_t)((c / kSlots) & 1)))
+        stream_give_up(err, abortp);
+      if (*abortp) break;
+
+      unsigned char* slot = smem + s * A_BYTES;
+      {
+        // the row this thread owns, from the 128-byte swizzled A box of its K half
+        if (warp_live) {
+          const unsigned char* sa = slot + kq * A_HALF + (uint32_t)R * 128u;
+          float hi[32], lo[32];
+  #pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const float4 x = *reinterpret_cast<const float4*>(sa + ((uint32_t)(j ^ (R & 7)) << 4));
+            hi[4 * j] = tf32_rz(x.x);
+            hi[4 * j + 1] = tf32_rz(x.y);
+            hi[4 * j + 2] = tf32_rz(x.z);
+            hi[4 * j + 3] = tf32_rz(x.w);
+            lo[4 * j] = x.x - hi[4 * j];
+            lo[4 * j + 1] = x.y - hi[4 * j + 1];
+            lo[4 * j + 2] = x.z - hi[4 * j + 2];
+            lo[4 * j + 3] = x.w - hi[4 * j + 3];
+          }
+          const uint32_t ta = tmem + TM_A + TM_ASTRIDE * (uint32_t)(c % kABuf) + 32u * kq + lane_base;
+          tc::tmem_st32(ta, hi);
+          tc::tmem_st32(ta + (uint32_t)KC, lo);
+        }
+        // the A slot is free once every worker warp has read its rows
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&bar[BAR_EMPTY + s]);
+        if (src.fresh_b(c)) {
+          // the B segments this thread copied: low parts next to them
+          unsigned char* bslot = smem + B_RING + (c % kBSlots) * B_SLOT;
+          float4 xb[BCOPIES];
+#pragma unroll
+          for (int i = 0; i < BCOPIES; ++i)
+            xb[i] = *reinterpret_cast<const float4*>(bslot + bslot_off(i0 + i, lane));
+#pragma unroll
+          for (int i = 0; i < BCOPIES; ++i) {
+            float4 lb;
+            lb.x = xb[i].x - tf32_rz(xb[i].x);
+            lb.y = xb[i].y - tf32_rz(xb[i].y);
+            lb.z = xb[i].z - tf32_rz(xb[i].z);
+            lb.w = xb[i].w - tf32_rz(xb[i].w);
+            *reinterpret_cast<float4*>(bslot + bslot_off(i0 + i, lane) + B_LO) = lb;
+          }
+        }
+        tc::tmem_wait_st();
+      }
+      // B (copies and low parts) to the tensor core's proxy; A stored in
+      // tensor memory before the issuer multiplies it
+      tc::fence_async_smem();
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&bar[BAR_READY + c % kABuf]);
+    }
+    if (c >= kLag) {
+      const int r = c - kLag;
+      read(r);
+      if (r % cpt == cpt - 1) {
+        src.finish(r / cpt, sum, comp, cross);
+#pragma unroll
+        for (int j = 0; j < NCOL; ++j) sum[j] = comp[j] = cross[j] = 0.f;
+      }
+    }
   }
   cp_async_wait<0>();
   return nch;
@@ -445,16 +424,12 @@ __device__ __forceinline__ uint32_t block_setup(uint64_t* bar, uint32_t* tslot, 
   if (threadIdx.x == 0) {
     *abort_flag = 0;
     tc::mbar_init(&bar[BAR_DRAIN], 1);
-    tc::mbar_init(&bar[BAR_DRAIN + 1], 1);
     for (int i = 0; i < kSlots; ++i) {
       tc::mbar_init(&bar[BAR_FULL + i], 1);
       tc::mbar_init(&bar[BAR_EMPTY + i], WORKERS / 32);
     }
-    for (int i = 0; i < kABuf; ++i) {
-      tc::mbar_init(&bar[BAR_READY + i], WORKERS / 32);
-      tc::mbar_init(&bar[BAR_MPAR + i], 2);
-    }
-    for (int i = 0; i < 2; ++i) tc::mbar_init(&bar[BAR_ACC + i], 2);
+    for (int i = 0; i < kABuf; ++i) tc::mbar_init(&bar[BAR_READY + i], WORKERS / 32);
+    for (int i = 0; i < kAcc; ++i) tc::mbar_init(&bar[BAR_DONE + i], 1);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   tc::fence_before_sync();
@@ -557,11 +532,13 @@ struct SrcTa {
       ++pc;
     }
   }
-  __device__ void load_b(int c, unsigned char* slot, const CopyMap& m) {
+  __device__ void load_b(int c, unsigned char* slot, int lane, int i0) {
     if (fresh_b(c)) {
-      const int kb = wk + 4 * m.qb;
+      const int kb = wk + 4 * (lane & 15);
       const bool ok = kb < kin;
-      cp_async16(slot + m.offB, ok ? b + m.cb * bs + kb : b, ok);
+#pragma unroll
+      for (int i = i0; i < i0 + BCOPIES; ++i)
+        cp_async16(slot + bslot_off(i, lane), ok ? b + bslot_col(i, lane) * bs + kb : b, ok);
     }
     wk += KC;
     if (wk >= cpt * KC) wk = 0;
@@ -734,7 +711,7 @@ struct SrcItems {
   // producer cursor (lane 0): item, K offset, the item's map, row and K
   int pi = -1, pk = 0, py = 0, plen = 0;
   const CUtensorMap* pmap = nullptr;
-  // worker cursor: item, K offset, the item's B column base, stride and K
+  // B warp cursor: item, K offset, the item's B (column 0), column stride and K
   int wi = -1, wk = 0, wbs = 0, wlen = 0;
   const float* wb = nullptr;
 
@@ -762,18 +739,20 @@ struct SrcItems {
     tma_load_2d(a + A_HALF, pmap, pk + 32, py, full);
     pk += KC;
   }
-  __device__ void load_b(int, unsigned char* slot, const CopyMap& m) {
+  __device__ void load_b(int, unsigned char* slot, int lane, int i0) {
     if (wk >= wlen) {
       wi = next_item(wi);
       const Item& it = items[wi];
-      wb = it.b + (int64_t)m.cb * it.bs;
+      wb = it.b;
       wbs = it.bs;
       wlen = it.blen;
       wk = 0;
     }
-    const int kb = wk + 4 * m.qb;
+    const int kb = wk + 4 * (lane & 15);
     const bool ok = kb < wlen;
-    cp_async16(slot + m.offB, ok ? wb + kb : wb, ok);
+#pragma unroll
+    for (int i = i0; i < i0 + BCOPIES; ++i)
+      cp_async16(slot + bslot_off(i, lane), ok ? wb + (int64_t)bslot_col(i, lane) * wbs + kb : wb, ok);
     wk += KC;
   }
 };
@@ -957,6 +936,13 @@ __global__ void k_near_lo(const int32_t* __restrict__ leaf_off, NearOp nr,
 // producer for its copies in flight before the block frees its tensor memory
 // and exits.
 namespace lr {
+// roles of the leaf-row kernel: 16 worker warps (four per 32 TMEM lanes, one
+// K quarter each), 2 issuer warps, 1 producer warp
+constexpr int WORKERS = 512;
+constexpr int ISSUER0 = WORKERS;
+constexpr int PRODUCER = WORKERS + 64;
+constexpr int THREADS = WORKERS + 96;
+constexpr int NCOL = 8;                     // accumulator columns per worker
 constexpr int KC = 64;
 constexpr int NB = 2 * NR;                  // B columns: top and bottom right-hand sides
 constexpr int A_HALF = 128 * 32 * 4;        // one K half of A (rows 0..127, 32 K): 16 KB
@@ -993,7 +979,7 @@ __device__ __forceinline__ void give_up(int* err, volatile int* flag) {
 }
 
 // rows of the workers' named barrier (barrier 1, the 512 worker threads)
-__device__ __forceinline__ void workers_sync() { asm volatile("bar.sync 1, %0;\n" ::"n"(WORKERS) : "memory"); }
+__device__ __forceinline__ void workers_sync() { asm volatile("bar.sync 1, %0;\n" ::"n"(lr::WORKERS) : "memory"); }
 
 __device__ __forceinline__ void tmem_ld8x3(uint32_t a0, uint32_t a1, uint32_t a2, float* v0, float* v1,
                                            float* v2) {
@@ -1067,7 +1053,7 @@ __global__ void k_row_blocks(const int32_t* __restrict__ leaf_off, NearOp nr,
 // accumulators of chunk c - 1, copy B of chunk c + 1 into the B slot chunk
 // c - 1 used, and signal "ready"; the issuers multiply chunk c into the one
 // accumulator set.
-__global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
+__global__ void __launch_bounds__(lr::THREADS, 1) k_leaf_rows_tc(
     const int32_t* __restrict__ leaf_off, const LeafBlock* __restrict__ blocks,
     const int32_t* __restrict__ block_ptr, const CUtensorMap* __restrict__ rmaps,
     const float* __restrict__ Xt, int64_t N, const double* __restrict__ Ynl, int levels,
@@ -1094,7 +1080,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
   const int nch = (nit + 1) / 2;
   // the leaf's block list, staged in shared memory
   LeafBlock* it = reinterpret_cast<LeafBlock*>(smem + lr::TAB_OFF);
-  for (int i = threadIdx.x; i < nit; i += THREADS) it[i] = blocks[block_ptr[k] + i];
+  for (int i = threadIdx.x; i < nit; i += lr::THREADS) it[i] = blocks[block_ptr[k] + i];
   const CUtensorMap* map = rmaps + k;
   const int tid = threadIdx.x;
   volatile int* abortp = &abort_flag;
@@ -1103,9 +1089,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
     abort_flag = 0;
     for (int i = 0; i < lr::kASlots; ++i) {
       tc::mbar_init(&bar[lr::BAR_FULL + i], 1);
-      tc::mbar_init(&bar[lr::BAR_EMPTY + i], WORKERS / 32);
+      tc::mbar_init(&bar[lr::BAR_EMPTY + i], lr::WORKERS / 32);
     }
-    tc::mbar_init(&bar[lr::BAR_READY], WORKERS / 32);
+    tc::mbar_init(&bar[lr::BAR_READY], lr::WORKERS / 32);
     tc::mbar_init(&bar[lr::BAR_ACC], 2);
     tc::mbar_init(&bar[lr::BAR_DRAIN], 1);
     tc::mbar_init(&bar[lr::BAR_DRAIN + 1], 1);
@@ -1116,7 +1102,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
   tc::fence_after_sync();
   const uint32_t tmem = tslot;
 
-  if (tid >= PRODUCER) {
+  if (tid >= lr::PRODUCER) {
     // producer warp (lane 0): four 32 x 64 boxes per chunk (K halves of the
     // top and bottom blocks); a missing bottom block reads rows 64..127 of
     // the leaf's matrix, all outside it: zeros
@@ -1125,8 +1111,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
       for (int c = 0; c < nch; ++c) {
         const int s = c % lr::kASlots;
         if (c >= lr::kASlots &&
-            !tc::mbar_wait_sleep(&bar[lr::BAR_EMPTY + s], (uint32_t)(((c / lr::kASlots) - 1) & 1),
-                                 kWaitLimit, kWaitHintNs))
+            !tc::mbar_wait_try(&bar[lr::BAR_EMPTY + s], (uint32_t)(((c / lr::kASlots) - 1) & 1)))
           lr::give_up(err, abortp);
         if (lr::aborted(abortp)) break;
         unsigned char* a = smem + s * lr::A_BYTES;
@@ -1146,13 +1131,13 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
                                  kWaitLimit, kWaitHintNs))
           lr::give_up(err, abortp);
     }
-  } else if (tid >= ISSUER0) {
+  } else if (tid >= lr::ISSUER0) {
     // issuers (lane 0 of warps 16 and 17): A_hi [B_hi | B_lo] -> [HH | X1],
     // A_lo B_hi -> X2, A from tensor memory
     if ((tid & 31) == 0) {
-      const bool second = tid >= ISSUER0 + 32;
+      const bool second = tid >= lr::ISSUER0 + 32;
       for (int c = 0; c < nch; ++c) {
-        if (!tc::mbar_wait_sleep(&bar[lr::BAR_READY], (uint32_t)(c & 1), kWaitLimit, kWaitHintNs))
+        if (!tc::mbar_wait_try(&bar[lr::BAR_READY], (uint32_t)(c & 1)))
           lr::give_up(err, abortp);
         if (lr::aborted(abortp)) break;
         tc::fence_after_sync();
@@ -1183,9 +1168,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
     const int bcol = tid >> 4, bk = 4 * (tid & 15);
     const uint32_t boff_top = sw128_off(bcol, tid & 15, lr::B_HALF);
     const uint32_t boff_bot = sw128_off(bcol + NR, tid & 15, lr::B_HALF);
-    float sum[NCOL], comp[NCOL], cross[NCOL];
+    float sum[lr::NCOL], comp[lr::NCOL], cross[lr::NCOL];
 #pragma unroll
-    for (int j = 0; j < NCOL; ++j) sum[j] = comp[j] = cross[j] = 0.f;
+    for (int j = 0; j < lr::NCOL; ++j) sum[j] = comp[j] = cross[j] = 0.f;
 
     auto load_b = [&](int c) {
       unsigned char* bs = smem + lr::B_OFF + (c % lr::kBSlots) * lr::B_BYTES;
@@ -1203,15 +1188,15 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
       cp_async_commit();
     };
     auto read = [&](int c) {
-      const uint32_t acc = tmem + (bottom ? (uint32_t)NR : 0u) + (uint32_t)(NCOL * kq) + lane_base;
-      if (!tc::mbar_wait_sleep(&bar[lr::BAR_ACC], (uint32_t)(c & 1), kWaitLimit, kWaitHintNs))
+      const uint32_t acc = tmem + (bottom ? (uint32_t)NR : 0u) + (uint32_t)(lr::NCOL * kq) + lane_base;
+      if (!tc::mbar_wait_try(&bar[lr::BAR_ACC], (uint32_t)(c & 1)))
         lr::give_up(err, abortp);
       tc::fence_after_sync();
-      float hh[NCOL], x1[NCOL], x2[NCOL];
+      float hh[lr::NCOL], x1[lr::NCOL], x2[lr::NCOL];
       lr::tmem_ld8x3(acc, acc + (uint32_t)lr::NB, acc + lr::TM_X2, hh, x1, x2);
       tc::fence_before_sync();
 #pragma unroll
-      for (int j = 0; j < NCOL; ++j) {
+      for (int j = 0; j < lr::NCOL; ++j) {
         kahan_add(sum[j], comp[j], hh[j]);
         cross[j] += x1[j] + x2[j];
       }
@@ -1221,8 +1206,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
     int c = 0;
     for (; c < nch; ++c) {
       const int s = c % lr::kASlots;
-      if (!tc::mbar_wait_sleep(&bar[lr::BAR_FULL + s], (uint32_t)((c / lr::kASlots) & 1), kWaitLimit,
-                               kWaitHintNs))
+      if (!tc::mbar_wait_try(&bar[lr::BAR_FULL + s], (uint32_t)((c / lr::kASlots) & 1)))
         lr::give_up(err, abortp);
       if (lr::aborted(abortp)) break;
       {
@@ -1282,21 +1266,21 @@ __global__ void __launch_bounds__(THREADS, 1) k_leaf_rows_tc(
     // combine the halves: the bottom rows' sums go through shared memory
     // (A slot 0, free once every worker is past its last chunk)
     lr::workers_sync();
-    double v[NCOL];
+    double v[lr::NCOL];
 #pragma unroll
-    for (int j = 0; j < NCOL; ++j) v[j] = ((double)sum[j] - (double)comp[j]) + (double)cross[j];
+    for (int j = 0; j < lr::NCOL; ++j) v[j] = ((double)sum[j] - (double)comp[j]) + (double)cross[j];
     double* comb = reinterpret_cast<double*>(smem);
     if (bottom) {
 #pragma unroll
-      for (int j = 0; j < NCOL; ++j) comb[(R - 64) * NR + NCOL * kq + j] = v[j];
+      for (int j = 0; j < lr::NCOL; ++j) comb[(R - 64) * NR + lr::NCOL * kq + j] = v[j];
     }
     lr::workers_sync();
     if (!bottom && R < nk && !lr::aborted(abortp)) {
       const int64_t t = t0 + R;
       const int64_t orig = perm[t];
 #pragma unroll
-      for (int j = 0; j < NCOL; ++j) {
-        const int cc = NCOL * kq + j;
+      for (int j = 0; j < lr::NCOL; ++j) {
+        const int cc = lr::NCOL * kq + j;
         if (cc < nrhs) {
           const double yn = levels >= 2 ? Ynl[(int64_t)cc * N + t] : 0.0;
           Y[(int64_t)cc * ldy + orig] = (v[j] + comb[R * NR + cc]) + yn;
@@ -1379,7 +1363,7 @@ int launch_matvec_tc(cudaStream_t s, int64_t N, const int32_t* perm, const FarOp
     if (prof) prof->mark(s, "ut_tc");
   }
   // the leaf level (dense blocks) and the near field, plus the level sums
-  k_leaf_rows_tc<<<(unsigned)far.nleaf, THREADS, lr::SMEM_BYTES, s>>>(
+  k_leaf_rows_tc<<<(unsigned)far.nleaf, lr::THREADS, lr::SMEM_BYTES, s>>>(
       far.leaf_off, B.blocks, B.block_ptr, rmaps, B.xt, N, B.ynl, d, perm, nrhs, Y, ldy, B.err);
   ++launches;
   if (prof) prof->mark(s, "leaf_rows");
