@@ -499,9 +499,10 @@ struct SrcTa {
   // producer state (lane 0): the box of its current tile
   int pk = 0, pc = 0, px = 0, py = 0;
   const CUtensorMap* pmap = nullptr;
-  // worker state: K offset of the next B copy; the level and table entry of
-  // this thread's row in the last finished tile (rows only move forward)
-  int wk = 0, flev = -1, fidx = 0;
+  // worker state: K offset of the next B copy; the level, its first and
+  // last-plus-one tiles and rows, and the table entry of this thread's row in
+  // the last finished tile (rows only move forward)
+  int wk = 0, fidx = 0, ftile0 = 0, ftile1 = 0, fbase = 0, fend = 0;
 
   // B is X over the input box: when kBSlots is a multiple of cpt, B slot s
   // always holds K range s % cpt, so B is copied and split in the first
@@ -545,22 +546,40 @@ struct SrcTa {
   }
   __device__ void finish(int t, const float* sum, const float* comp, const float* cross) {
     const int tg = tile0 + t * tstep;
-    const int j = level_of(tg);
-    const int rho = (tg - lv[1][j]) * 128 + (threadIdx.x & 127);
-    const int base = cum[lv[0][j]];
-    if (base + rho >= cum[lv[0][j + 1]]) return;
-    if (j != flev) {  // first tile of a level: search; later tiles: step forward
-      fidx = upper_index(cum, n, base + rho);
-      flev = j;
+    const int v0 = (threadIdx.x & 127);
+    if (tg >= ftile1) {  // first tile of a level: its bounds, then a search
+      const int j = level_of(tg);
+      ftile0 = lv[1][j];
+      ftile1 = lv[1][j + 1];
+      fbase = cum[lv[0][j]];
+      fend = cum[lv[0][j + 1]];
+      const int v = fbase + (tg - ftile0) * 128 + v0;
+      if (v >= fend) return;
+      fidx = upper_index(cum, n, v);
     }
-    while (cum[fidx + 1] <= base + rho) ++fidx;
+    const int v = fbase + (tg - ftile0) * 128 + v0;
+    if (v >= fend) return;
+    // step forward to the entry holding row v, four entries per round trip
+    for (;;) {
+      const int c1 = cum[min(fidx + 1, n)], c2 = cum[min(fidx + 2, n)], c3 = cum[min(fidx + 3, n)],
+                c4 = cum[min(fidx + 4, n)];
+      if (v < c1) break;
+      if (v < c2) { fidx += 1; break; }
+      if (v < c3) { fidx += 2; break; }
+      if (v < c4) { fidx += 3; break; }
+      fidx += 4;
+    }
     const int idx = fidx;
-    const PairRow& e = tab[idx];
-    const int l = base + rho - cum[idx];
+    // the entry's fields in registers: the stores below could alias the
+    // table as far as the compiler knows, and would re-read it each time
+    const PairRow e = tab[idx];
+    const int l = v - cum[idx];
     const int c0 = (threadIdx.x >> 7) * NCOL;
+    float* __restrict__ dst = e.dst + (int64_t)c0 * e.ld + l;
+    const int64_t ld = e.ld;
     if (!e.t) {  // slice partial
 #pragma unroll
-      for (int j2 = 0; j2 < NCOL; ++j2) e.dst[(int64_t)(c0 + j2) * e.ld + l] = (sum[j2] - comp[j2]) + cross[j2];
+      for (int j2 = 0; j2 < NCOL; ++j2) dst[j2 * ld] = (sum[j2] - comp[j2]) + cross[j2];
       return;
     }
     // T in the split-exact form, zero padded to ld
@@ -568,12 +587,12 @@ struct SrcTa {
     for (int j2 = 0; j2 < NCOL; ++j2) {
       const float v = (sum[j2] - comp[j2]) + cross[j2];
       const float hi = tf32_rz(v);
-      e.dst[(int64_t)(c0 + j2) * e.ld + l] = hi + tf32_rn(v - hi);
+      dst[j2 * ld] = hi + tf32_rn(v - hi);
     }
     if (l == e.r - 1)
-      for (int lp = e.r; lp < ((e.r + 3) & ~3); ++lp)
+      for (int lp = 1; lp < ((e.r + 3) & ~3) - e.r + 1; ++lp)
 #pragma unroll
-        for (int j2 = 0; j2 < NCOL; ++j2) e.dst[(int64_t)(c0 + j2) * e.ld + lp] = 0.f;
+        for (int j2 = 0; j2 < NCOL; ++j2) dst[j2 * ld + lp] = 0.f;
   }
 };
 
