@@ -212,7 +212,7 @@ struct hodlr3d_handle {
   DevBuf dev_err;   // set by kernels whose bounded waits gave up
   bool leaves_aligned = false;  // every leaf population a multiple of 4
   DevBuf knear, near_off;       // FP32 near-field blocks of the tensor-core engine
-  DevBuf tct;                   // X and T of the tensor-core engine (split-exact FP32)
+  DevBuf tct;                   // X, T and their low parts (tensor-core engine, split-exact FP32)
   DevBuf tmaps;                 // tensor maps of the tensor-core engine: U, V, leaf rows
   // leaf rows of the tensor-core engine (product.cpp ensure_leaf_rows): per
   // leaf its dense FP32 blocks (near field, then the leaf-level interaction

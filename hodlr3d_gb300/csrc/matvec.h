@@ -109,6 +109,7 @@ struct LeafBlock {
 struct TcBuffers {
   float* xt;
   float* t;
+  int64_t lo_off;  // the low parts of X and T, lo_off floats after them
   float* p;
   double* ynl;
   int* err;

@@ -43,9 +43,11 @@
 // The factors, X and T are held in the split-exact FP32 form (common.cuh): v =
 // hi + lo with hi = v with the 13 low mantissa bits cleared and lo = v - hi,
 // both exact TF32.  The workers owning a row (two per row, 32 K values each)
-// read it from the swizzled tile, store hi and lo to tensor memory; the
-// thread that copied a B segment writes its low part next to it (the tensor
-// core reads B_hi from the copy itself).  The lo*lo term, below 2^-22 of the
+// read it from the swizzled tile, store hi and lo to tensor memory.  X and T
+// are written together with their low parts (lo_off floats further on): the
+// T and U kernels copy B and its low parts; the leaf kernel copies B and
+// writes the low parts next to it itself.  The tensor core reads B_hi from
+// the full value.  The lo*lo term, below 2^-22 of the
 // product, is left out.  Every chunk has its own accumulator (8 hi*hi MMAs,
 // so that the truncating FP32 accumulation of the tensor core sees few
 // additions: its bias stays well below 1e-6 of the product for all-positive
@@ -177,7 +179,7 @@ __device__ __forceinline__ uint32_t sw128_off(int n, int kc, int half) {
 // The B copies of one chunk: lane l of worker warp v copies k quad qb =
 // l % 16 of the columns cb = 2 i + l / 16, i = 2 v, 2 v + 1, to
 // bslot_off(i, l) of the slot, in the 128-byte swizzled layout (B_hi rows
-// 0..31, B_lo rows 32..63 of each K half); their low parts go B_LO further.
+// 0..31, B_lo rows 32..63 of each K half), and their low parts B_LO further.
 // 16 consecutive lanes copy one column's 64 K values (256 contiguous bytes);
 // a warp's 16-byte accesses fill four 128-byte rows, free of bank conflicts.
 constexpr int BCOPIES = 16 / (WORKERS / 32);  // column pairs per worker warp
@@ -372,27 +374,10 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
         // the A slot is free once every worker warp has read its rows
         __syncwarp();
         if (lane == 0) tc::mbar_arrive(&bar[BAR_EMPTY + s]);
-        if (src.fresh_b(c)) {
-          // the B segments this thread copied: low parts next to them
-          unsigned char* bslot = smem + B_RING + (c % kBSlots) * B_SLOT;
-          float4 xb[BCOPIES];
-#pragma unroll
-          for (int i = 0; i < BCOPIES; ++i)
-            xb[i] = *reinterpret_cast<const float4*>(bslot + bslot_off(i0 + i, lane));
-#pragma unroll
-          for (int i = 0; i < BCOPIES; ++i) {
-            float4 lb;
-            lb.x = xb[i].x - tf32_rz(xb[i].x);
-            lb.y = xb[i].y - tf32_rz(xb[i].y);
-            lb.z = xb[i].z - tf32_rz(xb[i].z);
-            lb.w = xb[i].w - tf32_rz(xb[i].w);
-            *reinterpret_cast<float4*>(bslot + bslot_off(i0 + i, lane) + B_LO) = lb;
-          }
-        }
         tc::tmem_wait_st();
       }
-      // B (copies and low parts) to the tensor core's proxy; A stored in
-      // tensor memory before the issuer multiplies it
+      // B (this thread's copies, landed) to the tensor core's proxy; A stored
+      // in tensor memory before the issuer multiplies it
       tc::fence_async_smem();
       tc::fence_before_sync();
       __syncwarp();
@@ -495,7 +480,7 @@ struct SrcTa {
   int tile0, tstep, ntile, cpt;
   int kin;
   const float* b;
-  int64_t bs;
+  int64_t bs, lo_off;
   // producer state (lane 0): the box of its current tile
   int pk = 0, pc = 0, px = 0, py = 0;
   const CUtensorMap* pmap = nullptr;
@@ -538,8 +523,11 @@ struct SrcTa {
       const int kb = wk + 4 * (lane & 15);
       const bool ok = kb < kin;
 #pragma unroll
-      for (int i = i0; i < i0 + BCOPIES; ++i)
-        cp_async16(slot + bslot_off(i, lane), ok ? b + bslot_col(i, lane) * bs + kb : b, ok);
+      for (int i = i0; i < i0 + BCOPIES; ++i) {
+        const float* g = ok ? b + bslot_col(i, lane) * bs + kb : b;
+        cp_async16(slot + bslot_off(i, lane), g, ok);
+        cp_async16(slot + bslot_off(i, lane) + B_LO, g + lo_off, ok);
+      }
     }
     wk += KC;
     if (wk >= cpt * KC) wk = 0;
@@ -582,17 +570,19 @@ struct SrcTa {
       for (int j2 = 0; j2 < NCOL; ++j2) dst[j2 * ld] = (sum[j2] - comp[j2]) + cross[j2];
       return;
     }
-    // T in the split-exact form, zero padded to ld
+    // T in the split-exact form and its low parts, zero padded to ld
 #pragma unroll
     for (int j2 = 0; j2 < NCOL; ++j2) {
       const float v = (sum[j2] - comp[j2]) + cross[j2];
       const float hi = tf32_rz(v);
-      dst[j2 * ld] = hi + tf32_rn(v - hi);
+      const float tv = hi + tf32_rn(v - hi);
+      dst[j2 * ld] = tv;
+      dst[j2 * ld + lo_off] = tv - tf32_rz(tv);
     }
     if (l == e.r - 1)
       for (int lp = 1; lp < ((e.r + 3) & ~3) - e.r + 1; ++lp)
 #pragma unroll
-        for (int j2 = 0; j2 < NCOL; ++j2) dst[j2 * ld + lp] = 0.f;
+        for (int j2 = 0; j2 < NCOL; ++j2) dst[j2 * ld + lp] = dst[j2 * ld + lp + lo_off] = 0.f;
   }
 };
 
@@ -600,7 +590,7 @@ template <bool SLICE>
 __global__ void __launch_bounds__(THREADS, 1) k_ta_tc(FarOp op, const CUtensorMap* __restrict__ vmaps,
                                                       const float* __restrict__ Xt, int64_t N,
                                                       float* __restrict__ T, float* __restrict__ Pp,
-                                                      int* __restrict__ err) {
+                                                      int64_t lo_off, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ uint64_t bar[NBAR];
   __shared__ uint32_t tslot;
@@ -697,6 +687,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_ta_tc(FarOp op, const CUtensorMa
   src.cpt = (kin + KC - 1) / KC;
   src.b = Xt + i0;
   src.bs = N;
+  src.lo_off = lo_off;
   run_stream(src, smem, bar, tmem, err, &abort_flag);
   block_teardown(tmem);
 }
@@ -704,7 +695,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_ta_tc(FarOp op, const CUtensorMa
 // Sum of slice partials into the padded T (split-exact form), compensated
 // FP32: T_p[c][l] = sum_s P_p[s][c][l]
 __global__ void k_tred_tc(FarOp op, const int32_t* __restrict__ pairs, const float* __restrict__ Pp,
-                          float* __restrict__ T) {
+                          float* __restrict__ T, int64_t lo_off) {
   const int p = pairs[blockIdx.x];
   const int r = op.rank[p], rp = (r + 3) & ~3;
   const int64_t ns = int64_t(1) << (3 * (op.levels - 1 - op.pair_level[p]));
@@ -716,7 +707,9 @@ __global__ void k_tred_tc(FarOp op, const int32_t* __restrict__ pairs, const flo
     float sum = 0.f, comp = 0.f;
     if (l < r)
       for (int64_t s = 0; s < ns; ++s) kahan_add(sum, comp, src[s * r * NR + c * r + l]);
-    dst[c * ld + l] = tf32_split_value((double)sum - (double)comp);
+    const float tv = tf32_split_value((double)sum - (double)comp);
+    dst[c * ld + l] = tv;
+    dst[c * ld + l + lo_off] = tv - tf32_rz(tv);
   }
 }
 
@@ -730,11 +723,11 @@ struct SrcItems {
   // producer cursor (lane 0): item, K offset, the item's map, row and K
   int pi = -1, pk = 0, py = 0, plen = 0;
   const CUtensorMap* pmap = nullptr;
-  // B warp cursor: item, K offset, the item's B (column 0), column stride and K
+  // worker cursor: item, K offset, the item's B (column 0), column stride and K
   int wi = -1, wk = 0, wbs = 0, wlen = 0;
   const float* wb = nullptr;
+  int64_t lo_off = 0;  // the low parts of B, lo_off floats after B
 
-  __device__ bool fresh_b(int) const { return true; }
   // rows of the block's tile that the epilogue writes (all items share them)
   __device__ int live_rows() const { return nrows; }
   // next item with K after item i
@@ -770,8 +763,11 @@ struct SrcItems {
     const int kb = wk + 4 * (lane & 15);
     const bool ok = kb < wlen;
 #pragma unroll
-    for (int i = i0; i < i0 + BCOPIES; ++i)
-      cp_async16(slot + bslot_off(i, lane), ok ? wb + (int64_t)bslot_col(i, lane) * wbs + kb : wb, ok);
+    for (int i = i0; i < i0 + BCOPIES; ++i) {
+      const float* g = ok ? wb + (int64_t)bslot_col(i, lane) * wbs + kb : wb;
+      cp_async16(slot + bslot_off(i, lane), g, ok);
+      cp_async16(slot + bslot_off(i, lane) + B_LO, g + lo_off, ok);
+    }
     wk += KC;
   }
 };
@@ -806,7 +802,8 @@ struct SrcUt : SrcItems {
 // Phase B over the levels above the leaves: one block per (slice, 128 rows).
 __global__ void __launch_bounds__(THREADS, 1) k_ut_tc(FarOp op, const CUtensorMap* __restrict__ umaps,
                                                       const float* __restrict__ T, int64_t N,
-                                                      double* __restrict__ Ynl, int* __restrict__ err) {
+                                                      double* __restrict__ Ynl, int64_t lo_off,
+                                                      int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ uint64_t bar[NBAR];
   __shared__ uint32_t tslot;
@@ -845,6 +842,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_ut_tc(FarOp op, const CUtensorMa
   src.ynl = Ynl;
   src.N = N;
   src.r0 = r0;
+  src.lo_off = lo_off;
   if (run_stream(src, smem, bar, tmem, err, &abort_flag) == 0 && threadIdx.x < WORKERS) {
     float z[NCOL] = {};
     src.finish(0, z, z, z);
@@ -852,14 +850,17 @@ __global__ void __launch_bounds__(THREADS, 1) k_ut_tc(FarOp op, const CUtensorMa
   block_teardown(tmem);
 }
 
-// X (original order, column-major) -> Xt[c * N + t] in tree order, split-exact FP32
+// X (original order, column-major) -> Xt[c * N + t] in tree order, split-exact
+// FP32, and its low parts at Xt[lo_off + c * N + t]
 __global__ void k_gather_xt(int64_t N, int nrhs, const double* __restrict__ X, int64_t ldx,
-                            const int32_t* __restrict__ perm, float* __restrict__ Xt) {
+                            const int32_t* __restrict__ perm, float* __restrict__ Xt, int64_t lo_off) {
   const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (o >= N * NR) return;
   const int c = (int)(o / N);
   const int64_t t = o - (int64_t)c * N;
-  Xt[o] = c < nrhs ? tf32_split_value(X[c * ldx + perm[t]]) : 0.f;
+  const float v = c < nrhs ? tf32_split_value(X[c * ldx + perm[t]]) : 0.f;
+  Xt[o] = v;
+  Xt[o + lo_off] = v - tf32_rz(v);
 }
 
 // Near-field blocks of every leaf: for neighbour slot s (0..25, 26 = the leaf
@@ -1256,6 +1257,8 @@ __global__ void __launch_bounds__(lr::THREADS, 1) k_leaf_rows_tc(
       if ((tid & 31) == 0) tc::mbar_arrive(&bar[lr::BAR_EMPTY + s]);
       {
         // low parts of this thread's two B segments of chunk c, next to B_hi
+        // (here cheaper than copying the precomputed ones: the copies of
+        // this kernel are not hidden behind its split)
         cp_async_wait<0>();
         unsigned char* bs = smem + lr::B_OFF + (c % lr::kBSlots) * lr::B_BYTES;
 #pragma unroll
@@ -1357,7 +1360,7 @@ int launch_matvec_tc(cudaStream_t s, int64_t N, const int32_t* perm, const FarOp
   const CUtensorMap* rmaps = static_cast<const CUtensorMap*>(B.rmaps);
   int launches = 0;
   if (prof) prof->begin(s);
-  k_gather_xt<<<(unsigned)((N * NR + 255) / 256), 256, 0, s>>>(N, nrhs, X, ldx, perm, B.xt);
+  k_gather_xt<<<(unsigned)((N * NR + 255) / 256), 256, 0, s>>>(N, nrhs, X, ldx, perm, B.xt, B.lo_off);
   ++launches;
   if (prof) prof->mark(s, "gather");
   const int d = far.levels;
@@ -1367,17 +1370,17 @@ int launch_matvec_tc(cudaStream_t s, int64_t N, const int32_t* perm, const FarOp
     // several blocks share a slice's row tiles when slices are few
     const int split = (int)std::max<int64_t>(1, std::min<int64_t>(32, (16 * 152) / nslice));
     k_ta_tc<true><<<dim3((unsigned)nslice, (unsigned)split), THREADS, SMEM_BYTES, s>>>(
-        far, vmaps, B.xt, N, B.t, B.p, B.err);
+        far, vmaps, B.xt, N, B.t, B.p, B.lo_off, B.err);
     ++launches;
     if (prof) prof->mark(s, "ta_slice");
     if (B.n_upper > 0) {
-      k_tred_tc<<<(unsigned)B.n_upper, 256, 0, s>>>(far, B.upper_pairs, B.p, B.t);
+      k_tred_tc<<<(unsigned)B.n_upper, 256, 0, s>>>(far, B.upper_pairs, B.p, B.t, B.lo_off);
       ++launches;
       if (prof) prof->mark(s, "tred");
     }
     const int tiles = (B.max_slice + 127) / 128;
     k_ut_tc<<<dim3((unsigned)nslice, (unsigned)std::max(1, tiles)), THREADS, SMEM_BYTES, s>>>(
-        far, umaps, B.t, N, B.ynl, B.err);
+        far, umaps, B.t, N, B.ynl, B.lo_off, B.err);
     ++launches;
     if (prof) prof->mark(s, "ut_tc");
   }

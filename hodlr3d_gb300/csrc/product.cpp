@@ -559,11 +559,14 @@ int run_tc(hodlr3d_t h, const h3d::FarOp& far, const h3d::NearOp& nr, const doub
   }
   H3D_TRY(ensure_leaf_rows(h, nr, s));
   if (!h->maps_built) H3D_TRY(build_tensor_maps(h));
-  // [X | T], the B operands in the split-exact form
-  H3D_CUDA(h->tct.ensure(sizeof(float) * 32 * (h->N + std::max<int64_t>(h->sum_rank4, 1))));
+  // [X | T | X_lo | T_lo], the B operands in the split-exact form and their
+  // low parts (v - v with the 13 low mantissa bits cleared)
+  const int64_t xt_floats = 32 * (h->N + std::max<int64_t>(h->sum_rank4, 1));
+  H3D_CUDA(h->tct.ensure(sizeof(float) * 2 * xt_floats));
   h3d::TcBuffers T{};
   T.xt = h->tct.as<float>();
   T.t = T.xt + 32 * h->N;
+  T.lo_off = xt_floats;
   T.p = reinterpret_cast<float*>(h->pbuf.p);
   T.ynl = h->ynl.as<double>();
   T.err = h->dev_err.as<int>();
