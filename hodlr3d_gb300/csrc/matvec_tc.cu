@@ -957,11 +957,11 @@ __global__ void k_near_lo(const int32_t* __restrict__ leaf_off, NearOp nr,
 // and exits.
 namespace lr {
 // roles of the leaf-row kernel: 16 worker warps (four per 32 TMEM lanes, one
-// K quarter each), 2 issuer warps, 1 producer warp
+// K quarter each), 1 issuer warp, 1 producer warp
 constexpr int WORKERS = 512;
 constexpr int ISSUER0 = WORKERS;
-constexpr int PRODUCER = WORKERS + 64;
-constexpr int THREADS = WORKERS + 96;
+constexpr int PRODUCER = WORKERS + 32;
+constexpr int THREADS = WORKERS + 64;
 constexpr int NCOL = 8;                     // accumulator columns per worker
 constexpr int KC = 64;
 constexpr int NB = 2 * NR;                  // B columns: top and bottom right-hand sides
@@ -973,21 +973,23 @@ constexpr int A_BYTES = 2 * A_HALF;         // an A slot: 32 KB
 constexpr int B_HALF = 2 * NB * 32 * 4;
 constexpr int B_LO = NB * 128;
 constexpr int B_BYTES = 2 * B_HALF;         // a B slot: 32 KB
-constexpr int kASlots = 4;                  // A tiles in flight (freed once split)
-constexpr int kBSlots = 2;                  // B tiles (freed once multiplied)
+constexpr int kASlots = 3;                  // A tiles in flight (freed once split)
+constexpr int kBSlots = 3;                  // B tiles (freed once multiplied), one copied ahead
 constexpr int B_OFF = kASlots * A_BYTES;
 constexpr int kMaxBlocks = 512;             // blocks of one leaf row (table in shared memory)
 constexpr int TAB_OFF = B_OFF + kBSlots * B_BYTES;
 constexpr int SMEM_BYTES = TAB_OFF + kMaxBlocks * (int)sizeof(LeafBlock);
 constexpr uint32_t IDESC_HL = tc::idesc_tf32(128, 2 * NB);  // A_hi [B_hi | B_lo]
 constexpr uint32_t IDESC_LH = tc::idesc_tf32(128, NB);      // A_lo B_hi
-// tensor memory (512 columns): the accumulators [HH | X1] (N = 128) at 0 and
-// X2 (N = 64) at 128; A buffer b (hi 64, lo 64 columns) at 256 + 128 b
-constexpr uint32_t TM_X2 = 128;
+// tensor memory (512 columns): the accumulator of chunk c at 128 (c % 2)
+// ([HH | X] with X = hi*lo + lo*hi, N = 128); A buffer c % 2 (hi 64, lo 64
+// columns) at 256 + 128 (c % 2)
+constexpr uint32_t TM_ACC = 128;
 constexpr uint32_t TM_A = 256;
 constexpr uint32_t TM_ASTRIDE = 128;
-constexpr int BAR_FULL = 0, BAR_EMPTY = kASlots, BAR_READY = 2 * kASlots, BAR_ACC = BAR_READY + 1,
-              BAR_DRAIN = BAR_ACC + 1, NBAR = BAR_DRAIN + 2;
+// FULL / EMPTY per A slot; READY / DONE per chunk parity (split / multiplied)
+constexpr int BAR_FULL = 0, BAR_EMPTY = kASlots, BAR_READY = 2 * kASlots, BAR_DONE = BAR_READY + 2,
+              BAR_DRAIN = BAR_DONE + 2, NBAR = BAR_DRAIN + 1;
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
 static_assert(64 * NR * 8 <= A_BYTES, "combine buffer fits an A slot");
 
@@ -1001,9 +1003,8 @@ __device__ __forceinline__ void give_up(int* err, volatile int* flag) {
 // rows of the workers' named barrier (barrier 1, the 512 worker threads)
 __device__ __forceinline__ void workers_sync() { asm volatile("bar.sync 1, %0;\n" ::"n"(lr::WORKERS) : "memory"); }
 
-__device__ __forceinline__ void tmem_ld8x3(uint32_t a0, uint32_t a1, uint32_t a2, float* v0, float* v1,
-                                           float* v2) {
-  uint32_t r[24];
+__device__ __forceinline__ void tmem_ld8x2(uint32_t a0, uint32_t a1, float* v0, float* v1) {
+  uint32_t r[16];
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
                  "=r"(r[7])
@@ -1012,16 +1013,11 @@ __device__ __forceinline__ void tmem_ld8x3(uint32_t a0, uint32_t a1, uint32_t a2
                : "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
                  "=r"(r[14]), "=r"(r[15])
                : "r"(a1));
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
-               : "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
-                 "=r"(r[22]), "=r"(r[23])
-               : "r"(a2));
   asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     v0[i] = __uint_as_float(r[i]);
     v1[i] = __uint_as_float(r[8 + i]);
-    v2[i] = __uint_as_float(r[16 + i]);
   }
 }
 }  // namespace lr
@@ -1111,10 +1107,11 @@ __global__ void __launch_bounds__(lr::THREADS, 1) k_leaf_rows_tc(
       tc::mbar_init(&bar[lr::BAR_FULL + i], 1);
       tc::mbar_init(&bar[lr::BAR_EMPTY + i], lr::WORKERS / 32);
     }
-    tc::mbar_init(&bar[lr::BAR_READY], lr::WORKERS / 32);
-    tc::mbar_init(&bar[lr::BAR_ACC], 2);
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&bar[lr::BAR_READY + i], lr::WORKERS / 32);
+      tc::mbar_init(&bar[lr::BAR_DONE + i], 1);
+    }
     tc::mbar_init(&bar[lr::BAR_DRAIN], 1);
-    tc::mbar_init(&bar[lr::BAR_DRAIN + 1], 1);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   tc::fence_before_sync();
@@ -1152,27 +1149,30 @@ __global__ void __launch_bounds__(lr::THREADS, 1) k_leaf_rows_tc(
           lr::give_up(err, abortp);
     }
   } else if (tid >= lr::ISSUER0) {
-    // issuers (lane 0 of warps 16 and 17): A_hi [B_hi | B_lo] -> [HH | X1],
-    // A_lo B_hi -> X2, A from tensor memory
-    if ((tid & 31) == 0) {
-      const bool second = tid >= lr::ISSUER0 + 32;
+    // the issuer (lane 0 of warp 16), per K step of 8: A_hi [B_hi | B_lo] ->
+    // [HH | X] (N = 128), then A_lo B_hi -> X (N = 64, accumulating), A from
+    // tensor memory; in order from one thread
+    if (tid == lr::ISSUER0) {
       for (int c = 0; c < nch; ++c) {
-        if (!tc::mbar_wait_try(&bar[lr::BAR_READY], (uint32_t)(c & 1)))
+        if (!tc::mbar_wait_try(&bar[lr::BAR_READY + (c & 1)], (uint32_t)((c >> 1) & 1)))
           lr::give_up(err, abortp);
         if (lr::aborted(abortp)) break;
         tc::fence_after_sync();
         const uint32_t b0 = tc::smem_addr(smem + lr::B_OFF + (c % lr::kBSlots) * lr::B_BYTES);
-        const uint32_t ab = tmem + lr::TM_A + lr::TM_ASTRIDE * (uint32_t)(c & 1) + (second ? 64u : 0u);
+        const uint32_t ab = tmem + lr::TM_A + lr::TM_ASTRIDE * (uint32_t)(c & 1);
+        const uint32_t d = tmem + lr::TM_ACC * (uint32_t)(c & 1);
 #pragma unroll
-        for (int ks = 0; ks < lr::KC / 8; ++ks)
-          tc::mma_tf32_ta(tmem + (second ? lr::TM_X2 : 0u), ab + 8u * ks,
-                          desc_sw128(b0 + (uint32_t)((ks >> 2) * lr::B_HALF + (ks & 3) * 32)),
-                          second ? lr::IDESC_LH : lr::IDESC_HL, ks > 0 ? 1u : 0u);
-        tc::mma_commit(&bar[lr::BAR_ACC]);
+        for (int ks = 0; ks < lr::KC / 8; ++ks) {
+          const uint64_t bd = desc_sw128(b0 + (uint32_t)((ks >> 2) * lr::B_HALF + (ks & 3) * 32));
+          tc::mma_tf32_ta(d, ab + 8u * ks, bd, lr::IDESC_HL, ks > 0 ? 1u : 0u);
+          tc::mma_tf32_ta(d + (uint32_t)lr::NB, ab + 64u + 8u * ks, bd, lr::IDESC_LH, 1u);
+        }
+        // chunk c multiplied: its accumulator complete, its A buffer and B slot free
+        tc::mma_commit(&bar[lr::BAR_DONE + (c & 1)]);
       }
       // the products issued so far complete before the block frees tensor memory
-      tc::mma_commit(&bar[lr::BAR_DRAIN + (second ? 1 : 0)]);
-      if (!tc::mbar_wait_sleep(&bar[lr::BAR_DRAIN + (second ? 1 : 0)], 0u, kWaitLimit, kWaitHintNs))
+      tc::mma_commit(&bar[lr::BAR_DRAIN]);
+      if (!tc::mbar_wait_sleep(&bar[lr::BAR_DRAIN], 0u, kWaitLimit, kWaitHintNs))
         lr::give_up(err, abortp);
     }
   } else {
@@ -1207,32 +1207,42 @@ __global__ void __launch_bounds__(lr::THREADS, 1) k_leaf_rows_tc(
       cp_async16(bs + boff_bot, srcb, okb);
       cp_async_commit();
     };
+    // waits for chunk c's products, then its accumulator into the sums
     auto read = [&](int c) {
-      const uint32_t acc = tmem + (bottom ? (uint32_t)NR : 0u) + (uint32_t)(lr::NCOL * kq) + lane_base;
-      if (!tc::mbar_wait_try(&bar[lr::BAR_ACC], (uint32_t)(c & 1)))
+      if (!tc::mbar_wait_try(&bar[lr::BAR_DONE + (c & 1)], (uint32_t)((c >> 1) & 1)))
         lr::give_up(err, abortp);
+      const uint32_t acc = tmem + lr::TM_ACC * (uint32_t)(c & 1) + (bottom ? (uint32_t)NR : 0u) +
+                           (uint32_t)(lr::NCOL * kq) + lane_base;
       tc::fence_after_sync();
-      float hh[lr::NCOL], x1[lr::NCOL], x2[lr::NCOL];
-      lr::tmem_ld8x3(acc, acc + (uint32_t)lr::NB, acc + lr::TM_X2, hh, x1, x2);
+      float hh[lr::NCOL], xx[lr::NCOL];
+      lr::tmem_ld8x2(acc, acc + (uint32_t)lr::NB, hh, xx);
       tc::fence_before_sync();
 #pragma unroll
       for (int j = 0; j < lr::NCOL; ++j) {
         kahan_add(sum[j], comp[j], hh[j]);
-        cross[j] += x1[j] + x2[j];
+        cross[j] += xx[j];
       }
     };
 
+    // iteration c: chunk c - 2 multiplied (its A buffer and its B slot, the
+    // one chunk c + 1 fills, are free) and read back (its accumulator is the
+    // one chunk c writes), then chunk c split and handed to the issuer while
+    // chunk c - 1 is multiplied; the last two chunks are read after the loop
     if (nch > 0) load_b(0);
     int c = 0;
     for (; c < nch; ++c) {
       const int s = c % lr::kASlots;
+      if (c >= 2) {
+        read(c - 2);
+        if (lr::aborted(abortp)) break;
+      }
+      if (c + 1 < nch) load_b(c + 1);
       if (!tc::mbar_wait_try(&bar[lr::BAR_FULL + s], (uint32_t)((c / lr::kASlots) & 1)))
         lr::give_up(err, abortp);
       if (lr::aborted(abortp)) break;
       {
         // row R, 16 K values, from the swizzled tile of its K half: hi (the
-        // value itself) and lo into A buffer c % 2, whose last reader (chunk
-        // c - 2) is complete (its accumulators were read back)
+        // value itself) and lo into A buffer c % 2
         const unsigned char* sa = smem + s * lr::A_BYTES + (kq >> 1) * lr::A_HALF + (uint32_t)R * 128u;
         float hi[16], lo[16];
 #pragma unroll
@@ -1259,7 +1269,8 @@ __global__ void __launch_bounds__(lr::THREADS, 1) k_leaf_rows_tc(
         // low parts of this thread's two B segments of chunk c, next to B_hi
         // (here cheaper than copying the precomputed ones: the copies of
         // this kernel are not hidden behind its split)
-        cp_async_wait<0>();
+        if (c + 1 < nch) cp_async_wait<1>();
+        else cp_async_wait<0>();
         unsigned char* bs = smem + lr::B_OFF + (c % lr::kBSlots) * lr::B_BYTES;
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
@@ -1274,16 +1285,13 @@ __global__ void __launch_bounds__(lr::THREADS, 1) k_leaf_rows_tc(
         }
       }
       tc::tmem_wait_st();
-      // chunk c - 1's accumulators back (the products of chunk c overwrite
-      // them), then B of chunk c + 1 into the slot chunk c - 1 read
-      if (c >= 1) read(c - 1);
-      if (c + 1 < nch) load_b(c + 1);
       tc::fence_async_smem();
       tc::fence_before_sync();
       __syncwarp();
-      if ((tid & 31) == 0) tc::mbar_arrive(&bar[lr::BAR_READY]);
+      if ((tid & 31) == 0) tc::mbar_arrive(&bar[lr::BAR_READY + (c & 1)]);
     }
-    if (c == nch && nch > 0) read(nch - 1);
+    if (c == nch)
+      for (int r = nch >= 2 ? nch - 2 : 0; r < nch && !lr::aborted(abortp); ++r) read(r);
     cp_async_wait<0>();
     // combine the halves: the bottom rows' sums go through shared memory
     // (A slot 0, free once every worker is past its last chunk)
