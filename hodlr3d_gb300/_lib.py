@@ -116,6 +116,7 @@ def lib() -> ctypes.CDLL:
         "hodlr3d_autotune": ([vp, i32, ctypes.c_char_p, i32], i32),
         "hodlr3d_get_tuning": ([vp, vp], i32),
         "hodlr3d_device_status": ([vp], i32),
+        "hodlr3d_test_drop_copy": ([vp, i32], i32),
         "hodlr3d_matvec_noalloc": ([vp, vp, vp, i32, i64, i32, vp], i32),
         "hodlr3d_profile_report": ([vp, ctypes.c_char_p, i32], i32),
     }

@@ -569,9 +569,19 @@ int hodlr3d_device_status(hodlr3d_t h) try {
   H3D_CUDA(cudaDeviceSynchronize());
   int v = 0;
   if (h->dev_err.p) H3D_CUDA(cudaMemcpy(&v, h->dev_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (v) H3D_CUDA(cudaMemset(h->dev_err.p, 0, sizeof(int)));  // reported once
   if (v == 2)
     return set_error(HODLR3D_ERR_CUDA, "a tensor-core block's operand table overflowed (results of that call are invalid)");
   if (v) return set_error(HODLR3D_ERR_CUDA, "a tensor-core wait gave up (results of that call are invalid)");
+  return HODLR3D_OK;
+} catch (...) {
+  return exception_status();
+}
+
+int hodlr3d_test_drop_copy(hodlr3d_t h, int chunk) try {
+  H3D_TRY(check_handle(h));
+  if (chunk < -1) return set_error(HODLR3D_ERR_INVALID_ARG, "chunk %d < -1", chunk);
+  H3D_CUDA(h3d::tc_set_drop_chunk(chunk));
   return HODLR3D_OK;
 } catch (...) {
   return exception_status();

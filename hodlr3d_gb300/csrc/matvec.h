@@ -143,6 +143,9 @@ int launch_matvec_tc(cudaStream_t s, int64_t N, const int32_t* perm, const FarOp
 int tc_max_entries();
 // Largest number of dense blocks in one leaf row of the tensor-core engine.
 int tc_max_row_blocks();
+// Test hook: the next T-kernel launch's block (0, 0) stops copying before
+// chunk `chunk` (-1: off), so that its bounded waits give up.
+cudaError_t tc_set_drop_chunk(int chunk);
 // Evaluates the dense FP32 blocks of the leaf rows (split-exact form): block
 // i of leaf k at column blocks[block_ptr[k] + i].x0 of the nk x row_ld[k]
 // row-major matrix at Krow + row_base[k]; max_blocks = the largest count.

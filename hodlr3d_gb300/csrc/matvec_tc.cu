@@ -230,6 +230,12 @@ __device__ __forceinline__ void stream_give_up(int* err, volatile int* abortp) {
   *abortp = 1;
 }
 
+// Test hook (hodlr3d_test_drop_copy): the producer of T-kernel block (0, 0)
+// of the next launch stops before the copy of chunk g_drop_chunk, so the
+// "landed" barrier of that chunk is never completed and the block's waits
+// give up; read and cleared by that block (-1: off).
+__device__ int g_drop_chunk = -1;
+
 template <class Src>
 __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t tmem, int* err,
                           volatile int* abortp) {
@@ -243,6 +249,7 @@ __device__ int run_stream(Src& src, unsigned char* smem, uint64_t* bar, uint32_t
     int issued = 0;
     for (int c = 0; c < nch; ++c) {
       const int s = c % kSlots;
+      if (c == src.drop) break;  // test hook: this chunk is never copied
       if (lane == 0 && c >= kSlots &&
           !tc::mbar_wait_spin(&bar[BAR_EMPTY + s], (uint32_t)(((c / kSlots) - 1) & 1)))
         stream_give_up(err, abortp);
@@ -484,6 +491,7 @@ struct SrcTa {
   // producer state (lane 0): the box of its current tile
   int pk = 0, pc = 0, px = 0, py = 0;
   const CUtensorMap* pmap = nullptr;
+  int drop = -1;  // test hook: the chunk the producer stops before (-1: none)
   // worker state: K offset of the next B copy; the level, its first and
   // last-plus-one tiles and rows, and the table entry of this thread's row in
   // the last finished tile (rows only move forward)
@@ -688,6 +696,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_ta_tc(FarOp op, const CUtensorMa
   src.b = Xt + i0;
   src.bs = N;
   src.lo_off = lo_off;
+  if (blockIdx.x == 0 && blockIdx.y == 0) {
+    src.drop = *(volatile int*)&g_drop_chunk;
+    __syncthreads();
+    if (threadIdx.x == 0) g_drop_chunk = -1;
+  }
   run_stream(src, smem, bar, tmem, err, &abort_flag);
   block_teardown(tmem);
 }
@@ -720,6 +733,7 @@ struct SrcItems {
   int n;
   int nrows;
   int ntile, cpt;
+  int drop = -1;  // test hook of the T kernel: never set here
   // producer cursor (lane 0): item, K offset, the item's map, row and K
   int pi = -1, pk = 0, py = 0, plen = 0;
   const CUtensorMap* pmap = nullptr;
@@ -1334,6 +1348,9 @@ int launch_near_lo(cudaStream_t s, int64_t nleaf, const int32_t* leaf_off, const
 }
 
 int tc_max_entries() { return kMaxEntries; }
+cudaError_t tc_set_drop_chunk(int chunk) {
+  return cudaMemcpyToSymbol(g_drop_chunk, &chunk, sizeof(int));
+}
 int tc_max_row_blocks() { return lr::kMaxBlocks; }
 
 int launch_row_blocks(cudaStream_t s, int64_t nleaf, int max_blocks, const int32_t* leaf_off,

@@ -251,8 +251,17 @@ int hodlr3d_autotune(hodlr3d_t h, int reps, char* report, int cap);
  * column-count rules apply. */
 int hodlr3d_get_tuning(hodlr3d_t h, int32_t* choice);
 /* Synchronises the device and reports HODLR3D_ERR_CUDA if a bounded
- * tensor-core wait gave up in an earlier call on this handle. */
+ * tensor-core wait gave up in an earlier call on this handle, then clears
+ * that flag (the products of later calls are checked afresh). */
 int hodlr3d_device_status(hodlr3d_t h);
+/* Testing of the bounded waits: in the next tensor-core product on this
+ * handle's device, block (0, 0) of the T kernel copies its chunks only up to
+ * chunk `chunk` (one-shot; -1: off).  The chunk's "landed" barrier is never
+ * completed, the block's waits give up after about a second each, the block
+ * drains its copies and products in flight and frees its tensor memory, and
+ * hodlr3d_device_status reports the failure; that product's results are
+ * invalid.  No reference counterpart. */
+int hodlr3d_test_drop_copy(hodlr3d_t h, int chunk);
 /* Per-kernel timing of the matvec launches with CUDA events recorded between
  * them on the launch stream (off by default).  The report lists one line per
  * kernel, "name launches total_ms", accumulated since the last report. */
