@@ -101,8 +101,12 @@ __device__ void col_pass(const AcaTask& T, const PointsF64& P, const KernelDesc&
   block_argmax<BS>(bv, bi, S, amax, aidx);
 }
 
+// 64-thread blocks (leaf pairs): 16 per SM at 64 registers.  256-thread
+// blocks (the larger pairs): one per SM with all the registers they want
+// (134, nothing spilled); held to 64 registers so that four fit, they spill
+// and run slower: 5.8 s of ACA kernels at 64^3 against 6.8-7.0 s.
 template <int BS>
-__global__ void __launch_bounds__(BS) k_aca(const AcaTask* __restrict__ tasks, int ntasks,
+__global__ void __launch_bounds__(BS, BS == 64 ? 16 : 1) k_aca(const AcaTask* __restrict__ tasks, int ntasks,
                                             int* __restrict__ counter, PointsF64 P, KernelDesc kd,
                                             double tol, double* __restrict__ ws,
                                             unsigned char* __restrict__ flags,

@@ -398,7 +398,7 @@ int run_aca_batch(hodlr3d_t h, std::vector<HostTask>& batch, std::vector<HostTas
   H3D_CUDA(cudaMemsetAsync(d_counter.p, 0, sizeof(int32_t), s));
   const int block = small_kernel ? 64 : 256;
   const size_t shm = h3d::aca_shared_bytes(cap_max);
-  int per_sm = small_kernel ? 16 : 4;
+  int per_sm = small_kernel ? 16 : 1;  // as k_aca's launch bounds allow
   if (shm > 0) {
     const int by_shm = (int)std::max<size_t>(1, (200 * 1024) / (shm + 2048));
     per_sm = std::max(1, std::min(per_sm, by_shm));
