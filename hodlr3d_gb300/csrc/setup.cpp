@@ -362,16 +362,64 @@ int group_fp32(hodlr3d_t h) {
   return HODLR3D_OK;
 }
 
-int run_aca_batch(hodlr3d_t h, std::vector<HostTask>& batch, std::vector<HostTask>& retry,
-                  bool small_kernel) {
-  cudaStream_t s = h->stream;
-  const int nt = (int)batch.size();
-  std::vector<h3d::AcaTask> tasks(nt);
+// The ACA batches of one pass: device buffers sized once for the largest
+// batch and the batch in flight.
+struct AcaLane {
+  cudaStream_t s = nullptr;
+  DevBuf d_tasks, d_ws, d_fl, d_pv, d_rank, d_status, d_counter, d_off;
+  EventPair ev;
+  std::vector<HostTask> batch;
+  std::vector<h3d::AcaTask> tasks;
+  int64_t pv = 0;
+  bool small = false;
+};
+
+// workspace doubles, flag bytes and pivot entries of a batch
+void batch_sizes(const std::vector<HostTask>& batch, int64_t& ws, int64_t& fl, int64_t& pv) {
+  ws = fl = pv = 0;
+  for (const HostTask& b : batch) {
+    ws += (int64_t)b.cap * (b.n + b.m);
+    fl += b.n + b.m;
+    pv += 2 * (int64_t)b.cap;
+  }
+}
+
+// Sizes the lane's buffers for the largest of its batches.
+int aca_lane_reserve(AcaLane& L, const std::vector<std::vector<HostTask>>& batches) {
+  int64_t nt = 1, ws = 1, fl = 1, pv = 1;
+  for (const auto& b : batches) {
+    int64_t w, f, p;
+    batch_sizes(b, w, f, p);
+    nt = std::max<int64_t>(nt, (int64_t)b.size());
+    ws = std::max(ws, w);
+    fl = std::max(fl, f);
+    pv = std::max(pv, p);
+  }
+  H3D_CUDA(L.d_tasks.ensure(sizeof(h3d::AcaTask) * nt));
+  H3D_CUDA(L.d_ws.ensure(sizeof(double) * ws));
+  H3D_CUDA(L.d_fl.ensure(fl));
+  H3D_CUDA(L.d_pv.ensure(sizeof(int32_t) * pv));
+  H3D_CUDA(L.d_rank.ensure(sizeof(int32_t) * nt));
+  H3D_CUDA(L.d_status.ensure(sizeof(int32_t) * nt));
+  H3D_CUDA(L.d_counter.ensure(sizeof(int32_t)));
+  H3D_CUDA(L.d_off.ensure(sizeof(int64_t) * nt));
+  if (!L.ev.a) H3D_CUDA(cudaEventCreate(&L.ev.a));
+  if (!L.ev.b) H3D_CUDA(cudaEventCreate(&L.ev.b));
+  return HODLR3D_OK;
+}
+
+// Launches the ACA of a batch on the lane's stream (no host synchronisation).
+int aca_launch(hodlr3d_t h, AcaLane& L, std::vector<HostTask>&& batch, bool small_kernel) {
+  cudaStream_t s = L.s;
+  L.batch = std::move(batch);
+  L.small = small_kernel;
+  const int nt = (int)L.batch.size();
+  L.tasks.assign(nt, h3d::AcaTask{});
   int64_t ws = 0, fl = 0, pv = 0;
   int cap_max = 1;
   for (int i = 0; i < nt; ++i) {
-    const HostTask& b = batch[i];
-    h3d::AcaTask& t = tasks[i];
+    const HostTask& b = L.batch[i];
+    h3d::AcaTask& t = L.tasks[i];
     t.t0 = b.t0;
     t.n = b.n;
     t.s0 = b.s0;
@@ -386,16 +434,9 @@ int run_aca_batch(hodlr3d_t h, std::vector<HostTask>& batch, std::vector<HostTas
     pv += 2 * (int64_t)b.cap;
     cap_max = std::max(cap_max, b.cap);
   }
-  DevBuf d_tasks, d_ws, d_fl, d_pv, d_rank, d_status, d_counter, d_off;
-  H3D_CUDA(d_tasks.ensure(sizeof(h3d::AcaTask) * nt));
-  H3D_CUDA(d_ws.ensure(sizeof(double) * std::max<int64_t>(ws, 1)));
-  H3D_CUDA(d_fl.ensure(std::max<int64_t>(fl, 1)));
-  H3D_CUDA(d_pv.ensure(sizeof(int32_t) * std::max<int64_t>(pv, 1)));
-  H3D_CUDA(d_rank.ensure(sizeof(int32_t) * nt));
-  H3D_CUDA(d_status.ensure(sizeof(int32_t) * nt));
-  H3D_CUDA(d_counter.ensure(sizeof(int32_t)));
-  H3D_CUDA(cudaMemcpyAsync(d_tasks.p, tasks.data(), sizeof(h3d::AcaTask) * nt, cudaMemcpyHostToDevice, s));
-  H3D_CUDA(cudaMemsetAsync(d_counter.p, 0, sizeof(int32_t), s));
+  L.pv = pv;
+  H3D_CUDA(cudaMemcpyAsync(L.d_tasks.p, L.tasks.data(), sizeof(h3d::AcaTask) * nt, cudaMemcpyHostToDevice, s));
+  H3D_CUDA(cudaMemsetAsync(L.d_counter.p, 0, sizeof(int32_t), s));
   const int block = small_kernel ? 64 : 256;
   const size_t shm = h3d::aca_shared_bytes(cap_max);
   int per_sm = small_kernel ? 16 : 1;  // as k_aca's launch bounds allow
@@ -405,26 +446,32 @@ int run_aca_batch(hodlr3d_t h, std::vector<HostTask>& batch, std::vector<HostTas
   }
   const int grid = std::max(1, std::min(nt, h->num_sms * per_sm));
   h3d::PointsF64 P{h->xs.as<double>(), h->ys.as<double>(), h->zs.as<double>()};
-  EventPair ev;
-  H3D_CUDA(cudaEventCreate(&ev.a));
-  H3D_CUDA(cudaEventCreate(&ev.b));
-  H3D_CUDA(cudaEventRecord(ev.a, s));
-  H3D_CUDA(h3d::launch_aca(s, block, grid, d_tasks.as<h3d::AcaTask>(), nt, d_counter.as<int>(), P,
-                           h->kd, h->tol, d_ws.as<double>(), d_fl.as<unsigned char>(),
-                           d_pv.as<int32_t>(), d_rank.as<int32_t>(), d_status.as<int32_t>(),
+  H3D_CUDA(cudaEventRecord(L.ev.a, s));
+  H3D_CUDA(h3d::launch_aca(s, block, grid, L.d_tasks.as<h3d::AcaTask>(), nt, L.d_counter.as<int>(), P,
+                           h->kd, h->tol, L.d_ws.as<double>(), L.d_fl.as<unsigned char>(),
+                           L.d_pv.as<int32_t>(), L.d_rank.as<int32_t>(), L.d_status.as<int32_t>(),
                            cap_max));
-  H3D_CUDA(cudaEventRecord(ev.b, s));
+  H3D_CUDA(cudaEventRecord(L.ev.b, s));
   ++h->launches;
-  std::vector<int32_t> rk(nt), st(nt), pvh(pv);
-  H3D_CUDA(cudaMemcpyAsync(rk.data(), d_rank.p, sizeof(int32_t) * nt, cudaMemcpyDeviceToHost, s));
-  H3D_CUDA(cudaMemcpyAsync(st.data(), d_status.p, sizeof(int32_t) * nt, cudaMemcpyDeviceToHost, s));
-  if (pv) H3D_CUDA(cudaMemcpyAsync(pvh.data(), d_pv.p, sizeof(int32_t) * pv, cudaMemcpyDeviceToHost, s));
+  return HODLR3D_OK;
+}
+
+// Waits for the lane's batch: ranks and pivots to the host, finished tasks
+// into an exact-size FP64 pool, capacity overflows into `retry` with twice
+// the capacity.
+int aca_finish(hodlr3d_t h, AcaLane& L, std::vector<HostTask>& retry) {
+  cudaStream_t s = L.s;
+  const std::vector<HostTask>& batch = L.batch;
+  const int nt = (int)batch.size();
+  std::vector<int32_t> rk(nt), st(nt), pvh(L.pv);
+  H3D_CUDA(cudaMemcpyAsync(rk.data(), L.d_rank.p, sizeof(int32_t) * nt, cudaMemcpyDeviceToHost, s));
+  H3D_CUDA(cudaMemcpyAsync(st.data(), L.d_status.p, sizeof(int32_t) * nt, cudaMemcpyDeviceToHost, s));
+  if (L.pv) H3D_CUDA(cudaMemcpyAsync(pvh.data(), L.d_pv.p, sizeof(int32_t) * L.pv, cudaMemcpyDeviceToHost, s));
   H3D_CUDA(cudaStreamSynchronize(s));
   H3D_CUDA(cudaGetLastError());
   float aca_ms = 0.f;
-  H3D_CUDA(cudaEventElapsedTime(&aca_ms, ev.a, ev.b));
+  H3D_CUDA(cudaEventElapsedTime(&aca_ms, L.ev.a, L.ev.b));
   h->aca_kernel_seconds += 1e-3 * aca_ms;
-  // finished tasks -> exact-size pools; capacity overflows -> retried with twice the capacity
   std::vector<int64_t> dst(nt, 0);
   int64_t total = 0;
   for (int i = 0; i < nt; ++i) {
@@ -446,11 +493,10 @@ int run_aca_batch(hodlr3d_t h, std::vector<HostTask>& batch, std::vector<HostTas
   h->pools.push_back(pool64);
   const int pool_id = (int)h->pools.size() - 1;
   H3D_CUDA(pool64->ensure(sizeof(double) * std::max<int64_t>(total, 1)));
-  H3D_CUDA(d_off.ensure(sizeof(int64_t) * nt));
-  H3D_CUDA(cudaMemcpyAsync(d_off.p, dst.data(), sizeof(int64_t) * nt, cudaMemcpyHostToDevice, s));
-  H3D_CUDA(cudaMemcpyAsync(d_rank.p, rk.data(), sizeof(int32_t) * nt, cudaMemcpyHostToDevice, s));
-  H3D_CUDA(h3d::launch_aca_compact(s, nt, d_tasks.as<h3d::AcaTask>(), d_rank.as<int32_t>(),
-                                   d_off.as<int64_t>(), d_ws.as<double>(), pool64->as<double>()));
+  H3D_CUDA(cudaMemcpyAsync(L.d_off.p, dst.data(), sizeof(int64_t) * nt, cudaMemcpyHostToDevice, s));
+  H3D_CUDA(cudaMemcpyAsync(L.d_rank.p, rk.data(), sizeof(int32_t) * nt, cudaMemcpyHostToDevice, s));
+  H3D_CUDA(h3d::launch_aca_compact(s, nt, L.d_tasks.as<h3d::AcaTask>(), L.d_rank.as<int32_t>(),
+                                   L.d_off.as<int64_t>(), L.d_ws.as<double>(), pool64->as<double>()));
   ++h->launches;
   for (int i = 0; i < nt; ++i) {
     if (st[i] == h3d::kAcaCapReached) continue;
@@ -462,12 +508,34 @@ int run_aca_batch(hodlr3d_t h, std::vector<HostTask>& batch, std::vector<HostTas
     h->h_fac_off[p] = dst[i];
     h->h_u64[p] = base64;
     h->h_v64[p] = base64 + (int64_t)r * batch[i].n;
-    const int32_t* pr = pvh.data() + tasks[i].piv_off;
+    const int32_t* pr = pvh.data() + L.tasks[i].piv_off;
     h->h_piv_rows[p].assign(pr, pr + r);
-    h->h_piv_cols[p].assign(pr + tasks[i].cap, pr + tasks[i].cap + r);
+    h->h_piv_cols[p].assign(pr + L.tasks[i].cap, pr + L.tasks[i].cap + r);
   }
   H3D_CUDA(cudaStreamSynchronize(s));
   ++h->aca_batches;
+  return HODLR3D_OK;
+}
+
+// The batches of one pass, one after another on the handle's stream: those
+// of the larger pairs (256-thread blocks, one per SM), then those of the leaf
+// pairs (64-thread blocks).  Running the first leaf batch on a second stream
+// beside the larger pairs' blocks (six per SM) did not shorten the assembly
+// at 64^3 (4.51 s either way): the leaf batch at that occupancy became the
+// longest, and both share the FP64 pipe.
+int run_aca_batches(hodlr3d_t h, std::vector<std::vector<HostTask>>& big,
+                    std::vector<std::vector<HostTask>>& small, std::vector<HostTask>& retry) {
+  AcaLane L;
+  L.s = h->stream;
+  std::vector<std::vector<HostTask>> all;
+  for (auto& b : big) all.push_back(std::move(b));
+  const size_t nbig = all.size();
+  for (auto& b : small) all.push_back(std::move(b));
+  H3D_TRY(aca_lane_reserve(L, all));
+  for (size_t k = 0; k < all.size(); ++k) {
+    H3D_TRY(aca_launch(h, L, std::move(all[k]), k >= nbig));
+    H3D_TRY(aca_finish(h, L, retry));
+  }
   return HODLR3D_OK;
 }
 
@@ -491,11 +559,12 @@ int assemble(hodlr3d_t h) {
   h->u32_pool = nullptr;
   h->aca_batches = 0;
   h->aca_kernel_seconds = 0.0;
-  // first rank capacity above leaf size: pairs that reach it run again with
-  // twice the capacity (same ranks and pivots).  128 and the workspace below:
-  // at 64^3 (1/r, tol 1e-10) 4 batches and 6.7-7.7 s against 20 and
-  // 8.9-11.1 s with 256 and 8 GiB in the same process (each batch waits for
-  // its slowest pair); 96 costs more in repeated pairs than it saves.
+  // first rank capacity above leaf size, 128 (twice that for boxes of 2048
+  // points and more): pairs that reach it run again with twice the capacity
+  // (same ranks and pivots).  With the workspace below, at 64^3 (1/r, tol
+  // 1e-10) 3 batches and 4.5 s; 256 for every pair above the leaves with an
+  // 8 GiB workspace took 20 batches and 8.9-11.1 s (each batch waits for its
+  // slowest pair); 96 costs more in repeated pairs than it saves.
   const int cap0 = h->opt.rank_cap > 0 ? h->opt.rank_cap : 128;
   std::vector<HostTask> todo;
   todo.reserve(np);
@@ -514,37 +583,43 @@ int assemble(hodlr3d_t h) {
     t.m = (int32_t)(b1 - b0);
     t.leaf = j == h->levels;
     const int mn = std::min(t.n, t.m);
-    t.cap = (t.leaf || mn <= cap0) ? mn : cap0;
+    // boxes of 2048 points and more start at twice the capacity: at 64^3 216
+    // of the level-2 pairs (4096 points) pass rank 128, and run again as a
+    // batch of their own that nothing overlaps (2.2 s of 6.0)
+    t.cap = (t.leaf || mn <= cap0) ? mn : (mn >= 2048 ? std::min(mn, 2 * cap0) : cap0);
     todo.push_back(t);
   }
   size_t budget = h->opt.aca_workspace_bytes;
-  if (!budget) {  // 32 GiB, or a quarter of the free device memory when less
+  if (!budget) {  // 64 GiB, or a quarter of the free device memory when less
     size_t free_b = 0, total_b = 0;
     H3D_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    budget = std::max<size_t>(size_t(1) << 30, std::min<size_t>(size_t(32) << 30, free_b / 4));
+    budget = std::max<size_t>(size_t(1) << 30, std::min<size_t>(size_t(64) << 30, free_b / 4));
   }
   while (!todo.empty()) {
-    // largest blocks first
+    // largest blocks first, in batches of at most `budget` bytes of workspace
+    // each, those of the larger pairs and those of the leaf pairs apart
     std::stable_sort(todo.begin(), todo.end(), [](const HostTask& a, const HostTask& b) {
       return (int64_t)a.n * a.m > (int64_t)b.n * b.m;
     });
-    std::vector<HostTask> retry;
+    std::vector<std::vector<HostTask>> big, small;
     size_t i = 0;
     while (i < todo.size()) {
-      const bool small = std::max(todo[i].n, todo[i].m) <= 128;
+      const bool is_small = std::max(todo[i].n, todo[i].m) <= 128;
       std::vector<HostTask> batch;
       size_t bytes = 0;
       while (i < todo.size()) {
         const HostTask& t = todo[i];
-        if ((std::max(t.n, t.m) <= 128) != small) break;
+        if ((std::max(t.n, t.m) <= 128) != is_small) break;
         const size_t tb = sizeof(double) * (size_t)t.cap * (t.n + t.m) + (t.n + t.m) + 8 * t.cap + 64;
         if (!batch.empty() && bytes + tb > budget) break;
         batch.push_back(t);
         bytes += tb;
         ++i;
       }
-      H3D_TRY(run_aca_batch(h, batch, retry, small));
+      (is_small ? small : big).push_back(std::move(batch));
     }
+    std::vector<HostTask> retry;
+    H3D_TRY(run_aca_batches(h, big, small, retry));
     todo.swap(retry);
   }
   return finish_assembly(h, t_start);

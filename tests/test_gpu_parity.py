@@ -167,3 +167,32 @@ def test_gmres_history_matches_reference(gcase):
     assert np.allclose(np.array(e[:n]), ref[:n], rtol=rtol, atol=1e-14)
     if ref[-1] <= 1e-10:
         assert np.linalg.norm(x - g["gmres_x"]) <= 1e-9 * np.linalg.norm(g["gmres_x"])
+
+
+def test_aca_capacity_retries_and_small_workspace_keep_ranks():
+    """A rank capacity of 8 and a 64 MiB workspace: most pairs above the
+    leaves reach the capacity and run again (capacities 8 -> 16 -> ... up to
+    their rank), the assembly takes many batches, and ranks, pivots and the
+    FP64 product are those of the reference all the same (grid32_q16_tol10)."""
+    from hodlr3d_gb300 import HODLR3D
+    from hodlr3d_gb300.workloads import charges_uniform
+    g = load("grid32_q16_tol10")
+    H = HODLR3D(int(g["nP1D"]), float(g["L"]), int(g["tol_pow"]), int(g["kernel"]), points_of(g),
+                diag_override=float(g["diag"]), aca_workspace_bytes=64 << 20, rank_cap=8)
+    try:
+        H.assemble()
+        st = H.stats()
+        assert st["aca_batches"] > 4, st["aca_batches"]
+        ranks = H.ranks()
+        assert np.array_equal(ranks, g["rank"].astype(np.int32))
+        rows, cols = H.pivots()
+        if "row_piv" in g:
+            assert np.array_equal(rows, g["row_piv"].astype(np.int32))
+            assert np.array_equal(cols, g["col_piv"].astype(np.int32))
+        else:
+            assert np.array_equal(pivot_crc_per_box(H.pairs(), ranks, rows, cols), g["piv_crc_box"])
+        q = charges_uniform(H.N, seed=1)
+        y = H.MatVecProduct(q, precision="fp64")
+        assert np.linalg.norm(y - g["matvec"]) <= 1e-12 * np.linalg.norm(g["matvec"])
+    finally:
+        H.close()
