@@ -101,10 +101,11 @@ __device__ void col_pass(const AcaTask& T, const PointsF64& P, const KernelDesc&
   block_argmax<BS>(bv, bi, S, amax, aidx);
 }
 
-// 64-thread blocks (leaf pairs): 16 per SM at 64 registers.  256-thread
-// blocks (the larger pairs): one per SM with all the registers they want
-// (134, nothing spilled); held to 64 registers so that four fit, they spill
-// and run slower: 5.8 s of ACA kernels at 64^3 against 6.8-7.0 s.
+// 64-thread blocks: 16 per SM at 64 registers (the leaf pairs run in
+// k_aca_warp, one warp each).  256-thread blocks (the larger pairs): one per
+// SM with all the registers they want (134, nothing spilled); held to 64
+// registers so that four fit, they spill and run slower: 5.8 s of ACA
+// kernels at 64^3 against 6.8-7.0 s.
 template <int BS>
 __global__ void __launch_bounds__(BS, BS == 64 ? 16 : 1) k_aca(const AcaTask* __restrict__ tasks, int ntasks,
                                             int* __restrict__ counter, PointsF64 P, KernelDesc kd,
@@ -264,6 +265,200 @@ __global__ void __launch_bounds__(BS, BS == 64 ? 16 : 1) k_aca(const AcaTask* __
   }
 }
 
+// One warp per pair (pairs of at most 128 points a side, the leaf level): the
+// steps of k_aca with warp shuffles for every reduction and no block
+// barrier, per-warp scratch (ubuf, vbuf, du, dv: cap_max doubles each) in
+// shared memory, each warp pulling pairs from the work counter.  Every
+// result is the same as k_aca's: the entries, residuals and quotients are the
+// same operations; the argmax is a total order (|value| descending, ties to
+// the lowest index) and the dot products canonical reductions, neither of
+// which depends on how the work is split.
+template <int WPB>
+__global__ void __launch_bounds__(32 * WPB, kAcaWarpBlocksPerSm) k_aca_warp(const AcaTask* __restrict__ tasks, int ntasks,
+                                                        int* __restrict__ counter, PointsF64 P,
+                                                        KernelDesc kd, double tol, int cap_max,
+                                                        double* __restrict__ ws,
+                                                        unsigned char* __restrict__ flags,
+                                                        int32_t* __restrict__ piv,
+                                                        int32_t* __restrict__ out_rank,
+                                                        int32_t* __restrict__ out_status) {
+  extern __shared__ double dyn[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double* ubuf = dyn + (size_t)4 * cap_max * w;
+  double* vbuf = ubuf + cap_max;
+  double* du = vbuf + cap_max;
+  double* dv = du + cap_max;
+  for (;;) {
+    int ti = 0;
+    if (lane == 0) ti = atomicAdd(counter, 1);
+    ti = __shfl_sync(0xffffffffu, ti, 0);
+    if (ti >= ntasks) break;
+    const AcaTask T = tasks[ti];
+    double* U = ws + T.ws_off;
+    double* V = U + (size_t)T.cap * T.n;
+    unsigned char* used_r = flags + T.fl_off;
+    unsigned char* used_c = used_r + T.n;
+    int32_t* rows = piv + T.piv_off;
+    int32_t* cols = rows + T.cap;
+    const int mn = min(T.n, T.m);
+    if (mn == 0 || T.cap == 0) {
+      if (lane == 0) {
+        out_rank[ti] = 0;
+        out_status[ti] = mn == 0 ? 0 : 1;
+      }
+      continue;
+    }
+    for (int i = lane; i < T.n + T.m; i += 32) used_r[i] = 0;
+    __syncwarp();
+    bool bad = false;
+    // residual row `row` with r terms -> V[:, r]; first max of |row| over
+    // unused columns (all lanes get it)
+    auto row_pass = [&](int row, int r, double& amax, int& aidx) {
+      const double xi = P.x[T.t0 + row], yi = P.y[T.t0 + row], zi = P.z[T.t0 + row];
+      double bv = 0.0;
+      int bi = -1;
+      bool b = false;
+      for (int s = lane; s < T.m; s += 32) {
+        const int q = T.s0 + s;
+        double e = entry64_offdiag(kd, __dsub_rn(xi, P.x[q]), __dsub_rn(yi, P.y[q]), __dsub_rn(zi, P.z[q]));
+        for (int l = 0; l < r; ++l) e = __dsub_rn(e, __dmul_rn(ubuf[l], V[(size_t)l * T.m + s]));
+        V[(size_t)r * T.m + s] = e;
+        if (!isfinite(e)) b = true;
+        if (!used_c[s]) argmax_merge(bv, bi, fabs(e), s);
+      }
+      bad = bad || __any_sync(0xffffffffu, b);
+      warp_argmax(bv, bi);
+      amax = bv;
+      aidx = bi;
+      __syncwarp();
+    };
+    // residual column `col` with r terms, divided by the pivot -> U[:, r];
+    // first max of |column| over unused rows
+    auto col_pass = [&](int col, int r, double pivot, double& amax, int& aidx) {
+      const int qc = T.s0 + col;
+      const double xj = P.x[qc], yj = P.y[qc], zj = P.z[qc];
+      double bv = 0.0;
+      int bi = -1;
+      bool b = false;
+      for (int t = lane; t < T.n; t += 32) {
+        const int q = T.t0 + t;
+        double e = entry64_offdiag(kd, __dsub_rn(P.x[q], xj), __dsub_rn(P.y[q], yj), __dsub_rn(P.z[q], zj));
+        for (int l = 0; l < r; ++l) e = __dsub_rn(e, __dmul_rn(vbuf[l], U[(size_t)l * T.n + t]));
+        const double u = __ddiv_rn(e, pivot);
+        U[(size_t)r * T.n + t] = u;
+        if (!isfinite(u)) b = true;
+        if (!used_r[t]) argmax_merge(bv, bi, fabs(e), t);
+      }
+      bad = bad || __any_sync(0xffffffffu, b);
+      warp_argmax(bv, bi);
+      amax = bv;
+      aidx = bi;
+      __syncwarp();
+    };
+    // first row with a maximum above 1e-16 (src/ACA.cpp:153-161)
+    double amax;
+    int aidx;
+    int row_index = -1, col_index = -1;
+    for (int l = 0; l < T.n; ++l) {
+      row_pass(l, 0, amax, aidx);
+      if (amax > 1e-16) {
+        row_index = l;
+        col_index = aidx;
+        break;
+      }
+    }
+    int status = 0;
+    int r = 0;
+    if (row_index >= 0) {
+      const double pivot0 = V[col_index];
+      if (lane == 0) used_r[row_index] = 1;
+      __syncwarp();
+      col_pass(col_index, 0, pivot0, amax, aidx);
+      if (lane == 0) {
+        rows[0] = row_index;
+        cols[0] = col_index;
+        used_c[col_index] = 1;
+      }
+      int next_row = aidx;
+      r = 1;
+      // norms of the first pair of vectors (loop test, src/ACA.cpp:178)
+      double nu = sqrt(warp_canonical_dot(U, U, T.n, lane));
+      double nv = sqrt(warp_canonical_dot(V, V, T.m, lane));
+      double normS = 0.0;
+      __syncwarp();
+      row_index = next_row;
+      for (;;) {
+        if (bad) {
+          status = 2;
+          break;
+        }
+        if (!(__dmul_rn(nu, nv) > __dmul_rn(tol, normS) && r < mn)) break;
+        if (r >= T.cap) {
+          status = 1;
+          break;
+        }
+        for (int l = lane; l < r; l += 32) ubuf[l] = U[(size_t)l * T.n + row_index];
+        __syncwarp();
+        row_pass(row_index, r, amax, aidx);
+        col_index = aidx;
+        const double pivot = V[(size_t)r * T.m + col_index];
+        for (int l = lane; l < r; l += 32) vbuf[l] = V[(size_t)l * T.m + col_index];
+        if (lane == 0) used_r[row_index] = 1;
+        __syncwarp();
+        col_pass(col_index, r, pivot, amax, aidx);
+        next_row = aidx;
+        const double* un = U + (size_t)r * T.n;
+        const double* vn = V + (size_t)r * T.m;
+        const double nu2 = warp_canonical_dot(un, un, T.n, lane);
+        const double nv2 = warp_canonical_dot(vn, vn, T.m, lane);
+        if (lane == 0) {
+          du[r] = nu2;
+          dv[r] = nv2;
+        }
+        nu = sqrt(nu2);
+        nv = sqrt(nv2);
+        if (bad) {
+          status = 2;
+          break;
+        }
+        if (nu < 1e-16 || nv < 1e-16) break;  // src/ACA.cpp:199-203
+        if (lane == 0) {
+          rows[r] = row_index;
+          cols[r] = col_index;
+          used_c[col_index] = 1;
+        }
+        // dot products with every kept vector (src/ACA.cpp:212-214)
+        for (int l = 0; l < r; ++l) {
+          const double a = warp_canonical_dot(U + (size_t)l * T.n, un, T.n, lane);
+          const double c = warp_canonical_dot(V + (size_t)l * T.m, vn, T.m, lane);
+          if (lane == 0) {
+            du[l] = a;
+            dv[l] = c;
+          }
+        }
+        ++r;
+        __syncwarp();
+        double ns = 0.0;
+        if (lane == 0) {
+          const double p = __dmul_rn(nu, nv);
+          ns = __dadd_rn(__dmul_rn(normS, normS), __dmul_rn(p, p));
+          for (int l = 0; l < r; ++l) ns = __dadd_rn(ns, __dmul_rn(2.0, fabs(__dmul_rn(du[l], dv[l]))));
+          ns = __dsqrt_rn(ns);
+        }
+        normS = __shfl_sync(0xffffffffu, ns, 0);
+        row_index = next_row;
+      }
+    } else if (bad) {
+      status = 2;
+    }
+    if (lane == 0) {
+      out_rank[ti] = r;
+      out_status[ti] = status;
+    }
+    __syncwarp();
+  }
+}
+
 // Copies the first r columns of U and V of every task into the final FP64
 // pool at dst_off: U (n x r) then V (m x r), column-major.  (The FP32 copies
 // are written after the assembly, grouped by box: k_u32, k_v32.)
@@ -349,6 +544,20 @@ cudaError_t launch_aca(cudaStream_t s, int block, int grid, const AcaTask* tasks
     k_aca<256><<<grid, 256, shm, s>>>(tasks, ntasks, counter, P, kd, tol, ws, flags, piv,
                                        out_rank, out_status);
   }
+  return cudaGetLastError();
+}
+
+size_t aca_warp_shared_bytes(int cap_max) { return (size_t)kAcaWarpsPerBlock * 4 * cap_max * sizeof(double); }
+
+cudaError_t launch_aca_warp(cudaStream_t s, int grid, const AcaTask* tasks, int ntasks, int* counter,
+                            PointsF64 P, KernelDesc kd, double tol, double* ws, unsigned char* flags,
+                            int32_t* piv, int32_t* out_rank, int32_t* out_status, int cap_max) {
+  const size_t shm = aca_warp_shared_bytes(cap_max);
+  cudaError_t e = cudaFuncSetAttribute(k_aca_warp<kAcaWarpsPerBlock>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  if (e != cudaSuccess) return e;
+  k_aca_warp<kAcaWarpsPerBlock><<<grid, 32 * kAcaWarpsPerBlock, shm, s>>>(
+      tasks, ntasks, counter, P, kd, tol, cap_max, ws, flags, piv, out_rank, out_status);
   return cudaGetLastError();
 }
 

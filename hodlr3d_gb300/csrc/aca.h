@@ -27,6 +27,14 @@ struct AcaTask {
 enum AcaStatus { kAcaOk = 0, kAcaCapReached = 1, kAcaNonFinite = 2 };
 
 size_t aca_shared_bytes(int cap_max);
+// One warp per pair (pairs of at most 128 points a side): kAcaWarpsPerBlock
+// warps per block, `grid` persistent blocks; same results as launch_aca.
+constexpr int kAcaWarpsPerBlock = 4;
+constexpr int kAcaWarpBlocksPerSm = 8;  // 32 pairs per SM at 64 registers
+size_t aca_warp_shared_bytes(int cap_max);
+cudaError_t launch_aca_warp(cudaStream_t s, int grid, const AcaTask* tasks, int ntasks, int* counter,
+                            PointsF64 P, KernelDesc kd, double tol, double* ws, unsigned char* flags,
+                            int32_t* piv, int32_t* out_rank, int32_t* out_status, int cap_max);
 cudaError_t launch_aca(cudaStream_t s, int block, int grid, const AcaTask* tasks, int ntasks,
                        int* counter, PointsF64 P, KernelDesc kd, double tol, double* ws,
                        unsigned char* flags, int32_t* piv, int32_t* out_rank, int32_t* out_status,

@@ -437,15 +437,34 @@ int aca_launch(hodlr3d_t h, AcaLane& L, std::vector<HostTask>&& batch, bool smal
   L.pv = pv;
   H3D_CUDA(cudaMemcpyAsync(L.d_tasks.p, L.tasks.data(), sizeof(h3d::AcaTask) * nt, cudaMemcpyHostToDevice, s));
   H3D_CUDA(cudaMemsetAsync(L.d_counter.p, 0, sizeof(int32_t), s));
-  const int block = small_kernel ? 64 : 256;
+  h3d::PointsF64 P{h->xs.as<double>(), h->ys.as<double>(), h->zs.as<double>()};
+  if (small_kernel) {
+    // one warp per pair, no block barriers: 1.29 s for the 435,520 leaf
+    // pairs at 64^3 against 1.35 s in 64-thread blocks (about half of the
+    // FP64 floor of their operations either way)
+    const int wpb = h3d::kAcaWarpsPerBlock;
+    int per_sm = h3d::kAcaWarpBlocksPerSm;
+    const size_t wshm = h3d::aca_warp_shared_bytes(cap_max);
+    per_sm = std::max(1, std::min(per_sm, (int)((200 * 1024) / (wshm + 1024))));
+    const int grid = std::max(1, std::min((nt + wpb - 1) / wpb, h->num_sms * per_sm));
+    H3D_CUDA(cudaEventRecord(L.ev.a, s));
+    H3D_CUDA(h3d::launch_aca_warp(s, grid, L.d_tasks.as<h3d::AcaTask>(), nt, L.d_counter.as<int>(), P,
+                                  h->kd, h->tol, L.d_ws.as<double>(), L.d_fl.as<unsigned char>(),
+                                  L.d_pv.as<int32_t>(), L.d_rank.as<int32_t>(), L.d_status.as<int32_t>(),
+                                  cap_max));
+    H3D_CUDA(cudaEventRecord(L.ev.b, s));
+    ++h->launches;
+    return HODLR3D_OK;
+  }
+  // the larger pairs: 256-thread blocks, one per SM (k_aca's launch bounds)
+  const int block = 256;
   const size_t shm = h3d::aca_shared_bytes(cap_max);
-  int per_sm = small_kernel ? 16 : 1;  // as k_aca's launch bounds allow
+  int per_sm = 1;
   if (shm > 0) {
     const int by_shm = (int)std::max<size_t>(1, (200 * 1024) / (shm + 2048));
     per_sm = std::max(1, std::min(per_sm, by_shm));
   }
   const int grid = std::max(1, std::min(nt, h->num_sms * per_sm));
-  h3d::PointsF64 P{h->xs.as<double>(), h->ys.as<double>(), h->zs.as<double>()};
   H3D_CUDA(cudaEventRecord(L.ev.a, s));
   H3D_CUDA(h3d::launch_aca(s, block, grid, L.d_tasks.as<h3d::AcaTask>(), nt, L.d_counter.as<int>(), P,
                            h->kd, h->tol, L.d_ws.as<double>(), L.d_fl.as<unsigned char>(),
