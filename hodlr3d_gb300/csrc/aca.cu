@@ -101,13 +101,12 @@ __device__ void col_pass(const AcaTask& T, const PointsF64& P, const KernelDesc&
   block_argmax<BS>(bv, bi, S, amax, aidx);
 }
 
-// 64-thread blocks: 16 per SM at 64 registers (the leaf pairs run in
-// k_aca_warp, one warp each).  256-thread blocks (the larger pairs): one per
-// SM with all the registers they want (134, nothing spilled); held to 64
-// registers so that four fit, they spill and run slower: 5.8 s of ACA
-// kernels at 64^3 against 6.8-7.0 s.
+// The larger pairs (the leaf pairs run in k_aca_warp, one warp each):
+// 256-thread blocks, one per SM with all the registers they want (134,
+// nothing spilled); held to 64 registers so that four fit, they spill and
+// run slower: 5.8 s of ACA kernels at 64^3 against 6.8-7.0 s.
 template <int BS>
-__global__ void __launch_bounds__(BS, BS == 64 ? 16 : 1) k_aca(const AcaTask* __restrict__ tasks, int ntasks,
+__global__ void __launch_bounds__(BS, 1) k_aca(const AcaTask* __restrict__ tasks, int ntasks,
                                             int* __restrict__ counter, PointsF64 P, KernelDesc kd,
                                             double tol, double* __restrict__ ws,
                                             unsigned char* __restrict__ flags,
@@ -527,23 +526,14 @@ __global__ void k_v32(const double* const* __restrict__ v64, float* const* __res
 
 size_t aca_shared_bytes(int cap_max) { return (size_t)4 * cap_max * sizeof(double); }
 
-cudaError_t launch_aca(cudaStream_t s, int block, int grid, const AcaTask* tasks, int ntasks,
-                       int* counter, PointsF64 P, KernelDesc kd, double tol, double* ws,
-                       unsigned char* flags, int32_t* piv, int32_t* out_rank, int32_t* out_status,
-                       int cap_max) {
+cudaError_t launch_aca(cudaStream_t s, int grid, const AcaTask* tasks, int ntasks, int* counter,
+                       PointsF64 P, KernelDesc kd, double tol, double* ws, unsigned char* flags,
+                       int32_t* piv, int32_t* out_rank, int32_t* out_status, int cap_max) {
   const size_t shm = aca_shared_bytes(cap_max);
-  cudaError_t e;
-  if (block == 64) {
-    e = cudaFuncSetAttribute(k_aca<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-    if (e != cudaSuccess) return e;
-    k_aca<64><<<grid, 64, shm, s>>>(tasks, ntasks, counter, P, kd, tol, ws, flags, piv, out_rank,
-                                     out_status);
-  } else {
-    e = cudaFuncSetAttribute(k_aca<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-    if (e != cudaSuccess) return e;
-    k_aca<256><<<grid, 256, shm, s>>>(tasks, ntasks, counter, P, kd, tol, ws, flags, piv,
-                                       out_rank, out_status);
-  }
+  cudaError_t e = cudaFuncSetAttribute(k_aca<kAcaBlock>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  if (e != cudaSuccess) return e;
+  k_aca<kAcaBlock><<<grid, kAcaBlock, shm, s>>>(tasks, ntasks, counter, P, kd, tol, ws, flags, piv,
+                                                out_rank, out_status);
   return cudaGetLastError();
 }
 

@@ -35,10 +35,11 @@ size_t aca_warp_shared_bytes(int cap_max);
 cudaError_t launch_aca_warp(cudaStream_t s, int grid, const AcaTask* tasks, int ntasks, int* counter,
                             PointsF64 P, KernelDesc kd, double tol, double* ws, unsigned char* flags,
                             int32_t* piv, int32_t* out_rank, int32_t* out_status, int cap_max);
-cudaError_t launch_aca(cudaStream_t s, int block, int grid, const AcaTask* tasks, int ntasks,
-                       int* counter, PointsF64 P, KernelDesc kd, double tol, double* ws,
-                       unsigned char* flags, int32_t* piv, int32_t* out_rank, int32_t* out_status,
-                       int cap_max);
+// One block of kAcaBlock threads per pair, `grid` persistent blocks.
+constexpr int kAcaBlock = 256;
+cudaError_t launch_aca(cudaStream_t s, int grid, const AcaTask* tasks, int ntasks, int* counter,
+                       PointsF64 P, KernelDesc kd, double tol, double* ws, unsigned char* flags,
+                       int32_t* piv, int32_t* out_rank, int32_t* out_status, int cap_max);
 cudaError_t launch_aca_compact(cudaStream_t s, int ntasks, const AcaTask* tasks,
                                const int32_t* rank, const int64_t* dst_off, const double* ws,
                                double* out64);

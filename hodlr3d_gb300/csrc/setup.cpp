@@ -456,8 +456,7 @@ int aca_launch(hodlr3d_t h, AcaLane& L, std::vector<HostTask>&& batch, bool smal
     ++h->launches;
     return HODLR3D_OK;
   }
-  // the larger pairs: 256-thread blocks, one per SM (k_aca's launch bounds)
-  const int block = 256;
+  // the larger pairs: kAcaBlock-thread blocks, one per SM (k_aca's launch bounds)
   const size_t shm = h3d::aca_shared_bytes(cap_max);
   int per_sm = 1;
   if (shm > 0) {
@@ -466,7 +465,7 @@ int aca_launch(hodlr3d_t h, AcaLane& L, std::vector<HostTask>&& batch, bool smal
   }
   const int grid = std::max(1, std::min(nt, h->num_sms * per_sm));
   H3D_CUDA(cudaEventRecord(L.ev.a, s));
-  H3D_CUDA(h3d::launch_aca(s, block, grid, L.d_tasks.as<h3d::AcaTask>(), nt, L.d_counter.as<int>(), P,
+  H3D_CUDA(h3d::launch_aca(s, grid, L.d_tasks.as<h3d::AcaTask>(), nt, L.d_counter.as<int>(), P,
                            h->kd, h->tol, L.d_ws.as<double>(), L.d_fl.as<unsigned char>(),
                            L.d_pv.as<int32_t>(), L.d_rank.as<int32_t>(), L.d_status.as<int32_t>(),
                            cap_max));
