@@ -589,9 +589,9 @@ int run_tc(hodlr3d_t h, const h3d::FarOp& far, const h3d::NearOp& nr, const doub
 }
 
 // largest column counts the few-column engine takes in the automatic choice
-// (measured at 64^3: 5.7 ms for 4 columns against 10.4 ms for the tensor
-// cores' 32; transposed, 7.0 ms for 4 and 46 ms for 32 columns against 28
-// and 53 ms for the CUDA-core transpose)
+// (measured at 64^3: 5.7 ms for 4 columns and 11.3 ms for 8 against 6.9 ms
+// for the tensor cores' 32; transposed, 7.0 ms for 4 and 46 ms for 32
+// columns against 28 and 53 ms for the CUDA-core transpose)
 constexpr int kGemvForwardMax = 4;
 constexpr int kGemvTransposeMax = 32;
 // on trees the tensor-core engine does not take, passes of 4 columns beat the
