@@ -562,12 +562,15 @@ def run_ours(args):
         t = time.perf_counter()
         tune_rows = H.autotune(reps=3)
         ch = H.tuning()
+        launch = H.launch_tuning()
         H.autotune(reps=0)
         counts = (1, 2, 4, 8, 16, 32, 64)
         tune = {"seconds": time.perf_counter() - t,
                 "forward": {n: ch["forward"][n - 1] for n in counts},
                 "transpose": {n: ch["transpose"][n - 1] for n in counts},
-                "ms": {f"{'AT' if tr else 'A'}_{n}_{e}": round(ms, 3) for tr, n, e, ms in tune_rows}}
+                "ms": {f"{'AT' if tr else 'A'}_{n}_{e}": round(ms, 3) for tr, n, e, ms in tune_rows},
+                "ta_split_ms": {k: round(v, 3) for k, v in launch["ta_split"].items()},
+                "ta_split_chosen": launch["ta_split_chosen"]}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -182,6 +182,8 @@ int hodlr3d_matvec_host(hodlr3d_t h, const double* x, double* y, int nrhs, int64
   H3D_TRY(check_handle(h));
   if (!x || !y) return set_error(HODLR3D_ERR_INVALID_ARG, "null vector");
   if (nrhs < 1 || nrhs > 64 || ld < h->N) return set_error(HODLR3D_ERR_INVALID_ARG, "bad nrhs or ld");
+  // products still in flight on the caller's streams use the same work buffers
+  H3D_CUDA(cudaDeviceSynchronize());
   const size_t bytes = sizeof(double) * h->N * nrhs;
   H3D_CUDA(h->stage_x.ensure(bytes));
   H3D_CUDA(h->stage_y.ensure(bytes));
@@ -201,6 +203,8 @@ int hodlr3d_matvec_host_rows(hodlr3d_t h, const double* x, double* y, int nrhs, 
   H3D_TRY(check_handle(h));
   if (!x || !y) return set_error(HODLR3D_ERR_INVALID_ARG, "null vector");
   if (nrhs < 1 || nrhs > 64) return set_error(HODLR3D_ERR_INVALID_ARG, "bad nrhs");
+  // products still in flight on the caller's streams use the same work buffers
+  H3D_CUDA(cudaDeviceSynchronize());
   const size_t bytes = sizeof(double) * h->N * nrhs;
   H3D_CUDA(h->stage_x.ensure(bytes));
   H3D_CUDA(h->stage_y.ensure(bytes));
@@ -277,8 +281,10 @@ int hodlr3d_gmres(hodlr3d_t h, const double* b, double* x, int nrhs, int64_t ld,
   if (!h->assembled) return set_error(HODLR3D_ERR_NOT_ASSEMBLED, "hodlr3d_assemble has not run");
   if (!b || !x || !prm || nrhs < 1 || nrhs > 64 || ld < h->N || prm->maxit < 1 || !(prm->tol > 0))
     return set_error(HODLR3D_ERR_INVALID_ARG, "bad GMRES arguments");
-  // inputs may still be in flight on the caller's stream
+  // inputs may still be in flight on the caller's stream, and products on
+  // the caller's streams use the same work buffers
   H3D_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  H3D_CUDA(cudaDeviceSynchronize());
   cudaStream_t s = h->stream;
   const int64_t N = h->N;
   const int64_t vec = N * nrhs;
@@ -543,6 +549,8 @@ int hodlr3d_set_engine(hodlr3d_t h, int engine) try {
 int hodlr3d_autotune(hodlr3d_t h, int reps, char* report, int cap) try {
   H3D_TRY(check_handle(h));
   if (reps < 0 || reps > 1000) return set_error(HODLR3D_ERR_INVALID_ARG, "reps must be in 0..1000");
+  // products still in flight on the caller's streams use the same work buffers
+  H3D_CUDA(cudaDeviceSynchronize());
   std::string rep;
   H3D_TRY(autotune(h, reps, rep));
   if (report && cap > 0) {

@@ -209,6 +209,9 @@ struct hodlr3d_handle {
   // automatic choice for the mixed product, per (transpose, nrhs), from the
   // timings of hodlr3d_autotune: 0 = the column-count rules, else an engine
   int8_t tuned[2][65] = {};
+  // blocks per level d-1 slice of the tensor-core T kernel chosen by
+  // hodlr3d_autotune (0: the rule of launch_matvec_tc)
+  int tc_split = 0;
   DevBuf dev_err;   // set by kernels whose bounded waits gave up
   bool leaves_aligned = false;  // every leaf population a multiple of 4
   DevBuf knear, near_off;       // FP32 near-field blocks of the tensor-core engine

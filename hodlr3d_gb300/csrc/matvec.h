@@ -110,6 +110,7 @@ struct TcBuffers {
   float* xt;
   float* t;
   int64_t lo_off;  // the low parts of X and T, lo_off floats after them
+  int ta_split;    // blocks per slice of the T kernel (0: the default rule)
   float* p;
   double* ynl;
   int* err;

@@ -1393,7 +1393,9 @@ int launch_matvec_tc(cudaStream_t s, int64_t N, const int32_t* perm, const FarOp
     // T of the pairs above the leaves, then their U T: level sums in Ynl
     const int64_t nslice = int64_t(1) << (3 * (d - 1));
     // several blocks share a slice's row tiles when slices are few
-    const int split = (int)std::max<int64_t>(1, std::min<int64_t>(32, (16 * 152) / nslice));
+    // (the default: about 16 blocks per SM in all; hodlr3d_autotune may pick another)
+    const int split = B.ta_split > 0 ? std::min(B.ta_split, 64)
+                                     : (int)std::max<int64_t>(1, std::min<int64_t>(32, (16 * 152) / nslice));
     k_ta_tc<true><<<dim3((unsigned)nslice, (unsigned)split), THREADS, SMEM_BYTES, s>>>(
         far, vmaps, B.xt, N, B.t, B.p, B.lo_off, B.err);
     ++launches;

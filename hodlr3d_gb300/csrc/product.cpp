@@ -567,6 +567,7 @@ int run_tc(hodlr3d_t h, const h3d::FarOp& far, const h3d::NearOp& nr, const doub
   T.xt = h->tct.as<float>();
   T.t = T.xt + 32 * h->N;
   T.lo_off = xt_floats;
+  T.ta_split = h->tc_split;
   T.p = reinterpret_cast<float*>(h->pbuf.p);
   T.ynl = h->ynl.as<double>();
   T.err = h->dev_err.as<int>();
@@ -765,6 +766,7 @@ constexpr int kNumTuneCounts = sizeof(kTuneCounts) / sizeof(kTuneCounts[0]);
 // (hodlr3d_set_engine) is restored.
 int autotune(hodlr3d_t h, int reps, std::string& report) {
   std::memset(h->tuned, 0, sizeof h->tuned);
+  h->tc_split = 0;
   report.clear();
   if (reps == 0) return HODLR3D_OK;
   if (!h->assembled) return set_error(HODLR3D_ERR_NOT_ASSEMBLED, "hodlr3d_assemble has not run");
@@ -784,6 +786,28 @@ int autotune(hodlr3d_t h, int reps, std::string& report) {
   char line[160];
   report = "transpose nrhs engine ms\n";
   int st = HODLR3D_OK;
+  bool tc_runs = false;
+  // median of `reps` timed products (after one untimed) under the current
+  // engine and launch shapes
+  auto time_product = [&](int nrhs, bool tr, float& med) -> int {
+    int e2 = matvec_device(h, X.as<double>(), Y.as<double>(), nrhs, N, HODLR3D_MIXED, s, tr);
+    if (e2 != HODLR3D_OK) return e2;
+    std::vector<float> ms(reps);
+    for (int r = 0; r < reps; ++r) {
+      cudaError_t e = cudaEventRecord(ev.a, s);
+      if (e == cudaSuccess) {
+        e2 = matvec_device(h, X.as<double>(), Y.as<double>(), nrhs, N, HODLR3D_MIXED, s, tr);
+        if (e2 != HODLR3D_OK) return e2;
+        e = cudaEventRecord(ev.b, s);
+      }
+      if (e == cudaSuccess) e = cudaEventSynchronize(ev.b);
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[r], ev.a, ev.b);
+      if (e != cudaSuccess) return set_error(HODLR3D_ERR_CUDA, "autotune timing: %s", cudaGetErrorString(e));
+    }
+    std::sort(ms.begin(), ms.end());
+    med = ms[reps / 2];
+    return HODLR3D_OK;
+  };
   for (int tr = 0; tr < 2 && st == HODLR3D_OK; ++tr) {
     for (int ci = 0; ci < kNumTuneCounts && st == HODLR3D_OK; ++ci) {
       const int nrhs = kTuneCounts[ci];
@@ -811,6 +835,7 @@ int autotune(hodlr3d_t h, int reps, std::string& report) {
             st = set_error(HODLR3D_ERR_CUDA, "autotune timing: %s", cudaGetErrorString(e));
         }
         if (st != HODLR3D_OK) break;
+        if (eng == 2) tc_runs = true;
         std::sort(ms.begin(), ms.end());
         const float med = ms[reps / 2];
         std::snprintf(line, sizeof line, "%d %d %d %.6f\n", tr, nrhs, eng, med);
@@ -820,6 +845,32 @@ int autotune(hodlr3d_t h, int reps, std::string& report) {
           best = med;
         }
       }
+    }
+  }
+  // launch shapes: blocks per slice of the tensor-core T kernel (which tile
+  // each block multiplies; the results do not depend on it), 32 columns
+  if (st == HODLR3D_OK && tc_runs) {
+    h->engine = 2;
+    int best_split = 0;
+    float best = 0.f;
+    std::string lines;
+    for (int k : {1, 2, 4, 8, 16, 32}) {
+      h->tc_split = k;
+      float med = 0.f;
+      st = time_product(32, false, med);
+      if (st != HODLR3D_OK) break;
+      std::snprintf(line, sizeof line, "launch ta_split %d %.6f\n", k, med);
+      lines += line;
+      if (best_split == 0 || med < best) {
+        best_split = k;
+        best = med;
+      }
+    }
+    h->tc_split = st == HODLR3D_OK ? best_split : 0;
+    report += lines;
+    if (st == HODLR3D_OK) {
+      std::snprintf(line, sizeof line, "launch ta_split_chosen %d %.6f\n", best_split, best);
+      report += line;
     }
   }
   h->engine = forced;

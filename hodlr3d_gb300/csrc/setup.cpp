@@ -649,6 +649,7 @@ int finish_assembly(hodlr3d_t h, double t_start) {
   const double t_finish = now_s();
   const int64_t np = h->npairs;
   std::memset(h->tuned, 0, sizeof h->tuned);  // timings of another operator
+  h->tc_split = 0;
   if (h->opt.keep_fp32) H3D_TRY(group_fp32(h));
   // per-pair tables for the matvec: T offsets, slice work items of the
   // non-leaf pairs, partial offsets of the pairs above level d - 1

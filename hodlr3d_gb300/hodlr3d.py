@@ -270,10 +270,24 @@ class HODLR3D:
         buf = ctypes.create_string_buffer(1 << 14)
         check(self._L.hodlr3d_autotune(self.handle, int(reps), buf, len(buf)))
         rows = []
+        self._launch = {"ta_split": {}, "ta_split_chosen": None}
         for line in buf.value.decode().splitlines()[1:]:
+            if line.startswith("launch "):
+                _, key, k, ms = line.split()
+                if key == "ta_split":
+                    self._launch["ta_split"][int(k)] = float(ms)
+                else:
+                    self._launch["ta_split_chosen"] = int(k)
+                continue
             t, n, e, ms = line.split()
             rows.append((bool(int(t)), int(n), self.ENGINES[int(e)], float(ms)))
         return rows
+
+    def launch_tuning(self) -> dict:
+        """The launch shapes the last autotune() timed on the tensor-core
+        engine: {"ta_split": {blocks per slice: ms}, "ta_split_chosen": k}
+        (None where it did not run)."""
+        return getattr(self, "_launch", {"ta_split": {}, "ta_split_chosen": None})
 
     def tuning(self) -> dict:
         """The automatic engine per column count after autotune():

@@ -244,7 +244,11 @@ int hodlr3d_set_engine(hodlr3d_t h, int engine);
  * one up.  Blocks the calling thread; allocates two n x 64 work arrays for
  * its duration.  reps = 0 returns to the column-count rules; a new assembly
  * or load does too.  report (optional, cap bytes, NUL-terminated, truncated):
- * one line "transpose nrhs engine ms" per timing.  No reference counterpart. */
+ * one line "transpose nrhs engine ms" per timing, then the launch shapes it
+ * times on the tensor-core engine (32 columns): "launch ta_split k ms" for
+ * k = 1, 2, 4, 8, 16, 32 blocks per slice of its T kernel and
+ * "launch ta_split_chosen k ms" (the results do not depend on k).  No
+ * reference counterpart. */
 int hodlr3d_autotune(hodlr3d_t h, int reps, char* report, int cap);
 /* The automatic choice after hodlr3d_autotune: choice[64 t + nrhs - 1] for
  * t = 0 (A x) and 1 (A^T x), nrhs 1..64; an engine number, or 0 where the

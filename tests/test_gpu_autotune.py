@@ -86,3 +86,48 @@ def test_reset_bad_reps_and_loaded_operators(tmp_path):
     assert set(H.tuning()["forward"] + H.tuning()["transpose"]) == {None}
     G.close()
     H.close()
+
+
+def test_launch_shape_tuning(tuned):
+    """The tuner also times the tensor-core T kernel at 1..32 blocks per slice
+    (32 columns) and keeps the fastest; the product does not depend on it."""
+    H, _ = tuned
+    lt = H.launch_tuning()
+    assert set(lt["ta_split"]) == {1, 2, 4, 8, 16, 32}
+    assert all(v > 0 for v in lt["ta_split"].values())
+    k = lt["ta_split_chosen"]
+    assert lt["ta_split"][k] == min(lt["ta_split"].values())
+    g = torch.Generator(device="cpu").manual_seed(7)
+    X = torch.randn(H.N, 32, generator=g, dtype=torch.float64).cuda()
+    H.set_engine("tc")
+    try:
+        y_tuned = H.matvec(X, "mixed")
+        torch.cuda.synchronize()
+        rows = H.autotune(reps=0)  # back to the default launch shapes
+        assert rows == [] and H.launch_tuning()["ta_split_chosen"] is None
+        y_rule = H.matvec(X, "mixed")
+        torch.cuda.synchronize()
+        assert torch.equal(y_tuned, y_rule)
+    finally:
+        H.set_engine("auto")
+        H.autotune(reps=3)
+
+
+def test_tuner_waits_for_products_in_flight(tuned):
+    """A product queued on torch's stream, then the tuner (which runs its
+    products on the handle's stream with the same work buffers) before any
+    synchronisation: the queued product's result is still exact."""
+    H, _ = tuned
+    g = torch.Generator(device="cpu").manual_seed(8)
+    X = torch.randn(H.N, 32, generator=g, dtype=torch.float64).cuda()
+    H.set_engine("tc")
+    try:
+        ref = H.matvec(X, "mixed")
+        torch.cuda.synchronize()
+        y = H.matvec(X, "mixed")
+        H.autotune(reps=1)  # no synchronisation before it
+        torch.cuda.synchronize()
+        assert torch.equal(y, ref)
+    finally:
+        H.set_engine("auto")
+        H.autotune(reps=3)
