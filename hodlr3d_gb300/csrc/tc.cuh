@@ -1,15 +1,8 @@
 // tcgen05 (5th-generation tensor core) helpers for sm_103a: TMEM allocation,
-// shared-memory matrix descriptors, kind::tf32 MMA issue and commit,
-// mbarrier waits with an iteration limit, TMEM loads, and the 3xTF32 split.
-//
-// Operand tiles live in shared memory in the canonical K-major layout without
-// swizzling: 8-row x 16-byte core matrices (8 rows x 4 tf32), element
-// (row, k) at  (k / 4) * 128 + (row / 8) * SBO + (row % 8) * 16 + (k % 4) * 4
-// with SBO = (KC / 4) * 128 for a tile of KC k-columns; the descriptor's
-// leading byte offset (between core matrices adjacent in K) is 128 and its
-// stride byte offset (between 8-row groups) is SBO.  One MMA consumes K = 8
-// (two core matrices along K): successive K steps advance the start address
-// by 256 bytes.
+// the kind::tf32 instruction descriptor, MMA issue with A in tensor memory and
+// commit, mbarrier waits with a bound, TMEM loads and stores.  The operand
+// layouts (128-byte swizzled K-major tiles) and their shared-memory
+// descriptors are defined where they are used (matvec_tc.cu).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -19,22 +12,6 @@ namespace tc {
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-// byte offset of (row, k) in a K-major tile with kc k-columns
-__device__ __forceinline__ uint32_t kmajor_off(int row, int k, int kc) {
-  return (uint32_t)((k >> 2) * 128 + (row >> 3) * (kc * 32) + (row & 7) * 16 + (k & 3) * 4);
-}
-
-// Shared-memory matrix descriptor: start >> 4 in bits 0-13, leading byte
-// offset >> 4 in 16-29, stride byte offset >> 4 in 32-45, descriptor version
-// 1 (bits 46-47), base offset 0, no swizzle (layout type 0 in bits 61-63).
-__device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-  d |= (uint64_t)1 << 46;
-  return d;
 }
 
 // Instruction descriptor of kind::tf32: D FP32 (bits 4-5 = 1), A and B TF32
@@ -56,16 +33,6 @@ __device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols) {
 __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
   asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" :: "r"(taddr), "r"(ncols)
                : "memory");
-}
-
-// D[tmem] (+)= A[desc] * B[desc], issued by one thread
-__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,
-                                         uint32_t idesc, uint32_t accumulate) {
-  asm volatile(
-      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n"
-      :: "r"(dtmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-      : "memory");
 }
 
 // D[tmem] (+)= A[tmem] * B[desc]: A in tensor memory (M rows in lanes, one
@@ -95,25 +62,10 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" :: "r"(smem_addr(bar)) : "memory");
 }
 
-// Waits for the phase with the given parity to complete; gives up after
-// `limit` polls (each poll itself blocks for a bounded, hardware-chosen
-// time) and returns false.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
-  const uint32_t a = smem_addr(bar);
-  for (uint32_t it = 0; it < limit; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        "selp.b32 %0, 1, 0, p;\n}\n"
-        : "=r"(done) : "r"(a), "r"(parity) : "memory");
-    if (done) return true;
-  }
-  return false;
-}
-
-// Same, with each poll suspending the thread for up to hint_ns nanoseconds
-// (it resumes when the phase completes): waiting warps leave the issue slots
-// to the others.  Gives up after `limit` polls and returns false.
+// Waits for the phase with the given parity to complete, each poll
+// suspending the thread for up to hint_ns nanoseconds (it resumes when the
+// phase completes): waiting warps leave the issue slots to the others.  Gives
+// up after `limit` polls and returns false.
 __device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, uint32_t limit,
                                                 uint32_t hint_ns) {
   const uint32_t a = smem_addr(bar);
@@ -184,62 +136,9 @@ __device__ __forceinline__ void fence_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
 }
 
-// 32 consecutive FP32 columns of this thread's TMEM lane (warp w reads lanes
-// 32 (w % 4) .. + 31; taddr carries the lane base in bits 16-31)
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
-        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
-        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-// 16 consecutive FP32 columns of this thread's TMEM lane
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-// 8 consecutive FP32 columns of this thread's TMEM lane
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
-  uint32_t r[8];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
-                 "=r"(r[6]), "=r"(r[7])
-               : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
-}
-// stores 8 consecutive 32-bit columns of this thread's TMEM lane; the caller
-// waits with tmem_wait_st before the data is used
-__device__ __forceinline__ void tmem_st8(uint32_t taddr, const float* v) {
-  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};\n"
-               :: "r"(taddr), "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]),
-                  "f"(v[6]), "f"(v[7])
-               : "memory");
-}
-
-// stores 16 consecutive 32-bit columns of this thread's TMEM lane; the caller
-// waits with tmem_wait_st before the data is used
+// stores 16 consecutive 32-bit columns of this thread's TMEM lane (warp w
+// reaches lanes 32 (w % 4) .. + 31; taddr carries the lane base in bits
+// 16-31); the caller waits with tmem_wait_st before the data is used
 __device__ __forceinline__ void tmem_st16(uint32_t taddr, const float* v) {
   asm volatile(
       "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
@@ -288,16 +187,6 @@ __device__ __forceinline__ void tmem_ld16x2(uint32_t a0, uint32_t a1, float* v0,
 
 __device__ __forceinline__ void tmem_wait_st() {
   asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
-}
-
-// x = hi + lo with hi, lo representable in TF32 (round to nearest)
-__device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
-  uint32_t h, l;
-  asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(h) : "f"(x));
-  const float r = x - __uint_as_float(h);
-  asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(l) : "f"(r));
-  hi = __uint_as_float(h);
-  lo = __uint_as_float(l);
 }
 
 }  // namespace tc
