@@ -29,6 +29,26 @@ def _prec(p) -> int:
         raise ValueError(f"precision must be 'fp64', 'mixed' or 'fp64x', got {p!r}") from None
 
 
+def parse_tune_report(text: str, engines) -> tuple:
+    """The report of hodlr3d_autotune (include/hodlr3d.h): a header line, one
+    "transpose nrhs engine ms" line per engine timing, then "launch ta_split k
+    ms" lines and "launch ta_split_chosen k ms".  Returns ([(transpose, nrhs,
+    engine name, ms)], {"ta_split": {k: ms}, "ta_split_chosen": k or None})."""
+    rows = []
+    launch = {"ta_split": {}, "ta_split_chosen": None}
+    for line in text.splitlines()[1:]:
+        if line.startswith("launch "):
+            _, key, k, ms = line.split()
+            if key == "ta_split":
+                launch["ta_split"][int(k)] = float(ms)
+            elif key == "ta_split_chosen":
+                launch["ta_split_chosen"] = int(k)
+            continue
+        t, n, e, ms = line.split()
+        rows.append((bool(int(t)), int(n), engines[int(e)], float(ms)))
+    return rows, launch
+
+
 class HODLR3D:
     """The HODLR3D operator on one GPU (reference: src/HODLR3D.cpp:3-32).
 
@@ -269,18 +289,7 @@ class HODLR3D:
         ms) tuples."""
         buf = ctypes.create_string_buffer(1 << 14)
         check(self._L.hodlr3d_autotune(self.handle, int(reps), buf, len(buf)))
-        rows = []
-        self._launch = {"ta_split": {}, "ta_split_chosen": None}
-        for line in buf.value.decode().splitlines()[1:]:
-            if line.startswith("launch "):
-                _, key, k, ms = line.split()
-                if key == "ta_split":
-                    self._launch["ta_split"][int(k)] = float(ms)
-                else:
-                    self._launch["ta_split_chosen"] = int(k)
-                continue
-            t, n, e, ms = line.split()
-            rows.append((bool(int(t)), int(n), self.ENGINES[int(e)], float(ms)))
+        rows, self._launch = parse_tune_report(buf.value.decode(), self.ENGINES)
         return rows
 
     def launch_tuning(self) -> dict:
