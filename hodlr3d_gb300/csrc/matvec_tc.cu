@@ -215,16 +215,16 @@ static_assert(sizeof(PairRow) == ENTRY_BYTES, "entry");
 // Streams the chunks of src through the tensor cores, called by all THREADS
 // threads of the block.  src: ntile tiles of cpt chunks; src.produce(c, a,
 // bar, lane), called by the 32 lanes of the producer warp, issues the A
-// copies of chunk c into a; src.load_b(c, slot, m) issues
-// this worker's B copy of chunk c (both called for c = 0, 1, ... in order);
+// copies of chunk c into a; src.load_b(c, slot, lane, i0) issues this
+// worker's B copies of chunk c (both called for c = 0, 1, ... in order);
 // every worker calls src.finish(tile, sum, comp, cross) once a tile's
 // products are summed (the tile's value is (sum - comp) + cross).  Returns the
 // number of chunks.
 //
 // A bounded wait that gives up sets the error flag and *abortp: every role
-// then stops issuing copies and products, the issuers wait (bounded) for
-// their products in flight and the producer for its copies in flight, and
-// no tile is finished, before the block frees its tensor memory.
+// then stops issuing copies and products, the issuer waits (bounded) for its
+// products in flight and the producer for its copies in flight, and no tile
+// is finished, before the block frees its tensor memory.
 __device__ __forceinline__ void stream_give_up(int* err, volatile int* abortp) {
   atomicExch(err, 1);
   *abortp = 1;
@@ -1076,13 +1076,14 @@ __global__ void k_row_blocks(const int32_t* __restrict__ leaf_off, NearOp nr,
 // sums of the levels above (Ynl, d >= 2); owner write of the leaf's rows in
 // the original order.
 //
-// Pipeline: the producer keeps up to kASlots A tiles in flight; the workers
-// split tile c into tensor memory (hi = the value itself, which the tensor
-// core reads as TF32, and lo = its remainder; A buffer c % 2), which frees
-// its shared-memory slot at once, write the low part of B, read back the
-// accumulators of chunk c - 1, copy B of chunk c + 1 into the B slot chunk
-// c - 1 used, and signal "ready"; the issuers multiply chunk c into the one
-// accumulator set.
+// Pipeline: the producer keeps up to kASlots A tiles in flight; per chunk c
+// the workers wait for the products of chunk c - 2 and read its accumulator
+// back, copy B of chunk c + 1 into the B slot chunk c - 2 used, split tile c
+// into tensor memory (hi = the value itself, which the tensor core reads as
+// TF32, and lo = its remainder; A buffer c % 2), which frees its
+// shared-memory slot at once, write the low part of B, and signal "ready";
+// the issuer multiplies chunk c into accumulator c % 2 while the workers
+// move on to chunk c + 1.
 __global__ void __launch_bounds__(lr::THREADS, 1) k_leaf_rows_tc(
     const int32_t* __restrict__ leaf_off, const LeafBlock* __restrict__ blocks,
     const int32_t* __restrict__ block_ptr, const CUtensorMap* __restrict__ rmaps,
