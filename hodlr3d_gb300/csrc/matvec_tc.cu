@@ -956,17 +956,16 @@ __global__ void k_near_lo(const int32_t* __restrict__ leaf_off, NearOp nr,
 // over its own 64-wide K range, and B = [X_top | X_bottom] (64 columns): the
 // wanted products are the diagonal quarters of D (rows 0..63 x columns 0..31,
 // rows 64..127 x columns 32..63); both halves add to the leaf's rows and are
-// combined at the end.  Per K = 8 step one issuer multiplies A_hi (the loaded
-// FP32 tile itself, read by the tensor core as TF32 from the 128-byte
-// swizzled shared memory) by [B_hi | B_lo] (N = 128), the other A_lo (tensor
-// memory) by B_hi (N = 64).  Accumulation groups are one chunk (8 MMAs per
-// accumulator), read back and summed with compensated FP32 additions: the
-// truncating FP32 accumulation of the tensor core stays below 1e-6 of
-// same-sign sums.
+// combined at the end.  Per K = 8 step the issuer multiplies A_hi (tensor
+// memory) by [B_hi | B_lo] (N = 128), then A_lo (tensor memory) by B_hi
+// (N = 64) onto the hi*lo columns.  Accumulation groups are one chunk (8
+// hi*hi MMAs per accumulator, two accumulators), read back and summed with
+// compensated FP32 additions: the truncating FP32 accumulation of the tensor
+// core stays below 1e-6 of same-sign sums.
 //
 // Every mbarrier wait is bounded.  A wait that gives up sets the error flag
 // and the block-wide abort flag: no role issues new copies or products after
-// that, the issuers wait (bounded) for their products in flight and the
+// that, the issuer waits (bounded) for its products in flight and the
 // producer for its copies in flight before the block frees its tensor memory
 // and exits.
 namespace lr {
